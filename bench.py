@@ -1,0 +1,368 @@
+#!/usr/bin/env python
+"""Benchmark: BiCGStab time to true relative residual 1e-10 on one GB300 (per rank).
+
+Workload (the configuration the headline metric is quoted on): the random banded 450,000-row
+nonsymmetric CSR system -- diagonal + 10 entries in a +-64 band + 6 uniform off-band entries per
+row (7.65M nonzeros, int32 indices, FP64 values), x_target ~ N(0,1) seed 1, b = A x_target,
+x0 = 0 -- generated by hethyppar_gb300.synth (seeded; no dataset is needed).
+
+One step = one full FP64 solve to rtol 1e-10 through the library (graph-captured loop).
+  value     device time per solve, inputs resident in HBM (hhp_bicgstab_dev), CUDA events on the
+            library's stream, L2 flushed (256 MiB write) before every step
+  e2e       the same solve through the host-buffer C ABI (hhp_bicgstab): b and x0 copied in from
+            pinned host memory and x copied out inside the timed region
+  roofline  the dominant kernel (the FP64 SpMV) timed alone, L2 flushed: algorithmic bytes
+            12*nnz + 20*m per launch / CUDA-event time, against the measured HBM copy peak
+  cpu_baseline  the reference's CPU BiCGStab restated (oracle/): its MPI-rank decomposition with
+            ranks as threads on all host cores, at the reference's own iteration count to 1e-10
+Extras (--extras, on by default): the mixed-precision form against FP64 on the 3D 160^3
+convection-diffusion system, and forward + adjoint on the 2D 1024^2 system.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--no-extras]
+For N > 1 run under torchrun: every rank solves its own replica (the solve is not sharded).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "BiCGStab time to rel-res 1e-10 (mixed vs FP64); SpMV GB/s/HBM peak; fwd+adj s"
+WORKLOAD = "c2: banded random 450000x450000, 17 nnz/row (7.65M nnz), FP64, int32 CSR, rtol 1e-10, x0=0"
+DATA = "synthetic, seeded (hethyppar_gb300.synth); stands in for cage13-scale SuiteSparse inputs"
+FLUSH_BYTES = 256 << 20
+RTOL = 1e-10
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampled every 200 ms while the timed region runs."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = []
+        for line in open(self.f.name):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 8:
+                rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return float("nan")
+        sm = [num(r[0]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[4 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(num(r[1]) for r in rows),
+                "power_w_max": max(num(r[2]) for r in rows), "samples": len(rows), "reasons": reasons}
+
+
+def cpu_reference_time(s, nthreads, k_ref):
+    """The reference's MPI-rank BiCGStab (ranks as threads) for k_ref iterations, seconds."""
+    from oracle import oracle as orc
+    t0 = time.perf_counter()
+    _, rr = orc.bicgstab_fixed_mt(s.rowptr, s.col, s.val, s.b, s.x0, k_ref, nthreads)
+    return time.perf_counter() - t0, rr
+
+
+def cpu_baseline(s, budget_s=20.0):
+    """Reference iteration count to 1e-10 (serial reference loop with a true-residual check per
+    iteration), then the multi-threaded reference form timed at that count, and a serial sample."""
+    from oracle import oracle as orc
+    nthreads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    k_ref, _, rr_ref = orc.iters_to_tol(s.rowptr, s.col, s.val, s.b, s.x0, RTOL, 5000)
+    t_find = time.perf_counter() - t0
+    t_mt, rr = cpu_reference_time(s, nthreads, max(k_ref, 1))
+    k_ser = max(1, min(k_ref, 20))
+    t0 = time.perf_counter()
+    orc.bicgstab_fixed(s.rowptr, s.col, s.val, s.b, s.x0, k_ser)
+    t_ser = (time.perf_counter() - t0) / k_ser * max(k_ref, 1)
+    return {"value": t_mt, "unit": "s", "cores": nthreads, "kind": "port",
+            "sample": f"full solve of the same system: reference BiCGStab loop (bicgstab_mpi.c decomposition, "
+                      f"{nthreads} threads as ranks) run for the reference's own iteration count to 1e-10 "
+                      f"({k_ref}, found by a serial run with per-iteration true residual in {t_find:.1f} s); "
+                      f"relres {rr:.2e}",
+            "iters_ref": k_ref, "relres_ref": rr_ref,
+            "serial_1core_s": t_ser, "serial_sample": f"{k_ser} iterations of bicgstab_cpu.c's loop, scaled to {k_ref}"}
+
+
+def run_reference_arm(args, rk):
+    from hethyppar_gb300 import synth
+    if rk.rank != 0:
+        return None
+    s = synth.config("c2")
+    from oracle import oracle as orc
+    nthreads = os.cpu_count() or 1
+    k_ref, _, rr_ref = orc.iters_to_tol(s.rowptr, s.col, s.val, s.b, s.x0, RTOL, 5000)
+    for _ in range(args.warmup):
+        cpu_reference_time(s, nthreads, k_ref)
+    times = []
+    for _ in range(args.steps):
+        t, rr = cpu_reference_time(s, nthreads, k_ref)
+        times.append(t)
+    v = statistics.mean(times)
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": DATA,
+            "config": {"workload": WORKLOAD, "m": s.m, "nnz": s.nnz, "rtol": RTOL, "parallelism": "cpu threads"},
+            "iters": k_ref, "rel_res_true": rr,
+            "cpu_baseline": {"value": v, "unit": "s", "cores": nthreads, "kind": "port",
+                             "sample": f"full solve per step: the reference's BiCGStab loop in its MPI-rank form "
+                                       f"(ranks as {nthreads} threads) for its own iteration count to 1e-10 ({k_ref})"},
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def traffic_from_profile():
+    """DRAM bytes per SpMV launch from the committed ncu summary (scaled to the full workload)."""
+    p = os.path.join(ROOT, "profiles", "spmv_fp64_banded450k_ncu.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+def run_ours(args, rk):
+    import torch
+    from hethyppar_gb300 import Context, Matrix, bicgstab, bicgstab_backward, spmv_bytes, synth
+    from hethyppar_gb300 import dist
+
+    dev = rk.local_rank
+    torch.cuda.set_device(dev)
+    ctx = Context(dev)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def flush_l2():
+        flush.add_(1.0)
+        torch.cuda.synchronize()
+
+    s = synth.config("c2")
+    A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
+    b_d = torch.as_tensor(s.b, device="cuda")
+    xt_d = torch.as_tensor(s.x_target, device="cuda")
+    x_d = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+
+    def solve_dev():
+        x_d.zero_()
+        torch.cuda.synchronize()
+        return bicgstab(ctx, A, b_d, x_d, xt_d, rtol=RTOL, maxit=5000)[1]
+
+    for _ in range(max(args.warmup, 3)):
+        res = solve_dev()
+    assert res.status == 0, res
+
+    # ---- timed region: K device-resident solves --------------------------------------------------
+    clocks = Clocks(dev)
+    launches0 = ctx.kernel_launches
+    dist.barrier(rk)
+    torch.cuda.synchronize()
+    step_ms = []
+    for _ in range(args.steps):
+        x_d.zero_()
+        flush_l2()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        res = bicgstab(ctx, A, b_d, x_d, xt_d, rtol=RTOL, maxit=5000)[1]
+        e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    dist.barrier(rk)
+    launches = ctx.kernel_launches - launches0
+    clk = clocks.stop()
+    t_solve = dist.max_over_ranks(rk, statistics.mean(step_ms) / 1e3)
+
+    # ---- e2e: host buffers through hhp_bicgstab (H2D b, x0; D2H x) ---------------------------------
+    b_h = torch.empty(s.n, dtype=torch.float64, pin_memory=True).numpy()
+    b_h[:] = s.b
+    x_h = torch.empty(s.n, dtype=torch.float64, pin_memory=True).numpy()
+    e2e = []
+    for _ in range(max(3, args.steps // 2)):
+        x_h[:] = 0.0
+        flush_l2()
+        t0 = time.perf_counter()
+        x_out, r2 = bicgstab(ctx, A, b_h, x_h, None, rtol=RTOL, maxit=5000)
+        e2e.append(time.perf_counter() - t0)
+    assert r2.status == 0
+    t_e2e = dist.max_over_ranks(rk, statistics.median(e2e))
+
+    # ---- roofline: the FP64 SpMV alone ----------------------------------------------------------
+    xs = torch.randn(s.n, dtype=torch.float64, device="cuda")
+    ys = torch.empty(s.m, dtype=torch.float64, device="cuda")
+    for _ in range(5):
+        A.spmv_dev(xs, ys)
+    torch.cuda.synchronize()
+    spmv_ms = []
+    for _ in range(30):
+        flush_l2()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        A.spmv_dev(xs, ys)
+        e1.record(stream)
+        e1.synchronize()
+        spmv_ms.append(e0.elapsed_time(e1))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(50):
+        A.spmv_dev(xs, ys)
+    e1.record(stream)
+    e1.synchronize()
+    warm_ms = e0.elapsed_time(e1) / 50
+    hbm, peak_kind = peaks()
+    bsp = spmv_bytes(s.m, s.n, s.nnz)
+    t_sp = statistics.median(spmv_ms) * 1e-3
+    achieved = bsp / t_sp / 1e9
+    traffic = traffic_from_profile()
+    roof = {"bound": "hbm", "kernel": "k_spmv<double> (FP64 CSR SpMV)", "achieved": achieved, "peak": hbm,
+            "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": traffic,
+            "algorithmic_bytes_per_launch": bsp, "launch_us": t_sp * 1e6,
+            "note": "algorithmic bytes 12*nnz+20*m per launch / median CUDA-event time, L2 flushed before each launch"}
+
+    out = {"metric": METRIC, "value": t_solve, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": False,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
+           "config": {"workload": WORKLOAD, "m": s.m, "nnz": s.nnz, "rtol": RTOL,
+                      "l2": "flushed before every timed step (256 MiB write)",
+                      "parallelism": f"replicas x{rk.world}" if rk.world > 1 else "single GPU"},
+           "iters": res.iters, "iters_per_s": res.iters / (statistics.mean(step_ms) / 1e3),
+           "rel_res_true": res.rel_res_true, "err_vs_target": res.err_vs_target,
+           "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": 2 * 8 * s.n, "d2h_bytes_per_step": 8 * s.n},
+           "roofline": roof,
+           "spmv": {"gbs_l2_flushed": achieved, "frac_of_hbm": achieved / hbm, "us_l2_flushed": t_sp * 1e6,
+                    "gbs_effective_warm_l2": bsp / (warm_ms * 1e-3) / 1e9, "us_warm": warm_ms * 1e3},
+           "clocks": clk, "gpu_launches": int(launches)}
+
+    # ---- extras: mixed vs FP64 (3D 160^3), forward + adjoint (2D 1024^2) ------------------------
+    if args.extras:
+        s4 = synth.config("c4")
+        A4 = Matrix.from_csr(ctx, s4.rowptr, s4.col, s4.val)
+        b4 = torch.as_tensor(s4.b, device="cuda")
+        t4 = torch.as_tensor(s4.x_target, device="cuda")
+
+        def timed(fn, reps):
+            ts, r = [], None
+            for _ in range(reps):
+                flush_l2()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                r = fn()
+                e1.record(stream)
+                e1.synchronize()
+                ts.append(e0.elapsed_time(e1) / 1e3)
+            return statistics.median(ts), r
+
+        x64 = torch.zeros_like(b4)
+        xm = torch.zeros_like(b4)
+        for prec, xx in (("fp64", x64), ("mixed", xm)):
+            xx.zero_()
+            bicgstab(ctx, A4, b4, xx, t4, rtol=RTOL, maxit=20000, precision=prec)
+
+        def run4(prec, xx):
+            xx.zero_()
+            return bicgstab(ctx, A4, b4, xx, t4, rtol=RTOL, maxit=20000, precision=prec)[1]
+        t64, r64 = timed(lambda: run4("fp64", x64), args.extra_reps)
+        tm, rm = timed(lambda: run4("mixed", xm), args.extra_reps)
+        out["mixed"] = {"workload": "c4: 3D 7-point upwind convection-diffusion 160^3 (4.096M rows, 28.5M nnz), Pe=20",
+                        "fp64_s": t64, "mixed_s": tm, "speedup": t64 / tm, "fp64_iters": r64.iters,
+                        "mixed_inner_iters": rm.iters, "mixed_outer": rm.outer_iters,
+                        "rel_res_true_fp64": r64.rel_res_true, "rel_res_true_mixed": rm.rel_res_true,
+                        "err_vs_target_fp64": r64.err_vs_target, "err_vs_target_mixed": rm.err_vs_target,
+                        "max_abs_mixed_minus_fp64": float((xm - x64).abs().max().item())}
+        del A4
+        s5 = synth.config("c5")
+        A5 = Matrix.from_csr(ctx, s5.rowptr, s5.col, s5.val)
+        b5 = torch.as_tensor(s5.b, device="cuda")
+        xt5 = torch.as_tensor(s5.x_target, device="cuda")
+        x5 = torch.zeros_like(b5)
+        bicgstab(ctx, A5, b5, x5, rtol=1e-12, maxit=50000)
+        bicgstab_backward(ctx, A5, x5, x5 - xt5, rtol=1e-12, maxit=50000)  # builds the transpose once
+
+        def fwd():
+            x5.zero_()
+            return bicgstab(ctx, A5, b5, x5, rtol=1e-12, maxit=50000)[1]
+
+        def adj():
+            return bicgstab_backward(ctx, A5, x5, x5 - xt5, rtol=1e-12, maxit=50000)[2]
+        tf, rf = timed(fwd, args.extra_reps)
+        ta, ra = timed(adj, args.extra_reps)
+        out["adjoint"] = {"workload": "c5: 2D 5-point convection-diffusion 1024^2 (1.05M rows, 5.24M nnz), Pe=30, "
+                                      "L = 1/2||x - x_t||^2, rtol 1e-12",
+                          "forward_s": tf, "adjoint_s": ta, "fwd_plus_adj_s": tf + ta, "ratio_total_to_forward":
+                          (tf + ta) / tf, "forward_iters": rf.iters, "adjoint_iters": ra.iters,
+                          "note": "transpose built once beforehand (not in the timed adjoint)"}
+
+    if rk.rank == 0 and rk.world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(s)
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-extras", dest="extras", action="store_false")
+    ap.add_argument("--extra-reps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    from hethyppar_gb300 import dist
+    rk = dist.init_from_env()
+    if args.impl == "reference":
+        out = run_reference_arm(args, rk)
+    else:
+        out = run_ours(args, rk)
+    if rk.rank == 0 and out is not None:
+        print(json.dumps(out), flush=True)
+    dist.finalize(rk)
+
+
+if __name__ == "__main__":
+    main()

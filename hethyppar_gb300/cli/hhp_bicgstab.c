@@ -1,0 +1,226 @@
+/*
+ * hhp-bicgstab -- command-line BiCGStab solve on one GB300 through libhhp_gpu.so.
+ *
+ * Drop-in for the reference's solver executables (src/entry/bicgstab_gpu_dp.c, bicgstab_cpu.c):
+ * the same argp flags (-m matrix, -x X_init, -y B, -o X_out, -n iterations), the same input
+ * files (Matrix Market, header-less vectors) and the same "key : value" stdout lines
+ * (n_iters, spmv, file_read, relative_residual, everything_total; bicgstab_cpu.c:261-273) that
+ * the reference's tooling parses. Additions: a tolerance and a real stop test (-n is then the
+ * iteration cap), the mixed-precision form, an X_target error report, a partition file applied
+ * as a row permutation, and per-iteration residual lines.
+ *
+ *   --rtol R          stop at ||b-Ax|| <= R ||b-Ax0|| (default 1e-10)
+ *   --fixed           run exactly -n iterations with no stop test, as the reference does
+ *   --precision P     fp64 (default) | mixed (FP32 inner solve, FP64 refinement)
+ *   --x-target FILE   report max |x - x_target|
+ *   --perm FILE       row partition vector (one part id per row); rows are grouped by part in
+ *                     increasing part order, as bicgstab_hybrid_dist_dp.c:221-233 orders them
+ *   --print-every K   print "Iteration = i; Error Norm = e" every K iterations
+ *                     (gpu_BiCGStab's per-iteration line, bicgstab_gpu.c:156)
+ *   --out-format F    compat (default, "%lf" like vector_write) | exact ("%.17g")
+ */
+#include <argp.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+#include <unistd.h>
+
+#include "hhp_gpu.h"
+
+enum { OPT_RTOL = 1000, OPT_FIXED, OPT_PREC, OPT_XT, OPT_PERM, OPT_PRINT, OPT_OUTFMT, OPT_DEVICE };
+
+struct arguments {
+    char *input_matrix, *input_x, *input_y, *output_x, *x_target, *perm;
+    int n_iters, fixed, mixed, print_every, exact, device;
+    double rtol;
+};
+
+static struct argp_option options[] = {
+    {"input-matrix", 'm', "FILE", 0, "Input matrix market file path", 0},
+    {"input-x", 'x', "FILE", 0, "Input X vector file path (initial guess)", 0},
+    {"input-y", 'y', "FILE", 0, "Input Y target vector file path (right-hand side B)", 0},
+    {"output-x", 'o', "FILE", 0, "Output X vector file path", 0},
+    {"n-iters", 'n', "POSITIVE-INTEGER", 0, "Iteration cap (exact count with --fixed)", 0},
+    {"rtol", OPT_RTOL, "R", 0, "Relative residual tolerance (default 1e-10)", 0},
+    {"fixed", OPT_FIXED, 0, 0, "Run exactly -n iterations without a stop test", 0},
+    {"precision", OPT_PREC, "fp64|mixed", 0, "Arithmetic of the solve", 0},
+    {"x-target", OPT_XT, "FILE", 0, "Known solution to report the error against", 0},
+    {"perm", OPT_PERM, "FILE", 0, "Row partition vector applied as a row permutation", 0},
+    {"print-every", OPT_PRINT, "K", 0, "Print the residual every K iterations", 0},
+    {"out-format", OPT_OUTFMT, "compat|exact", 0, "Number format of the output X file", 0},
+    {"device", OPT_DEVICE, "ID", 0, "CUDA device (default 0)", 0},
+    {0}};
+
+static error_t parse_opt(int key, char *arg, struct argp_state *state) {
+    struct arguments *a = state->input;
+    char *end = NULL;
+    switch (key) {
+        case 'm': a->input_matrix = arg; break;
+        case 'x': a->input_x = arg; break;
+        case 'y': a->input_y = arg; break;
+        case 'o': a->output_x = arg; break;
+        case 'n': a->n_iters = (int)strtol(arg, &end, 10); break;
+        case OPT_RTOL: a->rtol = strtod(arg, &end); break;
+        case OPT_FIXED: a->fixed = 1; break;
+        case OPT_PREC:
+            if (strcmp(arg, "mixed") == 0) a->mixed = 1;
+            else if (strcmp(arg, "fp64") == 0) a->mixed = 0;
+            else argp_error(state, "unknown precision '%s'", arg);
+            break;
+        case OPT_XT: a->x_target = arg; break;
+        case OPT_PERM: a->perm = arg; break;
+        case OPT_PRINT: a->print_every = (int)strtol(arg, &end, 10); break;
+        case OPT_OUTFMT:
+            if (strcmp(arg, "exact") == 0) a->exact = 1;
+            else if (strcmp(arg, "compat") == 0) a->exact = 0;
+            else argp_error(state, "unknown output format '%s'", arg);
+            break;
+        case OPT_DEVICE: a->device = (int)strtol(arg, &end, 10); break;
+        case ARGP_KEY_ARG: return 0;
+        default: return ARGP_ERR_UNKNOWN;
+    }
+    return 0;
+}
+
+static struct argp argp = {options, parse_opt, "", "BiCGStab on one GB300 (libhhp_gpu.so)", 0, 0, 0};
+
+static double now_s(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+static void print_iter(int iter, double rel, void *user) {
+    (void)user;
+    printf("  Iteration = %d; Error Norm = %e\n", iter, rel);
+}
+
+#define FAIL(...)                                  \
+    do {                                           \
+        fprintf(stderr, "hhp-bicgstab: " __VA_ARGS__); \
+        fprintf(stderr, "\n");                     \
+        return EXIT_FAILURE;                       \
+    } while (0)
+#define CHECK(call)                                                                                  \
+    do {                                                                                             \
+        hhp_status _s = (call);                                                                      \
+        if (_s != HHP_OK) FAIL("%s: %s (%s)", #call, hhp_status_str(_s), hhp_last_error());          \
+    } while (0)
+
+static int read_part(const char *path, int m, int *perm) {
+    FILE *f = fopen(path, "r");
+    if (!f) return -1;
+    int *part = malloc(sizeof(int) * (size_t)m);
+    int np = 0, v, maxp = 0;
+    while (np < m && fscanf(f, "%d", &v) == 1) {
+        if (v < 0) { fclose(f); free(part); return -1; }
+        part[np++] = v;
+        if (v > maxp) maxp = v;
+    }
+    fclose(f);
+    if (np != m) { free(part); return -1; }
+    int k = 0;
+    for (int p = 0; p <= maxp; ++p)
+        for (int i = 0; i < m; ++i)
+            if (part[i] == p) perm[k++] = i;
+    free(part);
+    return 0;
+}
+
+int main(int argc, char **argv) {
+    struct arguments a;
+    memset(&a, 0, sizeof a);
+    a.n_iters = 2000;
+    a.rtol = 1e-10;
+    argp_parse(&argp, argc, argv, 0, 0, &a);
+    if (!a.input_matrix || !a.input_x || !a.input_y || !a.output_x)
+        FAIL("-m, -x, -y and -o must all be specified");
+    if (access(a.input_matrix, F_OK) == -1) FAIL("Input matrix '%s' does not exist", a.input_matrix);
+    if (access(a.input_x, F_OK) == -1) FAIL("Input X '%s' does not exist", a.input_x);
+    if (access(a.input_y, F_OK) == -1) FAIL("Input B '%s' does not exist", a.input_y);
+    if (a.n_iters < 0) FAIL("-n must be >= 0");
+
+    const double t_begin = now_s();
+    hhp_ctx *ctx = NULL;
+    CHECK(hhp_ctx_create(a.device, &ctx));
+
+    const double t_read0 = now_s();
+    hhp_mat *A = NULL;
+    CHECK(hhp_mat_from_mtx(ctx, a.input_matrix, &A));
+    int m = 0, n = 0, nnz = 0;
+    CHECK(hhp_mat_shape(A, &m, &n, &nnz));
+    printf("Matrix name : %s\n", a.input_matrix);
+    if (m != n) FAIL("the matrix is %d x %d; BiCGStab needs a square matrix", m, n);
+    double *X = malloc(sizeof(double) * (size_t)n), *B = malloc(sizeof(double) * (size_t)m);
+    double *XT = NULL;
+    int *perm = NULL;
+    CHECK(hhp_vector_read(a.input_x, n, X));
+    CHECK(hhp_vector_read(a.input_y, m, B));
+    if (a.x_target) {
+        XT = malloc(sizeof(double) * (size_t)n);
+        CHECK(hhp_vector_read(a.x_target, n, XT));
+    }
+    if (a.perm) {
+        perm = malloc(sizeof(int) * (size_t)m);
+        if (read_part(a.perm, m, perm) != 0) FAIL("cannot read a %d-entry partition vector from '%s'", m, a.perm);
+        int *rp = malloc(sizeof(int) * ((size_t)m + 1)), *cl = malloc(sizeof(int) * (size_t)(nnz > 0 ? nnz : 1));
+        double *vl = malloc(sizeof(double) * (size_t)(nnz > 0 ? nnz : 1));
+        CHECK(hhp_mat_get_csr(A, rp, cl, vl));
+        hhp_mat_destroy(A);
+        A = NULL;
+        CHECK(hhp_mat_from_csr(ctx, m, n, nnz, rp, cl, vl, perm, &A));
+        free(rp); free(cl); free(vl);
+        double *tmp = malloc(sizeof(double) * (size_t)m);
+        for (int i = 0; i < m; ++i) tmp[i] = X[perm[i]];
+        memcpy(X, tmp, sizeof(double) * (size_t)m);
+        for (int i = 0; i < m; ++i) tmp[i] = B[perm[i]];
+        memcpy(B, tmp, sizeof(double) * (size_t)m);
+        if (XT) {
+            for (int i = 0; i < m; ++i) tmp[i] = XT[perm[i]];
+            memcpy(XT, tmp, sizeof(double) * (size_t)m);
+        }
+        free(tmp);
+    }
+    const double t_read1 = now_s();
+
+    hhp_solve_opts o;
+    memset(&o, 0, sizeof o);
+    o.rtol = a.rtol;
+    o.maxit = a.n_iters;
+    o.precision = a.mixed ? HHP_PREC_MIXED : HHP_PREC_FP64;
+    o.inner_rtol = 1e-5;
+    o.fixed_iters = a.fixed;
+    o.print_every = a.print_every;
+    o.cb = a.print_every > 0 ? print_iter : NULL;
+    hhp_solve_info info;
+    memset(&info, 0, sizeof info);
+    hhp_status st = hhp_bicgstab(ctx, A, B, X, XT, &o, &info);
+    if (st != HHP_OK && st != HHP_ERR_MAXIT)
+        FAIL("hhp_bicgstab: %s (%s)", hhp_status_str(st), hhp_last_error());
+
+    if (perm) {
+        double *tmp = malloc(sizeof(double) * (size_t)m);
+        for (int i = 0; i < m; ++i) tmp[perm[i]] = X[i];
+        memcpy(X, tmp, sizeof(double) * (size_t)m);
+        free(tmp);
+    }
+    printf("n_iters : %d \n", info.iters);
+    printf("spmv : %lf \n", info.t_solve_s);
+    printf("file_read : %lf \n", t_read1 - t_read0);
+    printf("relative_residual : %E\n", info.rel_res_true);
+    printf("iterations_to_tol : %d\n", (st == HHP_OK && !a.fixed) ? info.iters : -1);
+    if (XT) printf("err_vs_target : %E\n", info.err_vs_target);
+    printf("outer_iters : %d\n", info.outer_iters);
+    printf("precision : %s\n", a.mixed ? "mixed" : "fp64");
+    printf("status : %s\n", hhp_status_str(st));
+    printf("everything_total : %lf\n", now_s() - t_begin);
+    printf("\n----------------------------------------------------------------------\n");
+    CHECK(hhp_vector_write(a.output_x, n, X, a.exact));
+
+    hhp_mat_destroy(A);
+    hhp_ctx_destroy(ctx);
+    free(X); free(B); free(XT); free(perm);
+    return EXIT_SUCCESS;
+}

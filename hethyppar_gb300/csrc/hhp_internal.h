@@ -1,0 +1,161 @@
+// hhp_internal.h -- host-side structures shared by the translation units of libhhp_gpu.so.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "hhp_gpu.h"
+
+namespace hhp {
+
+// ---- error plumbing ----------------------------------------------------------------------------
+void set_error(const char *fmt, ...);
+hhp_status cuda_fail(cudaError_t e, const char *what, const char *file, int line);
+
+#define HHP_CUDA(call)                                                          \
+    do {                                                                        \
+        cudaError_t _e = (call);                                                \
+        if (_e != cudaSuccess) return ::hhp::cuda_fail(_e, #call, __FILE__, __LINE__); \
+    } while (0)
+#define HHP_TRY(call)                          \
+    do {                                       \
+        hhp_status _s = (call);                \
+        if (_s != HHP_OK) return _s;           \
+    } while (0)
+
+// ---- SpMV work plan ----------------------------------------------------------------------------
+// One work item = 16 bytes:
+//   x   first row
+//   y   kind (bits 30-31) | payload (bits 0-29):
+//         KIND_ROWS : payload = number of rows (1..32), one row per lane, each row summed
+//                     sequentially (fused multiply-add in CSR order)
+//         KIND_VEC  : payload = 1; one row with MED < len <= cap, summed by the whole warp
+//         KIND_CHUNK: payload = chunk id; a slice of a long row (len > cap), summed by the warp,
+//                     slices combined in slice order by the last warp to finish one
+//   z,w nnz range [k0, k1)
+// Items are in row order and split into contiguous per-warp ranges of near-equal work.
+enum : int { KIND_ROWS = 0, KIND_VEC = 1, KIND_CHUNK = 2 };
+constexpr int KIND_SHIFT = 30;
+constexpr int PAYLOAD_MASK = (1 << 30) - 1;
+
+struct PlanHost {
+    int n_warps = 0, cap = 0, med = 0;
+    std::vector<int4> items;
+    std::vector<int> warp_begin;      // n_warps + 1
+    std::vector<int> long_rows;       // row of each long row
+    std::vector<int> long_first;      // first chunk id per long row, n_long + 1
+    std::vector<int> chunk_long;      // long-row index of each chunk
+    long long max_item_nnz = 0;
+    double imbalance = 1.0;           // max warp work / mean warp work
+};
+
+// Builds the plan from a host rowptr. med: longest row summed one-row-per-lane; cap: most
+// nonzeros one item holds (a stage buffer's capacity).
+void build_plan(int m, const int *rowptr, int n_warps, int cap, int med, PlanHost &out);
+
+struct PlanDev {
+    int n_warps = 0, cap = 0, n_items = 0, n_long = 0, n_chunks = 0;
+    int ctas = 0, warps_per_cta = 0, ns = 0;
+    size_t smem_bytes = 0;
+    int4 *items = nullptr;
+    int *warp_begin = nullptr;
+    int *long_rows = nullptr, *long_first = nullptr, *chunk_long = nullptr;
+    double *chunk_part = nullptr;     // n_chunks
+    unsigned *long_cnt = nullptr;     // n_long (kept at zero between launches)
+    double *long_dot = nullptr;       // n_long * 2 epilogue contributions of long rows
+    double *cta_part = nullptr;       // ctas * 2 epilogue partials
+    void release();
+};
+
+// ---- context and matrix ------------------------------------------------------------------------
+struct Solver;  // per-matrix solver workspace (hhp_krylov.cu)
+
+}  // namespace hhp
+
+struct hhp_ctx {
+    int device = 0;
+    int num_sms = 0;
+    size_t smem_optin = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int *dev_err = nullptr;           // device error word (hhp::DEV_*), zeroed
+    long long kernel_launches = 0;
+};
+
+struct hhp_mat {
+    hhp_ctx *ctx = nullptr;
+    int m = 0, n = 0, nnz = 0;
+    // Device CSR, padded: rowptr m+1+4, col nnz+4, val nnz+4 (padding zeroed) so 16-byte TMA
+    // copies rounded outwards stay inside the allocations.
+    int *rowptr = nullptr, *col = nullptr;
+    double *val = nullptr;
+    float *val32 = nullptr;           // lazily built FP32 copy of val
+    std::vector<int> rowptr_host;     // kept for planning
+    hhp::PlanDev plan64, plan32;      // plans for the FP64 and FP32 kernels
+    // transpose (lazily built on the device)
+    hhp_mat *t = nullptr;
+    int *t_map = nullptr;             // t_map[p] = index in A of A^T's entry p
+    int *rowidx = nullptr;            // row of each stored entry (built with the transpose)
+    hhp::Solver *solver = nullptr;    // FP64/mixed workspace for A (A^T's lives in t->solver)
+};
+
+namespace hhp {
+
+// ---- SpMV launchers (hhp_spmv.cu) ----------------------------------------------------------------
+// Epilogue kinds of the fused SpMV.
+enum EpKind : int {
+    EP_AXPBY = 0,   // y = alpha*(A x) + beta*y
+    EP_DOT1 = 1,    // y = A x; partial[0] += y.w1
+    EP_DOT2 = 2,    // y = A x; partial[0] += y.w1, partial[1] += y.y
+    EP_RESID = 3,   // y = w1 - A x (residual); partial[0] += y.y, partial[1] += w1.w1
+};
+
+hhp_status ensure_plan(hhp_mat *A, bool fp32);
+// Launches the FP64 SpMV with an epilogue on `stream` (x, y, w1 length-padded device vectors).
+hhp_status launch_spmv64(hhp_mat *A, cudaStream_t stream, EpKind ep, const double *x, double *y, const double *w1,
+                         double alpha, double beta);
+hhp_status launch_spmv32(hhp_mat *A, cudaStream_t stream, EpKind ep, const float *x, float *y, const float *w1);
+// Number of partial records (ctas) and long-row records of the last-used plan, for the reducers.
+inline int plan_ctas(const hhp_mat *A, bool fp32) { return fp32 ? A->plan32.ctas : A->plan64.ctas; }
+
+// ---- Krylov solver (hhp_krylov.cu) ---------------------------------------------------------------
+// b, x, xt are device pointers when host == false, host pointers when host == true.
+hhp_status solve_any(hhp_mat *A, const double *b, double *x, const double *xt, const hhp_solve_opts *o,
+                     hhp_solve_info *info, bool host);
+inline hhp_status solve_dev(hhp_mat *A, const double *b, double *x, const double *xt, const hhp_solve_opts *o,
+                            hhp_solve_info *info) {
+    return solve_any(A, b, x, xt, o, info, false);
+}
+void solver_release(Solver *s);
+// Adjoint: lambda = A^-T g; dlda[k] = -lambda[row(k)] * x[col(k)].
+hhp_status backward_dev(hhp_mat *A, const double *x_dev, const double *g_dev, double *dldb_dev, double *dlda_dev,
+                        const hhp_solve_opts *o, hhp_solve_info *info);
+
+// ---- transpose (hhp_transpose.cu) -----------------------------------------------------------------
+hhp_status ensure_transpose(hhp_mat *A);
+hhp_status refresh_transpose_values(hhp_mat *A);
+hhp_status launch_dlda(hhp_mat *A, cudaStream_t s, const double *lambda, const double *x, double *dlda);
+
+// ---- files (hhp_io.cpp) ----------------------------------------------------------------------------
+hhp_status read_mtx(const char *path, int &m, int &n, int &nnz, std::vector<int> &rowptr, std::vector<int> &col,
+                    std::vector<double> &val);
+
+// ---- matrix helpers (hhp_api.cpp) ------------------------------------------------------------------
+hhp_status mat_create_dev(hhp_ctx *ctx, int m, int n, int nnz, hhp_mat **out);  // allocates, zero padding
+hhp_status mat_refresh_derived(hhp_mat *A);                                      // after value changes
+inline int pad4(int n) { return (n + 3) & ~3; }
+
+// Kernel tuning knobs (environment overrides read once).
+struct Tuning {
+    int cap64 = 512, cap32 = 1024, med = 64, wpc = 12, ns = 2, vec_blocks_per_sm = 2, unroll_iters = 4;
+};
+const Tuning &tuning();
+
+// Reads an environment integer with a default.
+int env_int(const char *name, int dflt);
+
+}  // namespace hhp

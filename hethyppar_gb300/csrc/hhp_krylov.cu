@@ -1,0 +1,903 @@
+// hhp_krylov.cu -- BiCGStab on the GPU: fused vector kernels, device-resident scalars, and the
+// whole iteration loop inside one CUDA graph (a WHILE conditional node), plus the FP32-inner /
+// FP64-refinement form and the adjoint solve.
+//
+// The iteration is the reference's (src/entry/bicgstab_cpu.c:176-244, and the device-pointer
+// form src/entry/bicgstab_gpu_dp.c:165-196):
+//   rho_new = r.r0 ; beta = (rho_new/rho)(alpha/omega) ; p = r + beta (p - omega v)
+//   v = A p ; alpha = rho/(r0.v) ; s = r - alpha v ; t = A s ; omega = (t.s)/(t.t)
+//   x += alpha p + omega s ; r = s - omega t
+// with the stop tests of gpu_BiCGStab (src/entry/bicgstab_gpu.c:149-150, 231-236, 289-293):
+// threshold = rtol ||r0||, stop after the s-step if ||s|| < threshold (x += alpha p only), or
+// after a full step if ||r|| < threshold.
+//
+// One iteration = 5 kernels, 3 reduction points:
+//   K_P    reduces (r.r0, r.r) of the previous step, tests convergence, forms beta, updates p
+//   SpMV   v = A p, epilogue r0.v
+//   K_S    alpha = rho/(r0.v), s = r - alpha v, epilogue s.s
+//   SpMV   t = A s, epilogue (t.s, t.t)
+//   K_XR   omega, x += alpha p + omega s, r = s - omega t, epilogue (r.r0, r.r)
+// Reductions: each producer writes one partial per block; each consumer block re-reduces all
+// partials in a fixed order (so every block gets the same scalar, bit for bit, and runs are
+// reproducible). No host synchronisation inside the loop: kernels read the scalars from device
+// memory and the K_P kernel ends the WHILE loop with cudaGraphSetConditional.
+#include <algorithm>
+#include <cmath>
+#include <cstddef>
+#include <cstring>
+
+#include "hhp_device.cuh"
+#include "hhp_internal.h"
+
+namespace hhp {
+
+// Host-written control block followed by device-written state.
+struct DevScal {
+    // control (copied from pinned host memory at the start of each graph launch)
+    double rtol2;
+    double inner_rtol2;
+    int maxit;
+    int fixed;
+    int restart;
+    int first_outer;
+    // state
+    double rho_prev, rho_cur, alpha, omega, beta;
+    double rr0, thr2, bb, rr_last, true_rr;
+    double rd2, hist_scale;
+    int iter, iter_start, status, bodies, outer_conv, pad_;
+};
+constexpr size_t kCtlBytes = offsetof(DevScal, rho_prev);
+
+struct Solver {
+    hhp_mat *A = nullptr;
+    int n = 0, n_pad = 0, nblk = 0, nthr = 512;
+    // FP64 vectors (n_pad each)
+    double *X = nullptr, *B = nullptr, *R = nullptr, *R0 = nullptr, *P = nullptr, *V = nullptr, *S = nullptr,
+           *T = nullptr, *Y = nullptr;
+    // FP32 inner vectors (mixed form)
+    float *D32 = nullptr, *R32 = nullptr, *R0_32 = nullptr, *P32 = nullptr, *V32 = nullptr, *S32 = nullptr,
+          *T32 = nullptr;
+    double *part_xr = nullptr, *part_s = nullptr;      // nblk*2 each (FP64 loop)
+    double *part_xr32 = nullptr, *part_s32 = nullptr;  // nblk*2 each (FP32 inner loop)
+    DevScal *sc = nullptr, *sc32 = nullptr;            // device
+    DevScal *h_sc = nullptr, *h_sc32 = nullptr;        // pinned host mirrors
+    double *hist = nullptr;
+    int hist_cap = 0;
+    cudaStream_t s2 = nullptr;
+    cudaGraphExec_t g64 = nullptr, gmix = nullptr;
+    int g64_kernels_pro = 0, g64_kernels_epi = 0, gmix_kernels_pro = 0, gmix_kernels_epi = 0, unroll = 4;
+};
+
+namespace {
+
+template <typename T>
+struct Unit;
+template <>
+struct Unit<double> {
+    using V = double2;
+    static constexpr int E = 2;
+};
+template <>
+struct Unit<float> {
+    using V = float4;
+    static constexpr int E = 4;
+};
+
+template <typename T>
+__device__ __forceinline__ void ldu(T (&o)[Unit<T>::E], const T *p, int u) {
+    const typename Unit<T>::V v = reinterpret_cast<const typename Unit<T>::V *>(p)[u];
+    memcpy(o, &v, sizeof(v));
+}
+template <typename T>
+__device__ __forceinline__ void stu(T *p, int u, const T (&o)[Unit<T>::E]) {
+    typename Unit<T>::V v;
+    memcpy(&v, o, sizeof(v));
+    reinterpret_cast<typename Unit<T>::V *>(p)[u] = v;
+}
+
+__device__ __forceinline__ double tfma(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float tfma(float a, float b, float c) { return fmaf(a, b, c); }
+// Dot-product accumulation in FP64: one FP64 FMA for FP64 data; for FP32 data the product is
+// formed in FP32 and accumulated in FP64 (the partials stay FP64).
+__device__ __forceinline__ double dacc(double acc, double a, double b) { return fma(a, b, acc); }
+__device__ __forceinline__ double dacc(double acc, float a, float b) { return acc + static_cast<double>(a * b); }
+
+__device__ __forceinline__ bool b0t0() { return blockIdx.x == 0 && threadIdx.x == 0; }
+
+struct SpmvParts {
+    const double *cta_part;
+    int n_cta;
+    const double *long_dot;
+    int n_long;
+};
+
+// ---------------------------------------------------------------------------------------------
+// Initialisation: after the residual SpMV (R = B - A X; partials ||R||^2, ||B||^2).
+// R0 = R, P = V = 0, scalars rho = alpha = omega = 1 (bicgstab_cpu.c:176-188).
+template <typename T>
+__global__ void __launch_bounds__(512) k_init(DevScal *sc, const T *R, T *R0, T *P, T *V, int nu, SpmvParts sp,
+                                              double *part_xr, double *part_s) {
+    __shared__ double red[64];
+    double v[2];
+    reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
+    const double rr = v[0], bb = v[1];
+    constexpr int E = Unit<T>::E;
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += gridDim.x * blockDim.x) {
+        T r[E], z[E];
+        ldu(r, R, u);
+#pragma unroll
+        for (int e = 0; e < E; ++e) z[e] = T(0);
+        stu(R0, u, r);
+        stu(P, u, z);
+        stu(V, u, z);
+    }
+    if (threadIdx.x == 0) {
+        part_xr[2 * blockIdx.x] = blockIdx.x == 0 ? rr : 0.0;
+        part_xr[2 * blockIdx.x + 1] = blockIdx.x == 0 ? rr : 0.0;
+        part_s[2 * blockIdx.x] = 0.0;
+        part_s[2 * blockIdx.x + 1] = 0.0;
+    }
+    if (b0t0()) {
+        if (!sc->restart) {
+            sc->rr0 = rr;
+            sc->thr2 = sc->fixed ? -1.0 : sc->rtol2 * rr;
+            sc->iter = 0;
+            sc->bb = bb;
+            sc->hist_scale = 1.0;
+        }
+        sc->iter_start = sc->iter;
+        sc->bodies = 0;
+        sc->rho_prev = 1.0;
+        sc->alpha = 1.0;
+        sc->omega = 1.0;
+        sc->beta = 0.0;
+        sc->rr_last = rr;
+        sc->status = ST_RUNNING;
+    }
+}
+
+// K_P: convergence test on the previous step, beta, p = r + beta (p - omega v).
+template <typename T>
+__global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const T *R, int nu, const double *part_xr,
+                                           const double *part_s, int nparts, double *hist, int hist_cap,
+                                           cudaGraphConditionalHandle cond, int first_in_body, const int *dev_err) {
+    __shared__ double red[64];
+    double v[2], w[2];
+    reduce_partials<2>(part_xr, nparts, nullptr, 0, v, red);
+    reduce_partials<2>(part_s, nparts, nullptr, 0, w, red);
+    const double rho_new = v[0], rr = v[1], ss = w[0];
+    const int st = sc->status;
+    if (st != ST_RUNNING) {
+        if (b0t0()) cudaGraphSetConditional(cond, 0);
+        return;
+    }
+    if (b0t0() && first_in_body) sc->bodies += 1;
+    const int iter = sc->iter, it0 = sc->iter_start;
+    const double thr2 = sc->thr2;
+    if (b0t0() && iter > it0 && iter - 1 < hist_cap) hist[iter - 1] = sc->hist_scale * sqrt(rr / sc->rr0);
+    int term = ST_RUNNING;
+    if (*reinterpret_cast<volatile const int *>(dev_err) != DEV_OK) term = ST_DEVICE_ERROR;
+    else if (thr2 >= 0.0 && iter > it0 && ss <= thr2) term = ST_CONVERGED_HALF;
+    else if (thr2 >= 0.0 && rr <= thr2) term = ST_CONVERGED;
+    else if (iter >= sc->maxit) term = ST_MAXIT;
+    else if (!finite_nonzero(rho_new) || !isfinite(rr)) term = ST_BREAKDOWN;
+    if (term != ST_RUNNING) {
+        if (b0t0()) {
+            sc->status = term;
+            sc->rr_last = rr;
+            cudaGraphSetConditional(cond, 0);
+        }
+        return;
+    }
+    const double beta = (rho_new / sc->rho_prev) * (sc->alpha / sc->omega);
+    if (b0t0()) {
+        sc->rho_cur = rho_new;
+        sc->beta = beta;
+        sc->rr_last = rr;
+    }
+    const T tb = static_cast<T>(beta), tw = static_cast<T>(-sc->omega);
+    constexpr int E = Unit<T>::E;
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += gridDim.x * blockDim.x) {
+        T p[E], vv[E], r[E];
+        ldu(p, P, u);
+        ldu(vv, V, u);
+        ldu(r, R, u);
+#pragma unroll
+        for (int e = 0; e < E; ++e) p[e] = tfma(tb, tfma(tw, vv[e], p[e]), r[e]);
+        stu(P, u, p);
+    }
+}
+
+// K_S: alpha = rho / (r0.v), s = r - alpha v, partial s.s.
+template <typename T>
+__global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const T *V, int nu, SpmvParts sp,
+                                           double *part_s) {
+    __shared__ double red[64];
+    double v[2];
+    reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
+    if (sc->status != ST_RUNNING) return;
+    const double rv = v[0];
+    const double alpha = sc->rho_cur / rv;
+    if (!finite_nonzero(rv) || !isfinite(alpha)) {
+        if (b0t0()) sc->status = ST_BREAKDOWN;
+        return;
+    }
+    if (b0t0()) {
+        sc->alpha = alpha;
+        sc->rho_prev = sc->rho_cur;
+        sc->iter = sc->iter + 1;
+    }
+    const T ta = static_cast<T>(-alpha);
+    constexpr int E = Unit<T>::E;
+    double acc[1] = {0.0};
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += gridDim.x * blockDim.x) {
+        T r[E], vv[E], s[E];
+        ldu(r, R, u);
+        ldu(vv, V, u);
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            s[e] = tfma(ta, vv[e], r[e]);
+            acc[0] = dacc(acc[0], s[e], s[e]);
+        }
+        stu(S, u, s);
+    }
+    block_sum<1>(acc, red);
+    if (threadIdx.x == 0) {
+        part_s[2 * blockIdx.x] = acc[0];
+        part_s[2 * blockIdx.x + 1] = 0.0;
+    }
+}
+
+// K_XR: omega = (t.s)/(t.t), x += alpha p + omega s, r = s - omega t, partials (r.r0, r.r).
+// Half step (||s|| below the threshold): x += alpha p, r = s.
+template <typename T>
+__global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P, const T *S, const T *Tv,
+                                            const T *R0, int nu, SpmvParts sp, const double *part_s, int nparts,
+                                            double *part_xr) {
+    __shared__ double red[64];
+    double v[2], w[2];
+    reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
+    reduce_partials<2>(part_s, nparts, nullptr, 0, w, red);
+    if (sc->status != ST_RUNNING) return;
+    const double thr2 = sc->thr2;
+    const bool half = thr2 >= 0.0 && w[0] <= thr2;
+    const double alpha = sc->alpha;
+    double omega = 0.0;
+    if (!half) {
+        omega = v[0] / v[1];
+        if (!finite_nonzero(v[1]) || !isfinite(omega)) {
+            if (b0t0()) sc->status = ST_BREAKDOWN;
+            return;
+        }
+        if (b0t0()) sc->omega = omega;
+    }
+    const T ta = static_cast<T>(alpha), tw = static_cast<T>(omega), tnw = static_cast<T>(-omega);
+    constexpr int E = Unit<T>::E;
+    double acc[2] = {0.0, 0.0};
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += gridDim.x * blockDim.x) {
+        T x[E], p[E], s[E], r0[E], r[E];
+        ldu(x, X, u);
+        ldu(p, P, u);
+        ldu(s, S, u);
+        ldu(r0, R0, u);
+        if (!half) {
+            T t[E];
+            ldu(t, Tv, u);
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                x[e] = tfma(tw, s[e], tfma(ta, p[e], x[e]));
+                r[e] = tfma(tnw, t[e], s[e]);
+            }
+        } else {
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                x[e] = tfma(ta, p[e], x[e]);
+                r[e] = s[e];
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            acc[0] = dacc(acc[0], r[e], r0[e]);
+            acc[1] = dacc(acc[1], r[e], r[e]);
+        }
+        stu(X, u, x);
+        stu(R, u, r);
+    }
+    block_sum<2>(acc, red);
+    if (threadIdx.x == 0) {
+        part_xr[2 * blockIdx.x] = acc[0];
+        part_xr[2 * blockIdx.x + 1] = acc[1];
+    }
+}
+
+// Final true residual (SpMV EP_RESID into Y already done): ||b - A x||^2, ||b||^2.
+__global__ void k_finish(DevScal *sc, SpmvParts sp) {
+    __shared__ double red[64];
+    double v[2];
+    reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
+    if (threadIdx.x == 0) {
+        sc->true_rr = v[0];
+        sc->bb = v[1];
+    }
+}
+
+// Mixed form, outer step: given the FP64 residual Rd = B - A X (partials ||Rd||^2, ||B||^2),
+// decide convergence; otherwise scale Rd to unit norm into the FP32 right-hand side and reset
+// the FP32 inner solver (initial guess 0, so r = r0 = rhs).
+__global__ void __launch_bounds__(512) k_mix_prep(DevScal *sc, DevScal *sc32, const double *Rd, float *D32,
+                                                  float *R32, float *R0_32, float *P32, float *V32, int nu4,
+                                                  SpmvParts sp, double *part_xr32, double *part_s32,
+                                                  cudaGraphConditionalHandle inner_cond) {
+    __shared__ double red[64];
+    double v[2];
+    reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
+    const double rd2 = v[0], bb = v[1];
+    const bool first = sc->first_outer != 0;
+    const double rr0 = first ? rd2 : sc->rr0;
+    const double thr2 = sc->rtol2 * rr0;
+    if (b0t0()) {
+        if (first) {
+            sc->rr0 = rd2;
+            sc->bb = bb;
+            sc->thr2 = thr2;
+            sc->iter = 0;
+            sc32->iter = 0;
+        }
+        sc->rd2 = rd2;
+    }
+    if (rd2 <= thr2 || !isfinite(rd2)) {
+        if (b0t0()) {
+            sc->outer_conv = isfinite(rd2) ? 1 : -1;
+            cudaGraphSetConditional(inner_cond, 0);
+        }
+        return;
+    }
+    if (b0t0()) sc->outer_conv = 0;
+    const double scale = 1.0 / sqrt(rd2);
+    double acc[1] = {0.0};
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu4; u += gridDim.x * blockDim.x) {
+        const double2 a = reinterpret_cast<const double2 *>(Rd)[2 * u];
+        const double2 b = reinterpret_cast<const double2 *>(Rd)[2 * u + 1];
+        float4 r = make_float4(static_cast<float>(a.x * scale), static_cast<float>(a.y * scale),
+                               static_cast<float>(b.x * scale), static_cast<float>(b.y * scale));
+        acc[0] = dacc(dacc(dacc(dacc(acc[0], r.x, r.x), r.y, r.y), r.z, r.z), r.w, r.w);
+        const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+        reinterpret_cast<float4 *>(R32)[u] = r;
+        reinterpret_cast<float4 *>(R0_32)[u] = r;
+        reinterpret_cast<float4 *>(D32)[u] = z;
+        reinterpret_cast<float4 *>(P32)[u] = z;
+        reinterpret_cast<float4 *>(V32)[u] = z;
+    }
+    block_sum<1>(acc, red);
+    if (threadIdx.x == 0) {
+        part_xr32[2 * blockIdx.x] = acc[0];
+        part_xr32[2 * blockIdx.x + 1] = acc[0];
+        part_s32[2 * blockIdx.x] = 0.0;
+        part_s32[2 * blockIdx.x + 1] = 0.0;
+    }
+    if (b0t0()) {
+        sc32->rr0 = 1.0;
+        sc32->thr2 = sc->inner_rtol2;
+        sc32->iter_start = sc32->iter;
+        sc32->maxit = sc->maxit;
+        sc32->hist_scale = sqrt(rd2 / rr0);
+        sc32->rho_prev = 1.0;
+        sc32->alpha = 1.0;
+        sc32->omega = 1.0;
+        sc32->status = ST_RUNNING;
+        sc32->bodies = 0;
+    }
+}
+
+// Mixed form: x += ||Rd|| * d (FP64 update of the FP64 iterate).
+__global__ void __launch_bounds__(512) k_mix_update(const DevScal *sc, double *X, const float *D32, int nu4) {
+    if (sc->outer_conv != 0) return;
+    const double s = sqrt(sc->rd2);
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu4; u += gridDim.x * blockDim.x) {
+        const float4 d = reinterpret_cast<const float4 *>(D32)[u];
+        double2 a = reinterpret_cast<double2 *>(X)[2 * u];
+        double2 b = reinterpret_cast<double2 *>(X)[2 * u + 1];
+        a.x = fma(s, static_cast<double>(d.x), a.x);
+        a.y = fma(s, static_cast<double>(d.y), a.y);
+        b.x = fma(s, static_cast<double>(d.z), b.x);
+        b.y = fma(s, static_cast<double>(d.w), b.y);
+        reinterpret_cast<double2 *>(X)[2 * u] = a;
+        reinterpret_cast<double2 *>(X)[2 * u + 1] = b;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+template <typename T>
+T *dalloc(size_t n, hhp_status &st) {
+    T *p = nullptr;
+    if (st != HHP_OK) return nullptr;
+    if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) {
+        set_error("cudaMalloc of %zu bytes failed", n * sizeof(T));
+        st = HHP_ERR_OOM;
+        return nullptr;
+    }
+    cudaMemset(p, 0, n * sizeof(T));
+    return p;
+}
+
+SpmvParts parts_of(const PlanDev &p) { return SpmvParts{p.cta_part, p.ctas, p.long_dot, p.n_long}; }
+
+hhp_status ensure_solver(hhp_mat *A, Solver **out, int maxit) {
+    Solver *s = A->solver;
+    if (!s) {
+        s = new Solver();
+        s->A = A;
+        s->n = A->n;
+        s->n_pad = pad4(A->n);
+        s->nblk = std::max(1, A->ctx->num_sms * tuning().vec_blocks_per_sm);
+        s->unroll = std::max(1, std::min(tuning().unroll_iters, 16));
+        hhp_status st = HHP_OK;
+        const size_t np = static_cast<size_t>(s->n_pad);
+        s->X = dalloc<double>(np, st);
+        s->B = dalloc<double>(np, st);
+        s->R = dalloc<double>(np, st);
+        s->R0 = dalloc<double>(np, st);
+        s->P = dalloc<double>(np, st);
+        s->V = dalloc<double>(np, st);
+        s->S = dalloc<double>(np, st);
+        s->T = dalloc<double>(np, st);
+        s->Y = dalloc<double>(np, st);
+        s->part_xr = dalloc<double>(2 * s->nblk, st);
+        s->part_s = dalloc<double>(2 * s->nblk, st);
+        s->part_xr32 = dalloc<double>(2 * s->nblk, st);
+        s->part_s32 = dalloc<double>(2 * s->nblk, st);
+        s->sc = dalloc<DevScal>(1, st);
+        s->sc32 = dalloc<DevScal>(1, st);
+        if (st == HHP_OK && cudaMallocHost(&s->h_sc, sizeof(DevScal)) != cudaSuccess) st = HHP_ERR_OOM;
+        if (st == HHP_OK && cudaMallocHost(&s->h_sc32, sizeof(DevScal)) != cudaSuccess) st = HHP_ERR_OOM;
+        if (st == HHP_OK && cudaStreamCreateWithFlags(&s->s2, cudaStreamNonBlocking) != cudaSuccess)
+            st = HHP_ERR_CUDA;
+        A->solver = s;
+        if (st != HHP_OK) return st;
+        memset(s->h_sc, 0, sizeof(DevScal));
+        memset(s->h_sc32, 0, sizeof(DevScal));
+    }
+    const int need = std::max(maxit + 1, 1024);
+    if (s->hist_cap < need) {
+        cudaFree(s->hist);
+        s->hist = nullptr;
+        HHP_CUDA(cudaMalloc(&s->hist, sizeof(double) * static_cast<size_t>(need)));
+        s->hist_cap = need;
+        // graphs hold the old history pointer
+        if (s->g64) cudaGraphExecDestroy(s->g64);
+        if (s->gmix) cudaGraphExecDestroy(s->gmix);
+        s->g64 = s->gmix = nullptr;
+    }
+    *out = s;
+    return HHP_OK;
+}
+
+hhp_status ensure_fp32_inner(hhp_mat *A, Solver *s) {
+    if (!A->val32) HHP_TRY(mat_refresh_derived(A));
+    if (!s->D32) {
+        hhp_status st = HHP_OK;
+        const size_t np = static_cast<size_t>(s->n_pad);
+        s->D32 = dalloc<float>(np, st);
+        s->R32 = dalloc<float>(np, st);
+        s->R0_32 = dalloc<float>(np, st);
+        s->P32 = dalloc<float>(np, st);
+        s->V32 = dalloc<float>(np, st);
+        s->S32 = dalloc<float>(np, st);
+        s->T32 = dalloc<float>(np, st);
+        if (st != HHP_OK) return st;
+    }
+    return HHP_OK;
+}
+
+// Adds a WHILE conditional node to the graph being captured on `stream`, captures `unroll`
+// iterations of the loop body into it on s->s2, and makes later work on `stream` depend on it.
+template <typename T>
+hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R, T *R0, T *P, T *V, T *S, T *Tv,
+                        double *part_xr, double *part_s, bool fp32, cudaGraphConditionalHandle *cond_out) {
+    hhp_mat *A = s->A;
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t nd = 0;
+    HHP_CUDA(cudaStreamGetCaptureInfo(stream, &cs, nullptr, &g, &deps, nullptr, &nd));
+    cudaGraphConditionalHandle cond;
+    HHP_CUDA(cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {};
+    memset(&cp, 0, sizeof(cp));
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = cond;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cn;
+    HHP_CUDA(cudaGraphAddNode(&cn, g, deps, nullptr, nd, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    HHP_CUDA(cudaStreamUpdateCaptureDependencies(stream, &cn, nullptr, 1, cudaStreamSetCaptureDependencies));
+
+    HHP_CUDA(cudaStreamBeginCaptureToGraph(s->s2, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    constexpr int E = Unit<T>::E;
+    const int nu = s->n_pad / E;
+    const PlanDev &pl = fp32 ? A->plan32 : A->plan64;
+    hhp_status st = HHP_OK;
+    for (int k = 0; k < s->unroll && st == HHP_OK; ++k) {
+        k_p<T><<<s->nblk, s->nthr, 0, s->s2>>>(sc, P, V, R, nu, part_xr, part_s, s->nblk, s->hist, s->hist_cap, cond,
+                                               k == 0 ? 1 : 0, A->ctx->dev_err);
+        if (fp32)
+            st = launch_spmv32(A, s->s2, EP_DOT1, reinterpret_cast<const float *>(P), reinterpret_cast<float *>(V),
+                               reinterpret_cast<const float *>(R0));
+        else
+            st = launch_spmv64(A, s->s2, EP_DOT1, reinterpret_cast<const double *>(P), reinterpret_cast<double *>(V),
+                               reinterpret_cast<const double *>(R0), 1.0, 0.0);
+        if (st != HHP_OK) break;
+        k_s<T><<<s->nblk, s->nthr, 0, s->s2>>>(sc, S, R, V, nu, parts_of(pl), part_s);
+        if (fp32)
+            st = launch_spmv32(A, s->s2, EP_DOT2, reinterpret_cast<const float *>(S), reinterpret_cast<float *>(Tv),
+                               reinterpret_cast<const float *>(S));
+        else
+            st = launch_spmv64(A, s->s2, EP_DOT2, reinterpret_cast<const double *>(S),
+                               reinterpret_cast<double *>(Tv), reinterpret_cast<const double *>(S), 1.0, 0.0);
+        if (st != HHP_OK) break;
+        k_xr<T><<<s->nblk, s->nthr, 0, s->s2>>>(sc, X, R, P, S, Tv, R0, nu, parts_of(pl), part_s, s->nblk, part_xr);
+    }
+    cudaGraph_t body_out = body;
+    cudaError_t e = cudaStreamEndCapture(s->s2, &body_out);
+    if (st != HHP_OK) return st;
+    HHP_CUDA(e);
+    HHP_CUDA(cudaGetLastError());
+    *cond_out = cond;
+    return HHP_OK;
+}
+
+// FP64 solve graph: ctl copy, residual SpMV, init, WHILE{loop}, true-residual SpMV, finish.
+hhp_status build_g64(Solver *s) {
+    hhp_mat *A = s->A;
+    cudaStream_t st = A->ctx->stream;
+    HHP_TRY(ensure_plan(A, false));
+    const int nu = s->n_pad / 2;
+    HHP_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+    hhp_status rc = HHP_OK;
+    do {
+        if (cudaMemcpyAsync(s->sc, s->h_sc, kCtlBytes, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+            rc = HHP_ERR_CUDA;
+            break;
+        }
+        rc = launch_spmv64(A, st, EP_RESID, s->X, s->R, s->B, 1.0, 0.0);
+        if (rc != HHP_OK) break;
+        k_init<double><<<s->nblk, s->nthr, 0, st>>>(s->sc, s->R, s->R0, s->P, s->V, nu, parts_of(A->plan64),
+                                                     s->part_xr, s->part_s);
+        cudaGraphConditionalHandle cond;
+        rc = capture_loop<double>(s, st, s->sc, s->X, s->R, s->R0, s->P, s->V, s->S, s->T, s->part_xr, s->part_s,
+                                  false, &cond);
+        if (rc != HHP_OK) break;
+        rc = launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0);
+        if (rc != HHP_OK) break;
+        k_finish<<<1, 32, 0, st>>>(s->sc, parts_of(A->plan64));
+    } while (0);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (rc != HHP_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    HHP_CUDA(e);
+    cudaError_t ie = cudaGraphInstantiate(&s->g64, g, 0);
+    cudaGraphDestroy(g);
+    HHP_CUDA(ie);
+    s->g64_kernels_pro = 2;
+    s->g64_kernels_epi = 2;
+    // launch_spmv64 counted its captured launches; graph launches are counted when executed.
+    A->ctx->kernel_launches -= 2 + 2 * s->unroll;
+    return HHP_OK;
+}
+
+// Mixed outer-step graph: FP64 residual, prep (convergence test + FP32 RHS), WHILE{FP32 loop},
+// FP64 update.
+hhp_status build_gmix(Solver *s) {
+    hhp_mat *A = s->A;
+    cudaStream_t st = A->ctx->stream;
+    HHP_TRY(ensure_plan(A, false));
+    HHP_TRY(ensure_plan(A, true));
+    const int nu4 = s->n_pad / 4;
+    HHP_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+    hhp_status rc = HHP_OK;
+    do {
+        if (cudaMemcpyAsync(s->sc, s->h_sc, kCtlBytes, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+            rc = HHP_ERR_CUDA;
+            break;
+        }
+        rc = launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0);
+        if (rc != HHP_OK) break;
+        // k_mix_prep may skip the inner loop, so the loop's condition handle is created first.
+        cudaStreamCaptureStatus cs;
+        cudaGraph_t g = nullptr;
+        const cudaGraphNode_t *deps = nullptr;
+        size_t nd = 0;
+        if (cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd) != cudaSuccess) {
+            rc = HHP_ERR_CUDA;
+            break;
+        }
+        cudaGraphConditionalHandle cond;
+        if (cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) {
+            rc = HHP_ERR_CUDA;
+            break;
+        }
+        k_mix_prep<<<s->nblk, s->nthr, 0, st>>>(s->sc, s->sc32, s->Y, s->D32, s->R32, s->R0_32, s->P32, s->V32, nu4,
+                                                 parts_of(A->plan64), s->part_xr32, s->part_s32, cond);
+        // WHILE node using the pre-created handle.
+        if (cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd) != cudaSuccess) {
+            rc = HHP_ERR_CUDA;
+            break;
+        }
+        cudaGraphNodeParams cp = {};
+        memset(&cp, 0, sizeof(cp));
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = cond;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t cn;
+        if (cudaGraphAddNode(&cn, g, deps, nullptr, nd, &cp) != cudaSuccess) {
+            rc = HHP_ERR_CUDA;
+            break;
+        }
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        if (cudaStreamUpdateCaptureDependencies(st, &cn, nullptr, 1, cudaStreamSetCaptureDependencies) !=
+            cudaSuccess) {
+            rc = HHP_ERR_CUDA;
+            break;
+        }
+        if (cudaStreamBeginCaptureToGraph(s->s2, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) !=
+            cudaSuccess) {
+            rc = HHP_ERR_CUDA;
+            break;
+        }
+        const int nu = s->n_pad / 4;
+        for (int k = 0; k < s->unroll && rc == HHP_OK; ++k) {
+            k_p<float><<<s->nblk, s->nthr, 0, s->s2>>>(s->sc32, s->P32, s->V32, s->R32, nu, s->part_xr32,
+                                                       s->part_s32, s->nblk, s->hist, s->hist_cap, cond, k == 0,
+                                                       A->ctx->dev_err);
+            rc = launch_spmv32(A, s->s2, EP_DOT1, s->P32, s->V32, s->R0_32);
+            if (rc != HHP_OK) break;
+            k_s<float><<<s->nblk, s->nthr, 0, s->s2>>>(s->sc32, s->S32, s->R32, s->V32, nu, parts_of(A->plan32),
+                                                       s->part_s32);
+            rc = launch_spmv32(A, s->s2, EP_DOT2, s->S32, s->T32, s->S32);
+            if (rc != HHP_OK) break;
+            k_xr<float><<<s->nblk, s->nthr, 0, s->s2>>>(s->sc32, s->D32, s->R32, s->P32, s->S32, s->T32, s->R0_32,
+                                                        nu, parts_of(A->plan32), s->part_s32, s->nblk,
+                                                        s->part_xr32);
+        }
+        cudaGraph_t body_out = body;
+        cudaError_t e2 = cudaStreamEndCapture(s->s2, &body_out);
+        if (rc != HHP_OK) break;
+        if (e2 != cudaSuccess) {
+            rc = HHP_ERR_CUDA;
+            break;
+        }
+        k_mix_update<<<s->nblk, s->nthr, 0, st>>>(s->sc, s->X, s->D32, nu4);
+    } while (0);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (rc != HHP_OK) {
+        if (g) cudaGraphDestroy(g);
+        if (rc == HHP_ERR_CUDA) set_error("capturing the mixed-precision graph failed: %s",
+                                          cudaGetErrorString(cudaGetLastError()));
+        return rc;
+    }
+    HHP_CUDA(e);
+    cudaError_t ie = cudaGraphInstantiate(&s->gmix, g, 0);
+    cudaGraphDestroy(g);
+    HHP_CUDA(ie);
+    s->gmix_kernels_pro = 2;
+    s->gmix_kernels_epi = 1;
+    A->ctx->kernel_launches -= 1 + 2 * s->unroll;
+    return HHP_OK;
+}
+
+// Copies a caller vector of n elements into an internal padded vector (padding stays zero).
+hhp_status copy_in(double *dst, const double *src, int n, cudaStream_t st, bool host) {
+    HHP_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * static_cast<size_t>(n),
+                             host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, st));
+    return HHP_OK;
+}
+
+hhp_status status_of(int st) {
+    switch (st) {
+        case ST_CONVERGED:
+        case ST_CONVERGED_HALF: return HHP_OK;
+        case ST_BREAKDOWN: return HHP_ERR_BREAKDOWN;
+        case ST_MAXIT: return HHP_ERR_MAXIT;
+        case ST_DEVICE_ERROR: return HHP_ERR_TIMEOUT;
+        default: return HHP_ERR_STATE;
+    }
+}
+
+__global__ void k_err_vs_target(const double *x, const double *xt, int n, double *out_max) {
+    __shared__ double red[32];
+    double m = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        m = fmax(m, fabs(x[i] - xt[i]));
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double r = 0.0;
+        for (int w = 0; w < (blockDim.x >> 5); ++w) r = fmax(r, red[w]);
+        // max of non-negative doubles: the integer ordering of their bit patterns is the same
+        atomicMax(reinterpret_cast<unsigned long long *>(out_max), __double_as_longlong(r));
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------
+hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double *xt, const hhp_solve_opts *o,
+                     hhp_solve_info *info, bool host) {
+    hhp_ctx *ctx = A->ctx;
+    cudaStream_t st = ctx->stream;
+    const bool mixed = o->precision == HHP_PREC_MIXED;
+    Solver *s = nullptr;
+    HHP_TRY(ensure_solver(A, &s, o->maxit));
+    if (mixed) HHP_TRY(ensure_fp32_inner(A, s));
+    HHP_CUDA(cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), st));
+    HHP_TRY(copy_in(s->B, b_in, A->m, st, host));
+    HHP_TRY(copy_in(s->X, x_io, A->n, st, host));
+    HHP_CUDA(cudaEventRecord(ctx->ev0, st));
+
+    DevScal &h = *s->h_sc;
+    h.rtol2 = o->rtol * o->rtol;
+    const double irt = o->inner_rtol > 0.0 ? o->inner_rtol : 1e-5;
+    h.inner_rtol2 = irt * irt;
+    h.maxit = o->maxit;
+    h.fixed = (o->fixed_iters && !mixed) ? 1 : 0;
+    int total_iters = 0, outer = 0, half = 0;
+    hhp_status result = HHP_OK;
+    const int max_outer = o->max_outer > 0 ? o->max_outer : 50;
+    double rel_true = NAN, rel_rec = NAN;
+
+    if (!mixed) {
+        if (!s->g64) HHP_TRY(build_g64(s));
+        int dev_status = ST_RUNNING;
+        for (int pass = 0; pass < max_outer; ++pass) {
+            h.restart = pass > 0 ? 1 : 0;
+            h.first_outer = 0;
+            HHP_CUDA(cudaGraphLaunch(s->g64, st));
+            HHP_CUDA(cudaMemcpyAsync(s->h_sc, s->sc, sizeof(DevScal), cudaMemcpyDeviceToHost, st));
+            HHP_CUDA(cudaStreamSynchronize(st));
+            ++outer;
+            ctx->kernel_launches += s->g64_kernels_pro + s->g64_kernels_epi + 5LL * s->unroll * h.bodies;
+            dev_status = h.status;
+            // Residual replacement: the recursive residual met the threshold but the true one
+            // did not (rounding drift); restart from the current iterate with the original r0.
+            const bool conv = dev_status == ST_CONVERGED || dev_status == ST_CONVERGED_HALF;
+            if (conv && !h.fixed && h.true_rr > h.thr2 && h.iter < h.maxit) continue;
+            break;
+        }
+        total_iters = h.iter;
+        half = dev_status == ST_CONVERGED_HALF;
+        rel_true = sqrt(h.true_rr / h.bb);
+        rel_rec = sqrt(h.rr_last / h.rr0);
+        if (h.fixed) result = (dev_status == ST_MAXIT) ? HHP_OK : status_of(dev_status);
+        else if (dev_status == ST_CONVERGED || dev_status == ST_CONVERGED_HALF)
+            result = (h.true_rr <= h.thr2 || h.thr2 < 0) ? HHP_OK : HHP_ERR_MAXIT;
+        else result = status_of(dev_status);
+    } else {
+        if (!s->gmix) HHP_TRY(build_gmix(s));
+        DevScal &h32 = *s->h_sc32;
+        result = HHP_ERR_MAXIT;
+        bool need_final = true;
+        for (int k = 0; k < max_outer; ++k) {
+            h.first_outer = k == 0 ? 1 : 0;
+            h.restart = 0;
+            HHP_CUDA(cudaGraphLaunch(s->gmix, st));
+            HHP_CUDA(cudaMemcpyAsync(s->h_sc, s->sc, sizeof(DevScal), cudaMemcpyDeviceToHost, st));
+            HHP_CUDA(cudaMemcpyAsync(s->h_sc32, s->sc32, sizeof(DevScal), cudaMemcpyDeviceToHost, st));
+            HHP_CUDA(cudaStreamSynchronize(st));
+            ctx->kernel_launches += s->gmix_kernels_pro + s->gmix_kernels_epi + 5LL * s->unroll * h32.bodies;
+            ++outer;
+            if (h.outer_conv == 1) {
+                result = HHP_OK;
+                need_final = false;
+                break;
+            }
+            if (h.outer_conv < 0) {
+                result = HHP_ERR_BREAKDOWN;
+                need_final = false;
+                break;
+            }
+            if (h32.iter >= o->maxit) break;  // budget spent (this step's update was applied)
+            if (h32.status == ST_BREAKDOWN && h32.iter == h32.iter_start) {
+                result = HHP_ERR_BREAKDOWN;
+                break;
+            }
+        }
+        total_iters = h32.iter;
+        half = h32.status == ST_CONVERGED_HALF;
+        if (need_final) {
+            HHP_TRY(launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0));
+            k_finish<<<1, 32, 0, st>>>(s->sc, parts_of(A->plan64));
+            ctx->kernel_launches += 1;
+            HHP_CUDA(cudaMemcpyAsync(s->h_sc, s->sc, sizeof(DevScal), cudaMemcpyDeviceToHost, st));
+            HHP_CUDA(cudaStreamSynchronize(st));
+            rel_true = sqrt(h.true_rr / h.bb);
+        } else {
+            rel_true = sqrt(h.rd2 / h.bb);
+        }
+        rel_rec = rel_true;
+    }
+    HHP_CUDA(cudaEventRecord(ctx->ev1, st));
+    HHP_CUDA(cudaMemcpyAsync(x_io, s->X, sizeof(double) * static_cast<size_t>(A->n),
+                             host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
+    double err = NAN;
+    if (xt && !host) {
+        double *dmax = s->Y;  // scratch slot; Y is not needed after the solve
+        HHP_CUDA(cudaMemsetAsync(dmax, 0, sizeof(double), st));
+        k_err_vs_target<<<ctx->num_sms, 256, 0, st>>>(s->X, xt, A->n, dmax);
+        ctx->kernel_launches += 1;
+        HHP_CUDA(cudaMemcpyAsync(&err, dmax, sizeof(double), cudaMemcpyDeviceToHost, st));
+    }
+    int dev_err = 0;
+    HHP_CUDA(cudaMemcpyAsync(&dev_err, ctx->dev_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    HHP_CUDA(cudaStreamSynchronize(st));
+    if (dev_err != DEV_OK) {
+        set_error("a bounded device wait timed out inside the SpMV kernel");
+        result = HHP_ERR_TIMEOUT;
+    }
+    if (xt && host) {
+        err = 0.0;
+        for (int i = 0; i < A->n; ++i) err = std::max(err, std::fabs(x_io[i] - xt[i]));
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    if (info) {
+        info->iters = total_iters;
+        info->outer_iters = outer;
+        info->half_step = half;
+        info->rel_res_true = rel_true;
+        info->rel_res_recursive = rel_rec;
+        info->err_vs_target = err;
+        info->t_solve_s = ms * 1e-3;
+        info->status = result;
+    }
+    if (o->cb && o->print_every > 0 && total_iters > 0) {
+        const int nh = std::min(total_iters, s->hist_cap);
+        std::vector<double> hh(static_cast<size_t>(nh));
+        HHP_CUDA(cudaMemcpy(hh.data(), s->hist, sizeof(double) * static_cast<size_t>(nh), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < nh; ++i)
+            if ((i + 1) % o->print_every == 0 || i + 1 == nh) o->cb(i + 1, hh[static_cast<size_t>(i)], o->user);
+    }
+    return result;
+}
+
+void solver_release(Solver *s) {
+    if (!s) return;
+    if (s->g64) cudaGraphExecDestroy(s->g64);
+    if (s->gmix) cudaGraphExecDestroy(s->gmix);
+    double *d[] = {s->X, s->B, s->R, s->R0, s->P, s->V, s->S, s->T, s->Y, s->part_xr, s->part_s, s->part_xr32,
+                   s->part_s32, s->hist};
+    for (double *p : d) cudaFree(p);
+    float *f[] = {s->D32, s->R32, s->R0_32, s->P32, s->V32, s->S32, s->T32};
+    for (float *p : f) cudaFree(p);
+    cudaFree(s->sc);
+    cudaFree(s->sc32);
+    cudaFreeHost(s->h_sc);
+    cudaFreeHost(s->h_sc32);
+    if (s->s2) cudaStreamDestroy(s->s2);
+    delete s;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Adjoint: A^T lambda = g on the transpose (same solver), then dL/db = lambda and the fused
+// dL/dA kernel.
+hhp_status backward_dev(hhp_mat *A, const double *x_dev, const double *g_dev, double *dldb_dev, double *dlda_dev,
+                        const hhp_solve_opts *o, hhp_solve_info *info) {
+    HHP_TRY(ensure_transpose(A));
+    hhp_ctx *ctx = A->ctx;
+    cudaStream_t st = ctx->stream;
+    // lambda starts from zero
+    HHP_CUDA(cudaMemsetAsync(dldb_dev, 0, sizeof(double) * static_cast<size_t>(A->n), st));
+    hhp_status rc = solve_dev(A->t, g_dev, dldb_dev, nullptr, o, info);
+    if (rc != HHP_OK && rc != HHP_ERR_MAXIT) return rc;
+    if (dlda_dev) HHP_TRY(launch_dlda(A, st, dldb_dev, x_dev, dlda_dev));
+    HHP_CUDA(cudaStreamSynchronize(st));
+    return rc;
+}
+
+}  // namespace hhp

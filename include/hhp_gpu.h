@@ -1,0 +1,180 @@
+/*
+ * hhp_gpu.h -- C ABI of libhhp_gpu.so: GB300 (sm_103a) BiCGStab and CSR SpMV.
+ *
+ * A drop-in for the single-GPU solver path of HetHypPar. Every entry point takes plain pointers
+ * and sizes. Each declaration names the reference interface it replaces (paths inside the
+ * HetHypPar tree). Functions with a `_dev` suffix take caller-owned DEVICE pointers and run on
+ * the context's stream; the others take caller-owned HOST pointers and copy in and out.
+ *
+ * Conventions
+ *  - Every function returns an hhp_status (never exits the process); hhp_status_str() names it,
+ *    hhp_last_error() gives a one-line description of the most recent failure on this thread.
+ *  - An hhp_ctx owns one CUDA stream on one device; calls on a context are serialised on that
+ *    stream. Use one context per host thread.
+ *  - An hhp_mat owns its device CSR arrays (int32 indices, FP64 values) and everything derived
+ *    from them (the SpMV work plan, an FP32 copy of the values, the transpose), built lazily.
+ *  - Sizes are int (the reference's CSR uses int m, n, nnz: src/include/hhp_common.h:43-50).
+ */
+#ifndef HHP_GPU_H
+#define HHP_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct hhp_ctx hhp_ctx;
+typedef struct hhp_mat hhp_mat;
+
+typedef enum {
+    HHP_OK = 0,
+    HHP_ERR_ARG = 1,       /* invalid argument (null pointer, bad size, non-square for a solve) */
+    HHP_ERR_IO = 2,        /* file could not be opened / read / written, or is short            */
+    HHP_ERR_CUDA = 3,      /* a CUDA runtime call failed                                        */
+    HHP_ERR_OOM = 4,       /* device or host allocation failed                                  */
+    HHP_ERR_BREAKDOWN = 5, /* BiCGStab breakdown: rho, (r0,v) or (t,t) zero or not finite       */
+    HHP_ERR_MAXIT = 6,     /* maxit reached before the tolerance                                */
+    HHP_ERR_TIMEOUT = 7,   /* a bounded device wait gave up                                     */
+    HHP_ERR_FORMAT = 8,    /* Matrix Market banner/size/entry not supported or malformed        */
+    HHP_ERR_STATE = 9      /* call not valid in the object's current state                      */
+} hhp_status;
+
+/* Per-iteration residual callback: iter is 1-based, rel_res is the recursive ||r_k|| / ||r_0||.
+ * Called on the calling thread after the device loop, in iteration order (every `print_every`-th
+ * iteration when print_every > 0). Replaces the "Iteration = %d; Error Norm = %e" lines of
+ * gpu_BiCGStab (src/entry/bicgstab_gpu.c:156). */
+typedef void (*hhp_iter_cb)(int iter, double rel_res, void *user);
+
+typedef enum { HHP_PREC_FP64 = 0, HHP_PREC_MIXED = 1 } hhp_precision;
+
+typedef struct {
+    double rtol;        /* stop when ||b - A x|| <= rtol * ||b - A x0||   (threshold = tol * ||r0||,
+                           gpu_BiCGStab src/entry/bicgstab_gpu.c:149-150)                      */
+    int maxit;          /* iteration cap (maxIterations, bicgstab_gpu.c:120); >= 0                */
+    int precision;      /* hhp_precision                                                          */
+    double inner_rtol;  /* mixed form: relative tolerance of each FP32 inner solve (<= 0: 1e-5)   */
+    int max_outer;      /* mixed form: cap on FP64 refinement steps (<= 0: 50)                    */
+    int fixed_iters;    /* 1: run exactly maxit iterations with no stop test, like the reference's
+                           executables (src/entry/bicgstab_cpu.c:200); FP64 only                  */
+    int print_every;    /* callback stride; 0 = no callback                                       */
+    hhp_iter_cb cb;
+    void *user;
+} hhp_solve_opts;
+
+typedef struct {
+    int iters;                 /* BiCGStab iterations (mixed: total inner iterations)            */
+    int outer_iters;           /* mixed: FP64 refinement steps; FP64: residual replacements + 1  */
+    int half_step;             /* 1 if the last iteration stopped at the ||s|| test              */
+    double rel_res_true;       /* ||b - A x|| / ||b||, recomputed in FP64 after the solve         */
+    double rel_res_recursive;  /* the solver's own ||r_k|| / ||r_0||                              */
+    double err_vs_target;      /* max_i |x_i - x_target_i| (NaN when no target was given)        */
+    double t_solve_s;          /* device time of the solve (CUDA events on the context stream)   */
+    hhp_status status;
+} hhp_solve_info;
+
+/* ---- errors -------------------------------------------------------------------------------- */
+const char *hhp_status_str(hhp_status s);
+const char *hhp_last_error(void);
+
+/* ---- context: replaces cudaSetDevice + cusparseCreate/cublasCreate of the entries
+ *      (src/entry/bicgstab_gpu_dp.c:97-99) --------------------------------------------------- */
+hhp_status hhp_ctx_create(int device, hhp_ctx **out);
+void hhp_ctx_destroy(hhp_ctx *ctx);
+/* The context's cudaStream_t, as an opaque pointer. */
+void *hhp_ctx_stream(hhp_ctx *ctx);
+hhp_status hhp_ctx_sync(hhp_ctx *ctx);
+/* Number of kernels this context has launched (graph launches count their kernel nodes). */
+long long hhp_ctx_kernel_launches(const hhp_ctx *ctx);
+
+/* ---- matrices: replace device_csr_create / device_csr_destroy (src/util/hhp_cuda.c:19-51,
+ *      src/include/hhp_cuda.h:46-47) and buReadSparseMatrix (src/util/hhp_matrix.c:116) -------- */
+/* Host CSR (0-based, int32), copied to the device. Entries of a row are used in the given order.
+ * perm (nullable, length m, a permutation of 0..m-1; needs m == n) reorders the matrix as
+ * csr_permute does (src/util/hhp_dp_helpers.c:18-37): row i of the result is row perm[i] of A
+ * and column j becomes perm_inv[j]. */
+hhp_status hhp_mat_from_csr(hhp_ctx *ctx, int m, int n, int nnz, const int *rowptr, const int *col,
+                            const double *val, const int *perm, hhp_mat **out);
+/* Same, from device arrays (copied; the caller keeps ownership). */
+hhp_status hhp_mat_from_csr_dev(hhp_ctx *ctx, int m, int n, int nnz, const int *rowptr_dev, const int *col_dev,
+                                const double *val_dev, hhp_mat **out);
+/* Matrix Market coordinate real/integer general file (readMatrixMarketFromFile,
+ * src/util/hhp_wrap_bora.c:13-104): rows in order, entries of a row in file order. */
+hhp_status hhp_mat_from_mtx(hhp_ctx *ctx, const char *path, hhp_mat **out);
+void hhp_mat_destroy(hhp_mat *mat);
+hhp_status hhp_mat_shape(const hhp_mat *mat, int *m, int *n, int *nnz);
+/* Replace the values (same pattern) from host or device memory; derived copies are refreshed. */
+hhp_status hhp_mat_set_values(hhp_mat *mat, const double *val);
+hhp_status hhp_mat_set_values_dev(hhp_mat *mat, const double *val_dev);
+/* Copy the device CSR back to host arrays (m+1, nnz, nnz; any may be NULL). */
+hhp_status hhp_mat_get_csr(const hhp_mat *mat, int *rowptr, int *col, double *val);
+/* Host CSR of A^T built on the device (count, scan, scatter; within a row of A^T entries are in
+ * increasing row order of A, as CSR_to_CSC src/util/hhp_matrix.c:1476-1535). Arrays n+1, nnz, nnz. */
+hhp_status hhp_mat_get_transpose(hhp_mat *mat, int *t_rowptr, int *t_col, double *t_val);
+
+/* ---- SpMV: replaces device_csr_spmv (src/util/hhp_cuda.c:226-236): y = alpha*A*x + beta*y ---- */
+hhp_status hhp_spmv_dev(hhp_ctx *ctx, hhp_mat *mat, double alpha, const double *x_dev, double beta, double *y_dev);
+/* FP32 values (a rounded copy of A) and FP32 vectors, FP32 accumulation. */
+hhp_status hhp_spmv_f32_dev(hhp_ctx *ctx, hhp_mat *mat, const float *x_dev, float *y_dev);
+/* y = A^T x on the device-built transpose. */
+hhp_status hhp_spmv_t_dev(hhp_ctx *ctx, hhp_mat *mat, const double *x_dev, double *y_dev);
+/* Host-buffer SpMV, y = A x (copies in and out; the spmv-gpu path, src/entry/spmv_gpu.c:100-130). */
+hhp_status hhp_spmv(hhp_ctx *ctx, hhp_mat *mat, const double *x, double *y);
+
+/* ---- BiCGStab: replaces gpu_BiCGStab (src/entry/bicgstab_gpu.c:106-310) and the loop of
+ *      bicgstab-gpu-dp (src/entry/bicgstab_gpu_dp.c:123-208) ---------------------------------- */
+/* Host pointers: b (m), x (n; in: X_init, out: X), x_target (nullable). opts NULL = defaults
+ * (rtol 1e-10, maxit 2000, FP64). info may be NULL. Returns HHP_OK when the true relative
+ * residual reached rtol, HHP_ERR_MAXIT / HHP_ERR_BREAKDOWN otherwise (x holds the last iterate). */
+hhp_status hhp_bicgstab(hhp_ctx *ctx, hhp_mat *mat, const double *b, double *x, const double *x_target,
+                        const hhp_solve_opts *opts, hhp_solve_info *info);
+/* Device pointers, same semantics. */
+hhp_status hhp_bicgstab_dev(hhp_ctx *ctx, hhp_mat *mat, const double *b_dev, double *x_dev,
+                            const double *x_target_dev, const hhp_solve_opts *opts, hhp_solve_info *info);
+
+/* ---- adjoint (no reference counterpart): given x = A^-1 b and g = dL/dx, solve A^T lambda = g
+ *      with the same BiCGStab on the transpose, then dL/db = lambda and
+ *      dL/dA_ij = -lambda_i * x_j over A's sparsity pattern (one value per stored entry). ------- */
+hhp_status hhp_bicgstab_backward_dev(hhp_ctx *ctx, hhp_mat *mat, const double *x_dev, const double *dldx_dev,
+                                     double *dldb_dev, double *dlda_vals_dev, const hhp_solve_opts *opts,
+                                     hhp_solve_info *info);
+hhp_status hhp_bicgstab_backward(hhp_ctx *ctx, hhp_mat *mat, const double *x, const double *dldx, double *dldb,
+                                 double *dlda_vals, const hhp_solve_opts *opts, hhp_solve_info *info);
+
+/* ---- vector files: vector_read / vector_write (src/util/hhp_cpu.c:411-442) ------------------- */
+/* Reads exactly `size` whitespace-separated doubles; HHP_ERR_IO if the file is missing or short. */
+hhp_status hhp_vector_read(const char *path, int size, double *out);
+/* exact = 0: "%lf" (6 decimals, as the reference); exact = 1: "%.17g" (round-trip). */
+hhp_status hhp_vector_write(const char *path, int size, const double *v, int exact);
+
+/* Host-only Matrix Market read (no device needed), same rules as hhp_mat_from_mtx. The arrays
+ * are allocated with malloc (m+1, nnz, nnz); release each with hhp_free. */
+hhp_status hhp_mtx_read(const char *path, int *m, int *n, int *nnz, int **rowptr, int **col, double **val);
+void hhp_free(void *p);
+
+/* ---- host-side helpers exposed for testing the work plan without a GPU ---------------------- */
+/* The SpMV work plan for a host CSR: number of warp work lists, items and long-row chunks. */
+hhp_status hhp_plan_stats(int m, int nnz, const int *rowptr, int n_warps, int cap, int *n_items, int *n_long_rows,
+                          int *n_chunks, int *max_item_nnz, double *imbalance);
+/* The plan itself: items_out receives 4 ints per item (first row, kind<<30 | payload, k0, k1)
+ * for up to `capacity` items; warp_begin_out (n_warps+1 ints) the per-warp item ranges.
+ * *n_items is always set; HHP_ERR_ARG if capacity is too small. */
+hhp_status hhp_plan_dump(int m, int nnz, const int *rowptr, int n_warps, int cap, int capacity, int *items_out,
+                         int *warp_begin_out, int *n_items);
+
+/* ---- drop-ins for the reference's device-pointer launchers (src/include/hhp_dp_kernels.h:37-59).
+ *      Same names, arguments and meaning; `s` is a cudaStream_t. Unlike the reference's
+ *      one-thread kernels, the scalar updates here are single-thread kernels too (there is no
+ *      work to spread), and the vector ops use 128-bit loads. ---------------------------------- */
+void hhp_dp_vecop_P(double *P, const double *V, const double *R, const double *omega, const double *beta, int n,
+                    void *s);
+void hhp_dp_vecop_S(double *S, const double *R, const double *V, const double *neg_alpha, int n, void *s);
+void hhp_dp_vecop_XR(double *X, double *R, const double *P, const double *S, const double *T,
+                     const double *alpha, const double *omega, const double *neg_omega, int n, void *s);
+void hhp_dp_update_beta(double *beta, double *rho_old, const double *rho_new, const double *alpha,
+                        const double *omega, void *s);
+void hhp_dp_update_alpha(double *alpha, double *neg_alpha, const double *rho, const double *rv, void *s);
+void hhp_dp_update_omega(double *omega, double *neg_omega, const double *ts, const double *tt, void *s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HHP_GPU_H */

@@ -1,0 +1,142 @@
+"""BiCGStab on the GPU against the reference's loop (goldens) and the oracle.
+
+Bars (the reference has no stop test, so its iteration count to a tolerance is the smallest k
+whose fixed-k run reaches it):
+  * iterations to true rel-res 1e-10 within 5% (at least +-1) of the reference's count, and a
+    true relative residual <= 1e-10;
+  * fixed-k runs (no stop test, the reference's executables) follow the reference's iterates:
+    the residual after k steps within a factor 10 of the reference's (or both below 1e-13);
+  * bit-identical results run to run, and between the host and device entry points."""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden_names, load_golden
+from gpu_util import dev
+from hethyppar_gb300 import HHPError, Matrix, bicgstab, synth
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+SOLVE_CASES = [n for n in golden_names() if n not in ("crafted5",)]
+
+
+def _within_5pct(k_gpu, k_ref):
+    return abs(k_gpu - k_ref) <= max(1, math.ceil(0.05 * k_ref))
+
+
+@pytest.mark.parametrize("name", SOLVE_CASES)
+def test_fixed_iterations_follow_reference(ctx, name):
+    g = load_golden(name)
+    A = Matrix.from_csr(ctx, g["rowptr"], g["col"], g["val"])
+    for k in g["ks"]:
+        x, r = bicgstab(ctx, A, g["b"], g["x0"], rtol=0.0, maxit=int(k), fixed_iters=True)
+        assert r.iters == k
+        rr_ref = float(g[f"relres_k{k}"])
+        if rr_ref > 1e-13 or r.rel_res_true > 1e-13:
+            assert 0.1 <= r.rel_res_true / rr_ref <= 10.0, (k, r.rel_res_true, rr_ref)
+        xr = g[f"x_k{k}"]
+        assert np.max(np.abs(x - xr)) <= 1e-6 * np.max(np.abs(xr)) + 1e3 * rr_ref * np.max(np.abs(xr))
+
+
+@pytest.mark.parametrize("name", SOLVE_CASES)
+def test_iterations_to_tolerance_match_reference(ctx, name):
+    g = load_golden(name)
+    k_ref = int(g["iters_to_1e-10"])
+    A = Matrix.from_csr(ctx, g["rowptr"], g["col"], g["val"])
+    x, r = bicgstab(ctx, A, g["b"], g["x0"], g.get("x_target"), rtol=1e-10, maxit=max(len(g["relres_hist"]), 10))
+    if k_ref < 0:  # the reference does not reach 1e-10 either (stagnation): no convergence claimed
+        assert r.status in (0, 6, 5)
+        return
+    assert r.status == 0
+    assert r.rel_res_true <= 1e-10
+    assert _within_5pct(r.iters, k_ref), (r.iters, k_ref)
+    # the oracle's independent true residual of the returned x
+    res = g["b"] - orc.spmv(g["rowptr"], g["col"], g["val"], x)
+    assert math.sqrt(orc.dot(res, res) / orc.dot(g["b"], g["b"])) <= 1.0000001e-10
+
+
+@pytest.mark.parametrize("cfg", ["c1", "c2"])
+def test_full_size_configs_against_oracle(ctx, cfg):
+    s = synth.config(cfg)
+    k_ref, x_ref, rr_ref = orc.iters_to_tol(s.rowptr, s.col, s.val, s.b, s.x0, 1e-10, 3000)
+    assert k_ref > 0
+    A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
+    x, r = bicgstab(ctx, A, s.b, s.x0, s.x_target, rtol=1e-10, maxit=3000)
+    assert r.status == 0 and r.rel_res_true <= 1e-10 and r.rel_res_true <= max(rr_ref, 1e-10)
+    assert _within_5pct(r.iters, k_ref), (r.iters, k_ref)
+    assert r.err_vs_target <= 1e-6
+
+
+def test_device_and_host_entry_points_agree_and_repeat(ctx):
+    s = synth.config("c1")
+    A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
+    x_h, r_h = bicgstab(ctx, A, s.b, s.x0, rtol=1e-10, maxit=2000)
+    x_h2, _ = bicgstab(ctx, A, s.b, s.x0, rtol=1e-10, maxit=2000)
+    xd = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+    xd, r_d = bicgstab(ctx, A, dev(s.b), xd, dev(s.x_target), rtol=1e-10, maxit=2000)
+    assert np.array_equal(x_h, x_h2)
+    assert np.array_equal(x_h, xd.cpu().numpy())
+    assert r_h.iters == r_d.iters and r_d.err_vs_target <= 1e-6
+
+
+def test_history_callback(ctx):
+    g = load_golden("convdiff2d_32")
+    A = Matrix.from_csr(ctx, g["rowptr"], g["col"], g["val"])
+    seen = []
+    x, r = bicgstab(ctx, A, g["b"], g["x0"], rtol=1e-10, maxit=500, callback=lambda i, e: seen.append((i, e)),
+                    print_every=1)
+    assert [i for i, _ in seen] == list(range(1, r.iters + 1))
+    assert seen[-1][1] <= 1e-10 and seen[0][1] < 1.0
+    assert abs(seen[-1][1] - r.rel_res_recursive) <= 1e-12 * max(r.rel_res_recursive, 1e-30) + 1e-300
+
+
+def test_maxit_and_exact_start(ctx):
+    g = load_golden("convdiff2d_32")
+    A = Matrix.from_csr(ctx, g["rowptr"], g["col"], g["val"])
+    x, r = bicgstab(ctx, A, g["b"], g["x0"], rtol=1e-10, maxit=3)
+    assert r.status == 6 and r.iters == 3
+    x, r = bicgstab(ctx, A, g["b"], g["x0"], rtol=1e-10, maxit=0)
+    assert r.status == 6 and r.iters == 0 and np.array_equal(x, g["x0"])
+    b = orc.spmv(g["rowptr"], g["col"], g["val"], g["x_target"])
+    x, r = bicgstab(ctx, A, b, g["x_target"], rtol=1e-10, maxit=10)
+    assert r.status == 0 and r.iters == 0 and np.array_equal(x, g["x_target"])
+
+
+def test_breakdown_and_bad_input(ctx):
+    # a zero matrix: (r0, v) = 0 at the first step
+    m = 8
+    rp = np.arange(m + 1, dtype=np.int32)
+    A = Matrix.from_csr(ctx, rp, np.arange(m, dtype=np.int32), np.zeros(m))
+    x, r = bicgstab(ctx, A, np.ones(m), None, rtol=1e-10, maxit=10, raise_on_error=False)
+    assert r.status == 5
+    # NaN in b
+    A2 = Matrix.from_csr(ctx, rp, np.arange(m, dtype=np.int32), np.ones(m))
+    b = np.ones(m)
+    b[3] = np.nan
+    x, r = bicgstab(ctx, A2, b, None, rtol=1e-10, maxit=10, raise_on_error=False)
+    assert r.status == 5
+    # non-square
+    A3 = Matrix.from_csr(ctx, np.array([0, 1], np.int32), np.array([1], np.int32), np.ones(1), shape=(1, 2))
+    with pytest.raises(HHPError) as e:
+        bicgstab(ctx, A3, np.ones(1), np.zeros(2))
+    assert e.value.status == 1
+    # invalid CSR
+    with pytest.raises(HHPError):
+        Matrix.from_csr(ctx, np.array([0, 2, 1], np.int32), np.array([0, 1], np.int32), np.ones(2))
+    with pytest.raises(HHPError):
+        Matrix.from_csr(ctx, np.array([0, 1], np.int32), np.array([5], np.int32), np.ones(1))
+
+
+def test_permutation_solve(ctx):
+    g = load_golden("sample320")
+    A = Matrix.from_csr(ctx, g["rowptr"], g["col"], g["val"], perm=g["perm"])
+    rp, col, val = A.get_csr()
+    assert np.array_equal(rp, g["perm_rowptr"]) and np.array_equal(col, g["perm_col"]) and \
+        np.array_equal(val, g["perm_val"])
+    p = g["perm"]
+    x, r = bicgstab(ctx, A, g["b"][p], g["x0"][p], rtol=1e-12, maxit=200)
+    xx = np.empty_like(x)
+    xx[p] = x
+    assert np.max(np.abs(xx - np.arange(1, 321))) < 1e-8
