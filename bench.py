@@ -343,6 +343,50 @@ def run_ours(args, rk):
     return out
 
 
+def run_spmv_only(args):
+    """SpMV alone on one configuration: used for kernel sweeps and as the ncu capture target.
+    Prints one JSON line with the L2-flushed and warm-L2 timings."""
+    import torch
+    from hethyppar_gb300 import Context, Matrix, spmv_bytes, synth
+    ctx = Context(0)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    s = synth.config(args.config)
+    A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
+    fp32 = args.precision == "fp32"
+    dt = torch.float32 if fp32 else torch.float64
+    x = torch.randn(s.n, dtype=dt, device="cuda")
+    y = torch.empty(s.m, dtype=dt, device="cuda")
+    run = (lambda: A.spmv_f32_dev(x, y)) if fp32 else (lambda: A.spmv_dev(x, y))
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        run()
+    torch.cuda.synchronize()
+    cold = []
+    for _ in range(args.steps):
+        flush.add_(1.0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        run()
+        e1.record(stream)
+        e1.synchronize()
+        cold.append(e0.elapsed_time(e1))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        run()
+    e1.record(stream)
+    e1.synchronize()
+    warm = e0.elapsed_time(e1) / args.steps
+    hbm, kind = peaks()
+    nb = spmv_bytes(s.m, s.n, s.nnz, fp32)
+    t = statistics.median(cold) * 1e-3
+    print(json.dumps({"mode": "spmv", "config": args.config, "precision": args.precision, "m": s.m, "nnz": s.nnz,
+                      "bytes": nb, "us_l2_flushed": t * 1e6, "gbs_l2_flushed": nb / t / 1e9,
+                      "frac_of_hbm": nb / t / 1e9 / hbm, "us_warm": warm * 1e3, "gbs_warm": nb / (warm * 1e-3) / 1e9,
+                      "env": {k: v for k, v in os.environ.items() if k.startswith("HHP_")}}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -352,7 +396,14 @@ def main():
     ap.add_argument("--no-extras", dest="extras", action="store_false")
     ap.add_argument("--extra-reps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mode", default="solve", choices=["solve", "spmv"],
+                    help="spmv: time the SpMV kernel alone on --config (kernel sweeps, profiler target)")
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     args = ap.parse_args()
+    if args.mode == "spmv":
+        run_spmv_only(args)
+        return
     from hethyppar_gb300 import dist
     rk = dist.init_from_env()
     if args.impl == "reference":

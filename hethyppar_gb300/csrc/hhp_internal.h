@@ -151,7 +151,7 @@ inline int pad4(int n) { return (n + 3) & ~3; }
 
 // Kernel tuning knobs (environment overrides read once).
 struct Tuning {
-    int cap64 = 512, cap32 = 1024, med = 64, wpc = 12, ns = 2, vec_blocks_per_sm = 2, unroll_iters = 4;
+    int cap64 = 512, cap32 = 1024, med = 64, wpc = 12, ns = 3, vec_blocks_per_sm = 2, unroll_iters = 4;
 };
 const Tuning &tuning();
 

@@ -43,7 +43,9 @@ struct Geom {
     __host__ __device__ int col_bytes() const { return align16((cap + 8) * 4); }
     __host__ __device__ int rp_bytes() const { return align16(kRowPtrElems * 4); }
     __host__ __device__ int stage_bytes() const { return val_bytes() + col_bytes() + rp_bytes(); }
-    __host__ __device__ int warp_bytes(int ns) const { return kBarBytes + ns * stage_bytes(); }
+    // gathered x values of the item being computed (one buffer per warp)
+    __host__ __device__ int xs_bytes() const { return align16(cap * static_cast<int>(sizeof(VT))); }
+    __host__ __device__ int warp_bytes(int ns) const { return kBarBytes + ns * stage_bytes() + xs_bytes(); }
 };
 
 template <typename VT>
@@ -114,6 +116,7 @@ __global__ void __launch_bounds__(512, 1) k_spmv(const SpmvArgs<VT> a) {
     uint64_t *bar = reinterpret_cast<uint64_t *>(wb);
     unsigned char *stage_base = wb + kBarBytes;
     const int sbytes = geo.stage_bytes();
+    VT *xs = reinterpret_cast<VT *>(stage_base + NS * sbytes);
     double *red = reinterpret_cast<double *>(smem + static_cast<size_t>(nw) * a.warp_smem);
 
     if (lane == 0) {
@@ -170,6 +173,24 @@ __global__ void __launch_bounds__(512, 1) k_spmv(const SpmvArgs<VT> a) {
         const int k0a = d.z & ~(VPA - 1), k0c = d.z & ~3;
         const VT *sv = reinterpret_cast<const VT *>(st);
         const int *sc = reinterpret_cast<const int *>(st + geo.val_bytes());
+        // Gather pass: the whole warp fetches x for every nonzero of the item, lane-strided and
+        // in batches of 8 independent loads per lane, so one item costs about one L2 round trip
+        // instead of one per nonzero of the longest row. Values land in xs (item-relative).
+        const int nk = d.w - d.z;
+        for (int base = 0; base < nk; base += 32 * 8) {
+            VT v[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int kk = base + lane + 32 * j;
+                v[j] = kk < nk ? __ldg(a.x + sc[d.z + kk - k0c]) : VT(0);
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int kk = base + lane + 32 * j;
+                if (kk < nk) xs[kk] = v[j];
+            }
+        }
+        __syncwarp();
         if (kind == KIND_ROWS) {
             const int nrows = d.y & PAYLOAD_MASK;
             const int r0a = d.x & ~3;
@@ -178,23 +199,14 @@ __global__ void __launch_bounds__(512, 1) k_spmv(const SpmvArgs<VT> a) {
                 const int r = d.x + lane;
                 const int kb = sr[r - r0a], ke = sr[r + 1 - r0a];
                 VT acc = VT(0);
-                int k = kb;
-                for (; k + 4 <= ke; k += 4) {
-                    const int c0 = sc[k - k0c], c1 = sc[k + 1 - k0c], c2 = sc[k + 2 - k0c], c3 = sc[k + 3 - k0c];
-                    const VT x0 = __ldg(a.x + c0), x1 = __ldg(a.x + c1), x2 = __ldg(a.x + c2), x3 = __ldg(a.x + c3);
-                    acc = vfma(sv[k - k0a], x0, acc);
-                    acc = vfma(sv[k + 1 - k0a], x1, acc);
-                    acc = vfma(sv[k + 2 - k0a], x2, acc);
-                    acc = vfma(sv[k + 3 - k0a], x3, acc);
-                }
-                for (; k < ke; ++k) acc = vfma(sv[k - k0a], __ldg(a.x + sc[k - k0c]), acc);
+                for (int k = kb; k < ke; ++k) acc = vfma(sv[k - k0a], xs[k - d.z], acc);
                 row_epilogue<VT, EP>(a, r, acc, d0, d1);
             }
         } else {
             // One row (VEC) or one slice of a long row (CHUNK), summed by the warp: lane l takes
             // entries l, l+32, ... in order; the 32 lane sums meet in a fixed butterfly.
             VT acc = VT(0);
-            for (int k = d.z + lane; k < d.w; k += 32) acc = vfma(sv[k - k0a], __ldg(a.x + sc[k - k0c]), acc);
+            for (int k = d.z + lane; k < d.w; k += 32) acc = vfma(sv[k - k0a], xs[k - d.z], acc);
             acc = warp_sum_t<VT>(acc);
             if (kind == KIND_VEC) {
                 if (lane == 0) row_epilogue<VT, EP>(a, d.x, acc, d0, d1);
