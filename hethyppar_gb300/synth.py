@@ -14,6 +14,7 @@ them nonsymmetric and diagonally dominant.
 """
 from __future__ import annotations
 
+import os
 from dataclasses import dataclass
 from typing import Optional
 
@@ -201,8 +202,25 @@ def powerlaw(m: int = 3_500_000, a: float = 2.1, max_len: int = 100_000, n_dense
     return System(f"powerlaw_{m}", rp, col, val, b, np.zeros(m), ones)
 
 
-# The five benchmark configurations, by name.
 def config(name: str) -> System:
+    """The five benchmark configurations by name (c1..c5). When HHP_SYNTH_CACHE names a
+    directory, generated systems are cached there as .npz files."""
+    cache = os.environ.get("HHP_SYNTH_CACHE")
+    if cache:
+        path = os.path.join(cache, f"{name}.npz")
+        if os.path.exists(path):
+            d = np.load(path)
+            xt = d["x_target"] if d["x_target"].size else None
+            return System(str(d["name"]), d["rowptr"], d["col"], d["val"], d["b"], d["x0"], xt)
+        s = _config(name)
+        os.makedirs(cache, exist_ok=True)
+        np.savez(path, name=np.array(s.name), rowptr=s.rowptr, col=s.col, val=s.val, b=s.b, x0=s.x0,
+                 x_target=s.x_target if s.x_target is not None else np.zeros(0))
+        return s
+    return _config(name)
+
+
+def _config(name: str) -> System:
     if name == "c1":
         return convdiff2d(256, 50.0, (1.0, 0.5), seed=0, name="c1_convdiff2d")
     if name == "c2":
