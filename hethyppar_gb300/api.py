@@ -8,6 +8,7 @@ from __future__ import annotations
 
 import ctypes
 import math
+import weakref
 from dataclasses import dataclass, field
 from typing import Callable, List, Optional
 
@@ -42,6 +43,7 @@ class Context:
         check(lib().hhp_ctx_create(device, ctypes.byref(h)), "hhp_ctx_create")
         self._h = h
         self.device = device
+        self._mats = weakref.WeakSet()  # matrices are destroyed before their context
 
     @property
     def handle(self):
@@ -58,8 +60,14 @@ class Context:
     def kernel_launches(self) -> int:
         return int(lib().hhp_ctx_kernel_launches(self._h))
 
+    @property
+    def alive(self) -> bool:
+        return bool(self._h)
+
     def close(self):
         if self._h:
+            for m in list(self._mats):
+                m.close()
             lib().hhp_ctx_destroy(self._h)
             self._h = None
 
@@ -76,6 +84,7 @@ class Matrix:
     def __init__(self, ctx: Context, handle: ctypes.c_void_p):
         self.ctx = ctx
         self._h = handle
+        ctx._mats.add(self)
         m, n, nnz = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         check(lib().hhp_mat_shape(handle, ctypes.byref(m), ctypes.byref(n), ctypes.byref(nnz)), "hhp_mat_shape")
         self.shape = (m.value, n.value)
@@ -112,9 +121,11 @@ class Matrix:
         return self._h
 
     def close(self):
-        if self._h:
+        # A matrix must not outlive its context's stream: after the context is closed the
+        # handle is already gone (Context.close destroys its matrices first).
+        if self._h and self.ctx.alive:
             lib().hhp_mat_destroy(self._h)
-            self._h = None
+        self._h = None
 
     def __del__(self):
         try:

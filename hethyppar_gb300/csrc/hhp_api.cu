@@ -46,6 +46,8 @@ const Tuning &tuning() {
         d.med = env_int("HHP_SPMV_MED", d.med);
         d.wpc = env_int("HHP_SPMV_WPC", d.wpc);
         d.ns = env_int("HHP_SPMV_NS", d.ns);
+        d.ctas_per_sm = env_int("HHP_SPMV_CPS", d.ctas_per_sm);
+        d.gather = env_int("HHP_SPMV_GATHER", d.gather);
         d.vec_blocks_per_sm = env_int("HHP_VEC_BLOCKS_PER_SM", d.vec_blocks_per_sm);
         d.unroll_iters = env_int("HHP_UNROLL_ITERS", d.unroll_iters);
         return d;

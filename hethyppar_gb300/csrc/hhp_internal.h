@@ -60,6 +60,7 @@ void build_plan(int m, const int *rowptr, int n_warps, int cap, int med, PlanHos
 struct PlanDev {
     int n_warps = 0, cap = 0, n_items = 0, n_long = 0, n_chunks = 0;
     int ctas = 0, warps_per_cta = 0, ns = 0;
+    bool gather = false;
     size_t smem_bytes = 0;
     int4 *items = nullptr;
     int *warp_begin = nullptr;
@@ -151,7 +152,8 @@ inline int pad4(int n) { return (n + 3) & ~3; }
 
 // Kernel tuning knobs (environment overrides read once).
 struct Tuning {
-    int cap64 = 512, cap32 = 1024, med = 64, wpc = 12, ns = 3, vec_blocks_per_sm = 2, unroll_iters = 4;
+    int cap64 = 512, cap32 = 1024, med = 64, wpc = 12, ns = 2, ctas_per_sm = 1, gather = 1, vec_blocks_per_sm = 2,
+        unroll_iters = 4;
 };
 const Tuning &tuning();
 

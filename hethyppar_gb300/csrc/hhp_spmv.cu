@@ -45,7 +45,9 @@ struct Geom {
     __host__ __device__ int stage_bytes() const { return val_bytes() + col_bytes() + rp_bytes(); }
     // gathered x values of the item being computed (one buffer per warp)
     __host__ __device__ int xs_bytes() const { return align16(cap * static_cast<int>(sizeof(VT))); }
-    __host__ __device__ int warp_bytes(int ns) const { return kBarBytes + ns * stage_bytes() + xs_bytes(); }
+    __host__ __device__ int warp_bytes(int ns, bool gather) const {
+        return kBarBytes + ns * stage_bytes() + (gather ? xs_bytes() : 0);
+    }
 };
 
 template <typename VT>
@@ -103,8 +105,8 @@ __device__ __forceinline__ VT warp_sum_t(VT v) {
     return warp_sum(v);
 }
 
-template <typename VT, int NS, int EP>
-__global__ void __launch_bounds__(512, 1) k_spmv(const SpmvArgs<VT> a) {
+template <typename VT, int NS, int EP, bool GATHER>
+__global__ void __launch_bounds__(512) k_spmv(const SpmvArgs<VT> a) {
     extern __shared__ __align__(128) unsigned char smem[];
     // After a recorded device error every later launch returns at once (uniform across the CTA).
     if (*reinterpret_cast<volatile const int *>(a.err) != DEV_OK) return;
@@ -116,7 +118,7 @@ __global__ void __launch_bounds__(512, 1) k_spmv(const SpmvArgs<VT> a) {
     uint64_t *bar = reinterpret_cast<uint64_t *>(wb);
     unsigned char *stage_base = wb + kBarBytes;
     const int sbytes = geo.stage_bytes();
-    VT *xs = reinterpret_cast<VT *>(stage_base + NS * sbytes);
+    VT *xs = GATHER ? reinterpret_cast<VT *>(stage_base + NS * sbytes) : nullptr;
     double *red = reinterpret_cast<double *>(smem + static_cast<size_t>(nw) * a.warp_smem);
 
     if (lane == 0) {
@@ -176,21 +178,23 @@ __global__ void __launch_bounds__(512, 1) k_spmv(const SpmvArgs<VT> a) {
         // Gather pass: the whole warp fetches x for every nonzero of the item, lane-strided and
         // in batches of 8 independent loads per lane, so one item costs about one L2 round trip
         // instead of one per nonzero of the longest row. Values land in xs (item-relative).
-        const int nk = d.w - d.z;
-        for (int base = 0; base < nk; base += 32 * 8) {
-            VT v[8];
+        if (GATHER) {
+            const int nk = d.w - d.z;
+            for (int base = 0; base < nk; base += 32 * 8) {
+                VT v[8];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const int kk = base + lane + 32 * j;
-                v[j] = kk < nk ? __ldg(a.x + sc[d.z + kk - k0c]) : VT(0);
-            }
+                for (int j = 0; j < 8; ++j) {
+                    const int kk = base + lane + 32 * j;
+                    v[j] = kk < nk ? __ldg(a.x + sc[d.z + kk - k0c]) : VT(0);
+                }
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const int kk = base + lane + 32 * j;
-                if (kk < nk) xs[kk] = v[j];
+                for (int j = 0; j < 8; ++j) {
+                    const int kk = base + lane + 32 * j;
+                    if (kk < nk) xs[kk] = v[j];
+                }
             }
+            __syncwarp();
         }
-        __syncwarp();
         if (kind == KIND_ROWS) {
             const int nrows = d.y & PAYLOAD_MASK;
             const int r0a = d.x & ~3;
@@ -199,14 +203,28 @@ __global__ void __launch_bounds__(512, 1) k_spmv(const SpmvArgs<VT> a) {
                 const int r = d.x + lane;
                 const int kb = sr[r - r0a], ke = sr[r + 1 - r0a];
                 VT acc = VT(0);
-                for (int k = kb; k < ke; ++k) acc = vfma(sv[k - k0a], xs[k - d.z], acc);
+                if (GATHER) {
+                    for (int k = kb; k < ke; ++k) acc = vfma(sv[k - k0a], xs[k - d.z], acc);
+                } else {
+                    // gathers issued 8 at a time ahead of their multiply-adds
+                    int k = kb;
+                    for (; k + 8 <= ke; k += 8) {
+                        VT xv[8];
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) xv[j] = __ldg(a.x + sc[k + j - k0c]);
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) acc = vfma(sv[k + j - k0a], xv[j], acc);
+                    }
+                    for (; k < ke; ++k) acc = vfma(sv[k - k0a], __ldg(a.x + sc[k - k0c]), acc);
+                }
                 row_epilogue<VT, EP>(a, r, acc, d0, d1);
             }
         } else {
             // One row (VEC) or one slice of a long row (CHUNK), summed by the warp: lane l takes
             // entries l, l+32, ... in order; the 32 lane sums meet in a fixed butterfly.
             VT acc = VT(0);
-            for (int k = d.z + lane; k < d.w; k += 32) acc = vfma(sv[k - k0a], xs[k - d.z], acc);
+            for (int k = d.z + lane; k < d.w; k += 32)
+                acc = vfma(sv[k - k0a], GATHER ? xs[k - d.z] : __ldg(a.x + sc[k - k0c]), acc);
             acc = warp_sum_t<VT>(acc);
             if (kind == KIND_VEC) {
                 if (lane == 0) row_epilogue<VT, EP>(a, d.x, acc, d0, d1);
@@ -268,9 +286,9 @@ __global__ void __launch_bounds__(512, 1) k_spmv(const SpmvArgs<VT> a) {
     }
 }
 
-template <typename VT, int NS, int EP>
+template <typename VT, int NS, int EP, bool G>
 cudaError_t launch_one(const PlanDev &p, const SpmvArgs<VT> &a, cudaStream_t s) {
-    auto fn = k_spmv<VT, NS, EP>;
+    auto fn = k_spmv<VT, NS, EP, G>;
     static std::once_flag once;
     static cudaError_t attr_err = cudaSuccess;
     std::call_once(once, [&] {
@@ -281,22 +299,27 @@ cudaError_t launch_one(const PlanDev &p, const SpmvArgs<VT> &a, cudaStream_t s) 
     return cudaGetLastError();
 }
 
-template <typename VT, int EP>
+template <typename VT, int EP, bool G>
 cudaError_t launch_ns(const PlanDev &p, const SpmvArgs<VT> &a, cudaStream_t s) {
     switch (p.ns) {
-        case 3: return launch_one<VT, 3, EP>(p, a, s);
-        case 4: return launch_one<VT, 4, EP>(p, a, s);
-        default: return launch_one<VT, 2, EP>(p, a, s);
+        case 1: return launch_one<VT, 1, EP, G>(p, a, s);
+        case 3: return launch_one<VT, 3, EP, G>(p, a, s);
+        default: return launch_one<VT, 2, EP, G>(p, a, s);
     }
+}
+
+template <typename VT, int EP>
+cudaError_t launch_g(const PlanDev &p, const SpmvArgs<VT> &a, cudaStream_t s) {
+    return p.gather ? launch_ns<VT, EP, true>(p, a, s) : launch_ns<VT, EP, false>(p, a, s);
 }
 
 template <typename VT>
 cudaError_t launch_ep(EpKind ep, const PlanDev &p, const SpmvArgs<VT> &a, cudaStream_t s) {
     switch (ep) {
-        case EP_DOT1: return launch_ns<VT, EP_DOT1>(p, a, s);
-        case EP_DOT2: return launch_ns<VT, EP_DOT2>(p, a, s);
-        case EP_RESID: return launch_ns<VT, EP_RESID>(p, a, s);
-        default: return launch_ns<VT, EP_AXPBY>(p, a, s);
+        case EP_DOT1: return launch_g<VT, EP_DOT1>(p, a, s);
+        case EP_DOT2: return launch_g<VT, EP_DOT2>(p, a, s);
+        case EP_RESID: return launch_g<VT, EP_RESID>(p, a, s);
+        default: return launch_g<VT, EP_AXPBY>(p, a, s);
     }
 }
 
@@ -323,7 +346,7 @@ SpmvArgs<VT> make_args(hhp_mat *A, const PlanDev &p, const VT *val, const VT *x,
     a.cta_part = p.cta_part;
     a.err = A->ctx->dev_err;
     a.cap = p.cap;
-    a.warp_smem = Geom<VT>{p.cap}.warp_bytes(p.ns);
+    a.warp_smem = Geom<VT>{p.cap}.warp_bytes(p.ns, p.gather);
     return a;
 }
 
@@ -339,25 +362,32 @@ template <typename VT>
 hhp_status build_plan_dev(hhp_mat *A, PlanDev &p, int cap_req) {
     const Tuning &t = tuning();
     hhp_ctx *ctx = A->ctx;
-    int ns = std::min(std::max(t.ns, 2), 4);
-    int cap = std::max(64, std::min(cap_req, 4096)) & ~31;
+    const int ns = std::min(std::max(t.ns, 1), 3);
+    const bool gather = t.gather != 0;
+    const int cap = std::max(64, std::min(cap_req, 4096)) & ~31;
+    const int cps = std::min(std::max(t.ctas_per_sm, 1), 8);
     int wpc = std::min(std::max(t.wpc, 1), 16);
-    const size_t budget = std::min<size_t>(ctx->smem_optin, 227 * 1024) - 1024;
-    while (wpc > 1 && static_cast<size_t>(wpc) * Geom<VT>{cap}.warp_bytes(ns) + 64 * 8 > budget) --wpc;
-    if (static_cast<size_t>(wpc) * Geom<VT>{cap}.warp_bytes(ns) + 64 * 8 > budget) {
+    const Geom<VT> geo{cap};
+    // shared memory of one SM is split between its CTAs
+    const size_t sm_budget = 228 * 1024 - 1024 * static_cast<size_t>(cps);
+    const size_t cta_budget = std::min<size_t>(std::min<size_t>(ctx->smem_optin, 227 * 1024), sm_budget / cps);
+    auto need = [&](int w) { return static_cast<size_t>(w) * geo.warp_bytes(ns, gather) + 64 * 8; };
+    while (wpc > 1 && need(wpc) > cta_budget) --wpc;
+    if (need(wpc) > cta_budget) {
         set_error("SpMV plan: stage buffers of cap=%d do not fit in shared memory", cap);
         return HHP_ERR_ARG;
     }
     PlanHost h;
-    const int ctas = ctx->num_sms;
+    const int ctas = ctx->num_sms * cps;
     build_plan(A->m, A->rowptr_host.data(), ctas * wpc, cap, std::min(t.med, cap), h);
     p.release();
     p.n_warps = ctas * wpc;
     p.cap = cap;
     p.ns = ns;
+    p.gather = gather;
     p.ctas = ctas;
     p.warps_per_cta = wpc;
-    p.smem_bytes = static_cast<size_t>(wpc) * Geom<VT>{cap}.warp_bytes(ns) + 64 * 8;
+    p.smem_bytes = need(wpc);
     p.n_items = static_cast<int>(h.items.size());
     p.n_long = static_cast<int>(h.long_rows.size());
     p.n_chunks = static_cast<int>(h.chunk_long.size());

@@ -78,6 +78,7 @@ const char *hhp_last_error(void);
 /* ---- context: replaces cudaSetDevice + cusparseCreate/cublasCreate of the entries
  *      (src/entry/bicgstab_gpu_dp.c:97-99) --------------------------------------------------- */
 hhp_status hhp_ctx_create(int device, hhp_ctx **out);
+/* Destroy every hhp_mat created on the context before destroying the context. */
 void hhp_ctx_destroy(hhp_ctx *ctx);
 /* The context's cudaStream_t, as an opaque pointer. */
 void *hhp_ctx_stream(hhp_ctx *ctx);
