@@ -139,8 +139,10 @@ __global__ void __launch_bounds__(512) k_init(DevScal *sc, const T *R, T *R0, T 
     }
     if (b0t0()) {
         if (!sc->restart) {
-            sc->rr0 = rr;
-            sc->thr2 = sc->fixed ? -1.0 : sc->rtol2 * rr;
+            // ||b - A x|| <= rtol ||b||: the reference's relative residual (bicgstab_cpu.c:251-255);
+            // gpu_BiCGStab's threshold rtol ||r0|| (bicgstab_gpu.c:149-150) is the same for x0 = 0.
+            sc->rr0 = bb;
+            sc->thr2 = sc->fixed ? -1.0 : sc->rtol2 * bb;
             sc->iter = 0;
             sc->bb = bb;
             sc->hist_scale = 1.0;
@@ -333,11 +335,11 @@ __global__ void __launch_bounds__(512) k_mix_prep(DevScal *sc, DevScal *sc32, co
     reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
     const double rd2 = v[0], bb = v[1];
     const bool first = sc->first_outer != 0;
-    const double rr0 = first ? rd2 : sc->rr0;
+    const double rr0 = first ? bb : sc->rr0;
     const double thr2 = sc->rtol2 * rr0;
     if (b0t0()) {
         if (first) {
-            sc->rr0 = rd2;
+            sc->rr0 = bb;
             sc->bb = bb;
             sc->thr2 = thr2;
             sc->iter = 0;

@@ -38,7 +38,7 @@ typedef enum {
     HHP_ERR_STATE = 9      /* call not valid in the object's current state                      */
 } hhp_status;
 
-/* Per-iteration residual callback: iter is 1-based, rel_res is the recursive ||r_k|| / ||r_0||.
+/* Per-iteration residual callback: iter is 1-based, rel_res is the recursive ||r_k|| / ||b||.
  * Called on the calling thread after the device loop, in iteration order (every `print_every`-th
  * iteration when print_every > 0). Replaces the "Iteration = %d; Error Norm = %e" lines of
  * gpu_BiCGStab (src/entry/bicgstab_gpu.c:156). */
@@ -47,8 +47,9 @@ typedef void (*hhp_iter_cb)(int iter, double rel_res, void *user);
 typedef enum { HHP_PREC_FP64 = 0, HHP_PREC_MIXED = 1 } hhp_precision;
 
 typedef struct {
-    double rtol;        /* stop when ||b - A x|| <= rtol * ||b - A x0||   (threshold = tol * ||r0||,
-                           gpu_BiCGStab src/entry/bicgstab_gpu.c:149-150)                      */
+    double rtol;        /* stop when ||b - A x|| <= rtol * ||b|| (the relative residual the reference
+                           prints, bicgstab_cpu.c:251-255; equal to gpu_BiCGStab's threshold
+                           tol * ||r0||, bicgstab_gpu.c:149-150, when x0 = 0)                   */
     int maxit;          /* iteration cap (maxIterations, bicgstab_gpu.c:120); >= 0                */
     int precision;      /* hhp_precision                                                          */
     double inner_rtol;  /* mixed form: relative tolerance of each FP32 inner solve (<= 0: 1e-5)   */
@@ -65,7 +66,7 @@ typedef struct {
     int outer_iters;           /* mixed: FP64 refinement steps; FP64: residual replacements + 1  */
     int half_step;             /* 1 if the last iteration stopped at the ||s|| test              */
     double rel_res_true;       /* ||b - A x|| / ||b||, recomputed in FP64 after the solve         */
-    double rel_res_recursive;  /* the solver's own ||r_k|| / ||r_0||                              */
+    double rel_res_recursive;  /* the solver's own ||r_k|| / ||b||                                */
     double err_vs_target;      /* max_i |x_i - x_target_i| (NaN when no target was given)        */
     double t_solve_s;          /* device time of the solve (CUDA events on the context stream)   */
     hhp_status status;

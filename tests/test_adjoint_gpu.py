@@ -36,10 +36,12 @@ def test_dense_gradient_32x32(ctx):
 
 
 def test_finite_differences(ctx):
-    """Central differences (h = 1e-6) of L on 8 entries of b and 8 stored entries of A. Both
-    perturbed solves run the same fixed number of iterations (the unperturbed solve's count to
-    1e-13), so they follow the same Krylov path and the solver error cancels in the difference;
-    the difference of L is formed as 1/2 (x+ - x-).(x+ + x- - 2 x_t) to avoid cancellation."""
+    """Central differences of L on 8 entries of b and 8 stored entries of A, every solve at
+    rtol 1e-13. L is exactly quadratic in b, so for b the step can be large (h = 1e-2) and the
+    difference is exact up to the solver error / h. For A the truncation error is removed by
+    Richardson extrapolation of the h and h/2 central differences (h = 1e-4, O(h^4) remainder).
+    The difference of L is formed as 1/2 (x+ - x-).(x+ + x- - 2 x_t) to avoid cancellation.
+    (With h = 1e-6 the check would measure the solver: its error rtol*cond(A)*|x| over h.)"""
     s = synth.convdiff2d(64, 30.0, (1.0, 0.5), seed=4, target="normal")
     rng = np.random.default_rng(6)
     b = rng.standard_normal(s.m)
@@ -47,29 +49,33 @@ def test_finite_differences(ctx):
     A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
     x, r0 = bicgstab(ctx, A, b, None, rtol=1e-13, maxit=20000)
     assert r0.status == 0
-    k = r0.iters + 2
     dldb, dlda, _ = bicgstab_backward(ctx, A, x, x - xt, rtol=1e-13, maxit=20000)
 
     def solve(bv, vals):
         A.set_values(vals)
-        xx, _ = bicgstab(ctx, A, bv, None, rtol=0.0, maxit=k, fixed_iters=True)
+        xx, rr = bicgstab(ctx, A, bv, None, rtol=1e-13, maxit=20000)
+        assert rr.status == 0
         return xx
 
-    def fd(xp, xm, h):
+    def cd(xp, xm, h):
         return 0.5 * np.dot(xp - xm, xp + xm - 2.0 * xt) / (2.0 * h)
 
-    h = 1e-6
+    hb = 1e-2
     for i in rng.choice(s.m, 8, replace=False):
         bp, bm = b.copy(), b.copy()
-        bp[i] += h
-        bm[i] -= h
-        g = fd(solve(bp, s.val), solve(bm, s.val), h)
+        bp[i] += hb
+        bm[i] -= hb
+        g = cd(solve(bp, s.val), solve(bm, s.val), hb)
         assert abs(g - dldb[i]) <= 1e-6 * max(abs(dldb[i]), 1e-2 * np.max(np.abs(dldb))), (i, g, dldb[i])
+    ha = 1e-4
     for kk in rng.choice(s.nnz, 8, replace=False):
-        vp, vm = s.val.copy(), s.val.copy()
-        vp[kk] += h
-        vm[kk] -= h
-        g = fd(solve(b, vp), solve(b, vm), h)
+        est = []
+        for h in (ha, ha / 2):
+            vp, vm = s.val.copy(), s.val.copy()
+            vp[kk] += h
+            vm[kk] -= h
+            est.append(cd(solve(b, vp), solve(b, vm), h))
+        g = (4.0 * est[1] - est[0]) / 3.0
         assert abs(g - dlda[kk]) <= 1e-6 * max(abs(dlda[kk]), 1e-2 * np.max(np.abs(dlda))), (kk, g, dlda[kk])
     A.set_values(s.val)
 
