@@ -279,14 +279,15 @@ def vector_write(path: str, v, exact: bool = False):
     check(lib().hhp_vector_write(path.encode(), int(vv.size), _ptr(vv), 1 if exact else 0), "hhp_vector_write")
 
 
-def plan_stats(rowptr, n_warps: int, cap: int) -> dict:
+def plan_stats(rowptr, rows_per_lane: int = 2, cap: int = 2048) -> dict:
     rp = _host(rowptr, np.int32)
-    ni, nl, nc, mx = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-    imb = ctypes.c_double()
-    check(lib().hhp_plan_stats(rp.size - 1, int(rp[-1]), _ptr(rp), n_warps, cap, ctypes.byref(ni), ctypes.byref(nl),
-                               ctypes.byref(nc), ctypes.byref(mx), ctypes.byref(imb)), "hhp_plan_stats")
-    return {"items": ni.value, "long_rows": nl.value, "chunks": nc.value, "max_item_nnz": mx.value,
-            "imbalance": imb.value}
+    ns, nl, nc, so = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    pad = ctypes.c_double()
+    check(lib().hhp_plan_stats(rp.size - 1, int(rp[-1]), _ptr(rp), rows_per_lane, cap, ctypes.byref(ns),
+                               ctypes.byref(nl), ctypes.byref(nc), ctypes.byref(so), ctypes.byref(pad)),
+          "hhp_plan_stats")
+    return {"slices": ns.value, "long_rows": nl.value, "chunks": nc.value, "sorted": bool(so.value),
+            "padding": pad.value}
 
 
 def mtx_read(path: str):
@@ -307,17 +308,19 @@ def mtx_read(path: str):
     return rowptr, col, val, (m.value, n.value)
 
 
-def plan_dump(rowptr, n_warps: int, cap: int):
-    """The SpMV work plan: (items [n_items x 4] int32, warp_begin [n_warps+1])."""
+def plan_dump(rowptr, rows_per_lane: int = 2, cap: int = 2048):
+    """The SpMV work plan: (slice_rows [n_slices*32*rows_per_lane], chunks [n_chunks x 4])."""
     rp = _host(rowptr, np.int32)
-    ni = ctypes.c_int()
-    st = lib().hhp_plan_dump(rp.size - 1, int(rp[-1]), _ptr(rp), n_warps, cap, 0, None, None, ctypes.byref(ni))
-    items = np.empty((max(ni.value, 1), 4), np.int32)
-    wb = np.empty(n_warps + 1, np.int32)
-    check(lib().hhp_plan_dump(rp.size - 1, int(rp[-1]), _ptr(rp), n_warps, cap, ni.value, _ptr(items), _ptr(wb),
-                              ctypes.byref(ni)), "hhp_plan_dump")
-    del st
-    return items[:ni.value], wb
+    ns, nc = ctypes.c_int(), ctypes.c_int()
+    lib().hhp_plan_dump(rp.size - 1, int(rp[-1]), _ptr(rp), rows_per_lane, cap, 0, None, None, ctypes.byref(ns),
+                        ctypes.byref(nc))
+    H = 32 * rows_per_lane
+    cap_ints = ns.value * H + 4 * nc.value
+    rows = np.empty(max(ns.value * H, 1), np.int32)
+    chunks = np.empty((max(nc.value, 1), 4), np.int32)
+    check(lib().hhp_plan_dump(rp.size - 1, int(rp[-1]), _ptr(rp), rows_per_lane, cap, cap_ints, _ptr(rows),
+                              _ptr(chunks), ctypes.byref(ns), ctypes.byref(nc)), "hhp_plan_dump")
+    return rows[:ns.value * H], chunks[:nc.value]
 
 
 def spmv_bytes(m: int, n: int, nnz: int, fp32: bool = False) -> int:

@@ -41,13 +41,11 @@ int env_int(const char *name, int dflt) {
 const Tuning &tuning() {
     static const Tuning t = [] {
         Tuning d;
-        d.cap64 = env_int("HHP_SPMV_CAP64", d.cap64);
-        d.cap32 = env_int("HHP_SPMV_CAP32", d.cap32);
-        d.med = env_int("HHP_SPMV_MED", d.med);
+        d.cap = env_int("HHP_SPMV_CHUNK", d.cap);
+        d.long_thr = env_int("HHP_SPMV_LONG", d.long_thr);
+        d.window = env_int("HHP_SPMV_WINDOW", d.window);
         d.wpc = env_int("HHP_SPMV_WPC", d.wpc);
-        d.ns = env_int("HHP_SPMV_NS", d.ns);
         d.ctas_per_sm = env_int("HHP_SPMV_CPS", d.ctas_per_sm);
-        d.gather = env_int("HHP_SPMV_GATHER", d.gather);
         d.vec_blocks_per_sm = env_int("HHP_VEC_BLOCKS_PER_SM", d.vec_blocks_per_sm);
         d.unroll_iters = env_int("HHP_UNROLL_ITERS", d.unroll_iters);
         return d;
@@ -120,6 +118,7 @@ hhp_status mat_refresh_derived(hhp_mat *A) {
         k_to_f32<<<grid, 256, 0, A->ctx->stream>>>(A->val, A->val32, A->nnz);
         HHP_CUDA(cudaGetLastError());
     }
+    HHP_TRY(refresh_plan_values(A));
     if (A->t) HHP_TRY(refresh_transpose_values(A));
     return HHP_OK;
 }
@@ -343,7 +342,7 @@ static hhp_status set_values(hhp_mat *A, const double *v, cudaMemcpyKind kind) {
     }
     if (A->nnz > 0)
         HHP_CUDA(cudaMemcpyAsync(A->val, v, sizeof(double) * static_cast<size_t>(A->nnz), kind, A->ctx->stream));
-    if (A->val32 || A->t) HHP_TRY(mat_refresh_derived(A));
+    if (A->val32 || A->t || A->plan64.built() || A->plan32.built()) HHP_TRY(mat_refresh_derived(A));
     HHP_CUDA(cudaStreamSynchronize(A->ctx->stream));
     return HHP_OK;
 }

@@ -28,47 +28,42 @@ hhp_status cuda_fail(cudaError_t e, const char *what, const char *file, int line
     } while (0)
 
 // ---- SpMV work plan ----------------------------------------------------------------------------
-// One work item = 16 bytes:
-//   x   first row
-//   y   kind (bits 30-31) | payload (bits 0-29):
-//         KIND_ROWS : payload = number of rows (1..32), one row per lane, each row summed
-//                     sequentially (fused multiply-add in CSR order)
-//         KIND_VEC  : payload = 1; one row with MED < len <= cap, summed by the whole warp
-//         KIND_CHUNK: payload = chunk id; a slice of a long row (len > cap), summed by the warp,
-//                     slices combined in slice order by the last warp to finish one
-//   z,w nnz range [k0, k1)
-// Items are in row order and split into contiguous per-warp ranges of near-equal work.
-enum : int { KIND_ROWS = 0, KIND_VEC = 1, KIND_CHUNK = 2 };
-constexpr int KIND_SHIFT = 30;
-constexpr int PAYLOAD_MASK = (1 << 30) - 1;
-
-struct PlanHost {
-    int n_warps = 0, cap = 0, med = 0;
-    std::vector<int4> items;
-    std::vector<int> warp_begin;      // n_warps + 1
-    std::vector<int> long_rows;       // row of each long row
-    std::vector<int> long_first;      // first chunk id per long row, n_long + 1
-    std::vector<int> chunk_long;      // long-row index of each chunk
-    long long max_item_nnz = 0;
-    double imbalance = 1.0;           // max warp work / mean warp work
+// Sliced, row-interleaved layout (see hhp_plan.cpp). Positions p = s*H + q (slice s, row q of the
+// slice) map to original rows pos_row[p] (-1 for padding). The j-th nonzero of position p is at
+// slice_ptr[s] + j*H + q in the slice arrays. Rows longer than long_thr are cut into chunks
+// {row, chunk id, k0, k1} read straight from the CSR arrays.
+struct SellHost {
+    int rpl = 2, H = 64, long_thr = 0, cap = 0, n_slices = 0;
+    bool sorted = false, has_perm = false;
+    std::vector<int> pos_row, pos_len;   // n_slices * H
+    std::vector<long long> slice_ptr;    // n_slices + 1
+    long long total = 0, short_nnz = 0;  // slice storage (with padding), nonzeros in slices
+    double padding = 1.0;                // total / short_nnz
+    std::vector<int4> chunks;            // long-row chunks
+    std::vector<int> long_rows, long_first, chunk_long;
 };
 
-// Builds the plan from a host rowptr. med: longest row summed one-row-per-lane; cap: most
-// nonzeros one item holds (a stage buffer's capacity).
-void build_plan(int m, const int *rowptr, int n_warps, int cap, int med, PlanHost &out);
+// Builds the plan from a host rowptr: rpl rows per lane (H = 32*rpl rows per slice), rows longer
+// than long_thr go to chunks of at most cap nonzeros, `window` rows per length-sort window.
+void build_plan(int m, const int *rowptr, int rpl, int long_thr, int cap, int window, SellHost &out);
 
 struct PlanDev {
-    int n_warps = 0, cap = 0, n_items = 0, n_long = 0, n_chunks = 0;
-    int ctas = 0, warps_per_cta = 0, ns = 0;
-    bool gather = false;
-    size_t smem_bytes = 0;
-    int4 *items = nullptr;
-    int *warp_begin = nullptr;
-    int *long_rows = nullptr, *long_first = nullptr, *chunk_long = nullptr;
+    int rpl = 0, H = 0, n_slices = 0, n_long = 0, n_chunks = 0, ctas = 0, warps_per_cta = 0;
+    bool has_perm = false, sorted = false;
+    long long total = 0;
+    double padding = 1.0;
+    long long *slice_ptr = nullptr;   // n_slices + 1
+    int *pos_row = nullptr;           // n_slices * H (original row, -1 = padding)
+    int *pos_len = nullptr;           // n_slices * H
+    void *sval = nullptr;             // total values (double or float), padding zero
+    int *scol = nullptr;              // total column indices
+    int4 *chunks = nullptr;
+    int *long_first = nullptr, *chunk_long = nullptr;
     double *chunk_part = nullptr;     // n_chunks
     unsigned *long_cnt = nullptr;     // n_long (kept at zero between launches)
     double *long_dot = nullptr;       // n_long * 2 epilogue contributions of long rows
     double *cta_part = nullptr;       // ctas * 2 epilogue partials
+    bool built() const { return slice_ptr != nullptr; }
     void release();
 };
 
@@ -116,6 +111,8 @@ enum EpKind : int {
 };
 
 hhp_status ensure_plan(hhp_mat *A, bool fp32);
+// Rewrites the slice values of existing plans from the CSR values (after a value change).
+hhp_status refresh_plan_values(hhp_mat *A);
 // Launches the FP64 SpMV with an epilogue on `stream` (x, y, w1 length-padded device vectors).
 hhp_status launch_spmv64(hhp_mat *A, cudaStream_t stream, EpKind ep, const double *x, double *y, const double *w1,
                          double alpha, double beta);
@@ -152,7 +149,7 @@ inline int pad4(int n) { return (n + 3) & ~3; }
 
 // Kernel tuning knobs (environment overrides read once).
 struct Tuning {
-    int cap64 = 512, cap32 = 1024, med = 64, wpc = 12, ns = 2, ctas_per_sm = 1, gather = 1, vec_blocks_per_sm = 2,
+    int cap = 2048, long_thr = 256, window = 8192, wpc = 16, ctas_per_sm = 2, vec_blocks_per_sm = 2,
         unroll_iters = 4;
 };
 const Tuning &tuning();

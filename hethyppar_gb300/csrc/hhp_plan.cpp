@@ -1,108 +1,113 @@
-// hhp_plan.cpp -- host-side construction of the SpMV work plan (row-length binning + balanced
-// contiguous per-warp ranges).
+// hhp_plan.cpp -- host-side construction of the SpMV work plan: row-length binning into a sliced,
+// row-interleaved device layout plus equal-nnz chunks for long rows.
 //
 // Rows are binned by length:
-//   len <= med          -> grouped, in row order, into ROWS items of up to 32 rows and at most
-//                          `cap` nonzeros; each lane sums one row sequentially (vector-per-row
-//                          degenerates to thread-per-row: no intra-row reduction, so the sum
-//                          order equals the CSR order of the reference's CSR_spmxv_seq,
-//                          src/util/hhp_cpu.c:445-455, with each step fused)
-//   med < len <= cap    -> one VEC item: the row is summed by a whole warp
-//   len > cap           -> CHUNK items of `cap` nonzeros (merge-path-style equal-nnz slices),
-//                          combined in slice order
-// The item list (in row order) is then cut into n_warps contiguous ranges of near-equal work,
-// like a merge-path split of the (rows + nonzeros) list: warp g takes the items whose work
-// midpoint falls in [g*W/G, (g+1)*W/G).
+//   len <= long_thr  -> "slice rows": placed in slices of H = 32*RPL rows (RPL rows per lane).
+//                       Inside a slice the j-th nonzero of all H rows are stored next to each
+//                       other (step-major), so at every step a warp loads its lanes' values and
+//                       column indices with one coalesced 128-bit load per lane; each lane sums
+//                       its rows sequentially in CSR order (the order of CSR_spmxv_seq,
+//                       src/util/hhp_cpu.c:445-455), one fused multiply-add per nonzero.
+//                       Rows keep their natural order unless that would pad the slices by more
+//                       than 15%; then rows are sorted by length (descending, stable) inside
+//                       windows of `window` rows, so slice-mates have similar lengths.
+//   len >  long_thr  -> CHUNK items of at most `cap` nonzeros (equal-nnz slices of the row, as a
+//                       merge-path split would cut it), each summed by one warp, the chunk sums
+//                       combined in chunk order by whichever warp finishes the row's last chunk.
 #include <algorithm>
 #include <cmath>
+#include <numeric>
 
 #include "hhp_internal.h"
 
 namespace hhp {
 
-void build_plan(int m, const int *rowptr, int n_warps, int cap, int med, PlanHost &P) {
-    P = PlanHost();
-    P.n_warps = n_warps;
+void build_plan(int m, const int *rowptr, int rpl, int long_thr, int cap, int window, SellHost &P) {
+    P = SellHost();
+    P.rpl = rpl;
+    P.H = 32 * rpl;
+    P.long_thr = long_thr;
     P.cap = cap;
-    P.med = med;
-    std::vector<long long> work;
-    P.items.reserve(static_cast<size_t>(m) / 16 + 16);
-    work.reserve(static_cast<size_t>(m) / 16 + 16);
-
-    int t_r0 = -1, t_rows = 0, t_k0 = 0, t_k1 = 0;
-    auto close_tile = [&]() {
-        if (t_rows > 0) {
-            P.items.push_back(make_int4(t_r0, (KIND_ROWS << KIND_SHIFT) | t_rows, t_k0, t_k1));
-            work.push_back(static_cast<long long>(t_k1 - t_k0) + 2LL * t_rows + 16);
-            P.max_item_nnz = std::max<long long>(P.max_item_nnz, t_k1 - t_k0);
-        }
-        t_rows = 0;
-    };
+    const int H = P.H;
+    std::vector<int> order;
+    order.reserve(static_cast<size_t>(m));
+    long long short_nnz = 0;
     int n_chunks = 0;
     for (int r = 0; r < m; ++r) {
-        const int k0 = rowptr[r], k1 = rowptr[r + 1], len = k1 - k0;
-        if (len > cap) {
-            close_tile();
+        const int len = rowptr[r + 1] - rowptr[r];
+        if (len > long_thr) {
             const int l = static_cast<int>(P.long_rows.size());
             P.long_rows.push_back(r);
             P.long_first.push_back(n_chunks);
-            for (int a = k0; a < k1; a += cap) {
-                const int b = std::min(a + cap, k1);
-                P.items.push_back(make_int4(r, (KIND_CHUNK << KIND_SHIFT) | n_chunks, a, b));
-                work.push_back(static_cast<long long>(b - a) + 18);
+            for (int a = rowptr[r]; a < rowptr[r + 1]; a += cap) {
+                const int b = std::min(a + cap, rowptr[r + 1]);
+                P.chunks.push_back(make_int4(r, n_chunks, a, b));
                 P.chunk_long.push_back(l);
-                P.max_item_nnz = std::max<long long>(P.max_item_nnz, b - a);
                 ++n_chunks;
             }
-        } else if (len > med) {
-            close_tile();
-            P.items.push_back(make_int4(r, (KIND_VEC << KIND_SHIFT) | 1, k0, k1));
-            work.push_back(static_cast<long long>(len) + 18);
-            P.max_item_nnz = std::max<long long>(P.max_item_nnz, len);
         } else {
-            if (t_rows == 32 || (t_rows > 0 && (t_k1 - t_k0) + len > cap)) close_tile();
-            if (t_rows == 0) {
-                t_r0 = r;
-                t_k0 = k0;
-            }
-            t_k1 = k1;
-            ++t_rows;
+            order.push_back(r);
+            short_nnz += len;
         }
     }
-    close_tile();
     P.long_first.push_back(n_chunks);
-
-    // Balanced contiguous split.
-    const size_t ni = P.items.size();
-    long long total = 0;
-    for (long long w : work) total += w;
-    P.warp_begin.assign(static_cast<size_t>(n_warps) + 1, static_cast<int>(ni));  // trailing warps: empty
-    std::vector<long long> per_warp(static_cast<size_t>(n_warps), 0);
-    if (ni > 0 && total > 0) {
-        long long prefix = 0;
-        int cur = -1;
-        for (size_t i = 0; i < ni; ++i) {
-            const long double mid = static_cast<long double>(prefix) + 0.5L * static_cast<long double>(work[i]);
-            int g = static_cast<int>(mid * n_warps / static_cast<long double>(total));
-            g = std::min(std::max(g, 0), n_warps - 1);
-            if (g < cur) g = cur;
-            while (cur < g) P.warp_begin[static_cast<size_t>(++cur)] = static_cast<int>(i);
-            per_warp[static_cast<size_t>(g)] += work[i];
-            prefix += work[i];
+    auto padded = [&](const std::vector<int> &ord) {
+        long long tot = 0;
+        for (size_t s0 = 0; s0 < ord.size(); s0 += static_cast<size_t>(H)) {
+            int mx = 0;
+            for (size_t q = s0; q < std::min(ord.size(), s0 + static_cast<size_t>(H)); ++q)
+                mx = std::max(mx, rowptr[ord[q] + 1] - rowptr[ord[q]]);
+            tot += static_cast<long long>(mx) * H;
         }
-        P.warp_begin[0] = 0;
-        long long mx = *std::max_element(per_warp.begin(), per_warp.end());
-        P.imbalance = static_cast<double>(mx) / (static_cast<double>(total) / n_warps);
-    } else {
-        std::fill(P.warp_begin.begin(), P.warp_begin.end(), 0);  // no items (m == 0)
+        return tot;
+    };
+    long long tot = padded(order);
+    P.sorted = false;
+    if (short_nnz > 0 && static_cast<double>(tot) > 1.15 * static_cast<double>(short_nnz)) {
+        for (size_t w0 = 0; w0 < order.size(); w0 += static_cast<size_t>(window)) {
+            const auto b = order.begin() + static_cast<long>(w0);
+            const auto e = order.begin() + static_cast<long>(std::min(order.size(), w0 + static_cast<size_t>(window)));
+            std::stable_sort(b, e, [&](int x, int y) {
+                return (rowptr[x + 1] - rowptr[x]) > (rowptr[y + 1] - rowptr[y]);
+            });
+        }
+        tot = padded(order);
+        P.sorted = true;
     }
+    P.has_perm = P.sorted || !P.long_rows.empty();
+    const size_t ms = order.size();
+    P.n_slices = static_cast<int>((ms + static_cast<size_t>(H) - 1) / static_cast<size_t>(H));
+    const size_t npos = static_cast<size_t>(P.n_slices) * static_cast<size_t>(H);
+    P.pos_row.assign(npos, -1);
+    P.pos_len.assign(npos, 0);
+    P.slice_ptr.assign(static_cast<size_t>(P.n_slices) + 1, 0);
+    long long off = 0;
+    for (int s = 0; s < P.n_slices; ++s) {
+        int mx = 0;
+        for (int q = 0; q < H; ++q) {
+            const size_t p = static_cast<size_t>(s) * H + static_cast<size_t>(q);
+            if (p < ms) {
+                const int r = order[p];
+                P.pos_row[p] = r;
+                P.pos_len[p] = rowptr[r + 1] - rowptr[r];
+                mx = std::max(mx, P.pos_len[p]);
+            }
+        }
+        P.slice_ptr[static_cast<size_t>(s)] = off;
+        off += static_cast<long long>(mx) * H;
+    }
+    P.slice_ptr[static_cast<size_t>(P.n_slices)] = off;
+    P.total = off;
+    P.short_nnz = short_nnz;
+    P.padding = short_nnz > 0 ? static_cast<double>(off) / static_cast<double>(short_nnz) : 1.0;
 }
 
 }  // namespace hhp
 
-extern "C" hhp_status hhp_plan_stats(int m, int nnz, const int *rowptr, int n_warps, int cap, int *n_items,
-                                     int *n_long_rows, int *n_chunks, int *max_item_nnz, double *imbalance) {
-    if (m < 0 || nnz < 0 || !rowptr || n_warps <= 0 || cap < 32) {
+extern "C" hhp_status hhp_plan_stats(int m, int nnz, const int *rowptr, int rows_per_lane, int cap, int *n_slices,
+                                     int *n_long_rows, int *n_chunks, int *sorted, double *padding) {
+    if (m < 0 || nnz < 0 || !rowptr || (rows_per_lane != 1 && rows_per_lane != 2 && rows_per_lane != 4) ||
+        cap < 32) {
         hhp::set_error("hhp_plan_stats: invalid arguments");
         return HHP_ERR_ARG;
     }
@@ -110,19 +115,21 @@ extern "C" hhp_status hhp_plan_stats(int m, int nnz, const int *rowptr, int n_wa
         hhp::set_error("hhp_plan_stats: rowptr[0] must be 0 and rowptr[m] must equal nnz");
         return HHP_ERR_ARG;
     }
-    hhp::PlanHost P;
-    hhp::build_plan(m, rowptr, n_warps, cap, std::min(hhp::tuning().med, cap), P);
-    if (n_items) *n_items = static_cast<int>(P.items.size());
+    hhp::SellHost P;
+    const hhp::Tuning &t = hhp::tuning();
+    hhp::build_plan(m, rowptr, rows_per_lane, t.long_thr, cap, t.window, P);
+    if (n_slices) *n_slices = P.n_slices;
     if (n_long_rows) *n_long_rows = static_cast<int>(P.long_rows.size());
-    if (n_chunks) *n_chunks = static_cast<int>(P.chunk_long.size());
-    if (max_item_nnz) *max_item_nnz = static_cast<int>(P.max_item_nnz);
-    if (imbalance) *imbalance = P.imbalance;
+    if (n_chunks) *n_chunks = static_cast<int>(P.chunks.size());
+    if (sorted) *sorted = P.sorted ? 1 : 0;
+    if (padding) *padding = P.padding;
     return HHP_OK;
 }
 
-extern "C" hhp_status hhp_plan_dump(int m, int nnz, const int *rowptr, int n_warps, int cap, int capacity,
-                                    int *items_out, int *warp_begin_out, int *n_items) {
-    if (m < 0 || nnz < 0 || !rowptr || n_warps <= 0 || cap < 32 || !n_items) {
+extern "C" hhp_status hhp_plan_dump(int m, int nnz, const int *rowptr, int rows_per_lane, int cap, int capacity,
+                                    int *slice_rows, int *chunks, int *n_slices, int *n_chunks) {
+    if (m < 0 || nnz < 0 || !rowptr || (rows_per_lane != 1 && rows_per_lane != 2 && rows_per_lane != 4) ||
+        cap < 32 || !n_slices || !n_chunks) {
         hhp::set_error("hhp_plan_dump: invalid arguments");
         return HHP_ERR_ARG;
     }
@@ -130,19 +137,22 @@ extern "C" hhp_status hhp_plan_dump(int m, int nnz, const int *rowptr, int n_war
         hhp::set_error("hhp_plan_dump: rowptr[0] must be 0 and rowptr[m] must equal nnz");
         return HHP_ERR_ARG;
     }
-    hhp::PlanHost P;
-    hhp::build_plan(m, rowptr, n_warps, cap, std::min(hhp::tuning().med, cap), P);
-    *n_items = static_cast<int>(P.items.size());
-    if (capacity < *n_items || !items_out || !warp_begin_out) {
-        hhp::set_error("hhp_plan_dump: capacity %d < %d items", capacity, *n_items);
+    hhp::SellHost P;
+    const hhp::Tuning &t = hhp::tuning();
+    hhp::build_plan(m, rowptr, rows_per_lane, t.long_thr, cap, t.window, P);
+    *n_slices = P.n_slices;
+    *n_chunks = static_cast<int>(P.chunks.size());
+    const long long need = static_cast<long long>(P.pos_row.size()) + 4LL * static_cast<long long>(P.chunks.size());
+    if (capacity < need || !slice_rows || !chunks) {
+        hhp::set_error("hhp_plan_dump: capacity %d < %lld", capacity, need);
         return HHP_ERR_ARG;
     }
-    for (size_t i = 0; i < P.items.size(); ++i) {
-        items_out[4 * i] = P.items[i].x;
-        items_out[4 * i + 1] = P.items[i].y;
-        items_out[4 * i + 2] = P.items[i].z;
-        items_out[4 * i + 3] = P.items[i].w;
+    std::copy(P.pos_row.begin(), P.pos_row.end(), slice_rows);
+    for (size_t c = 0; c < P.chunks.size(); ++c) {
+        chunks[4 * c] = P.chunks[c].x;
+        chunks[4 * c + 1] = P.chunks[c].y;
+        chunks[4 * c + 2] = P.chunks[c].z;
+        chunks[4 * c + 3] = P.chunks[c].w;
     }
-    for (size_t g = 0; g < P.warp_begin.size(); ++g) warp_begin_out[g] = P.warp_begin[g];
     return HHP_OK;
 }

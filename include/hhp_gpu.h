@@ -153,14 +153,18 @@ hhp_status hhp_mtx_read(const char *path, int *m, int *n, int *nnz, int **rowptr
 void hhp_free(void *p);
 
 /* ---- host-side helpers exposed for testing the work plan without a GPU ---------------------- */
-/* The SpMV work plan for a host CSR: number of warp work lists, items and long-row chunks. */
-hhp_status hhp_plan_stats(int m, int nnz, const int *rowptr, int n_warps, int cap, int *n_items, int *n_long_rows,
-                          int *n_chunks, int *max_item_nnz, double *imbalance);
-/* The plan itself: items_out receives 4 ints per item (first row, kind<<30 | payload, k0, k1)
- * for up to `capacity` items; warp_begin_out (n_warps+1 ints) the per-warp item ranges.
- * *n_items is always set; HHP_ERR_ARG if capacity is too small. */
-hhp_status hhp_plan_dump(int m, int nnz, const int *rowptr, int n_warps, int cap, int capacity, int *items_out,
-                         int *warp_begin_out, int *n_items);
+/* The SpMV work plan of a host CSR (rows_per_lane 2 = the FP64 kernel's slices of 64 rows, 4 =
+ * the FP32 kernel's slices of 128 rows): number of slices, of long rows (cut into chunks of at
+ * most `cap` nonzeros) and chunks, whether rows were length-sorted inside windows, and the
+ * storage padding ratio of the slices. */
+hhp_status hhp_plan_stats(int m, int nnz, const int *rowptr, int rows_per_lane, int cap, int *n_slices,
+                          int *n_long_rows, int *n_chunks, int *sorted, double *padding);
+/* The plan itself: slice_rows receives, for every slice position (n_slices * 32 * rows_per_lane
+ * ints), the row placed there (-1 = padding); chunks receives 4 ints per chunk (row, chunk id,
+ * first nonzero, end). capacity counts both arrays' ints. *n_slices and *n_chunks are always set;
+ * HHP_ERR_ARG if capacity is too small. */
+hhp_status hhp_plan_dump(int m, int nnz, const int *rowptr, int rows_per_lane, int cap, int capacity,
+                         int *slice_rows, int *chunks, int *n_slices, int *n_chunks);
 
 /* ---- drop-ins for the reference's device-pointer launchers (src/include/hhp_dp_kernels.h:37-59).
  *      Same names, arguments and meaning; `s` is a cudaStream_t. Unlike the reference's

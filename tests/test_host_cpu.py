@@ -110,36 +110,27 @@ def test_vector_files_roundtrip_and_short_file():
         assert hhp.vector_read(p, 3).tolist() == [1.0, 2.0, -3.5]
 
 
-def _check_plan(rp, n_warps, cap):
-    items, wb = hhp.plan_dump(rp, n_warps, cap)
+def _check_plan(rp, rpl, cap):
+    rows, chunks = hhp.plan_dump(rp, rpl, cap)
     m = rp.size - 1
-    kind = (items[:, 1].astype(np.int64) >> 30) & 3
-    payload = items[:, 1] & ((1 << 30) - 1)
+    H = 32 * rpl
+    assert rows.size % H == 0
+    lens = np.diff(rp)
     covered = np.zeros(m, np.int64)
-    next_row = 0
-    chunk_ids = []
-    for (r0, _, k0, k1), kd, pl in zip(items, kind, payload):
-        if kd == 0:  # ROWS
-            assert 1 <= pl <= 32
-            assert r0 >= next_row
-            covered[r0:r0 + pl] += 1
-            assert k0 == rp[r0] and k1 == rp[r0 + pl]
-            assert k1 - k0 <= cap
-            next_row = r0 + pl
-        elif kd == 1:  # VEC
-            assert pl == 1 and k0 == rp[r0] and k1 == rp[r0 + 1] and k1 - k0 <= cap
-            covered[r0] += 1
-            next_row = r0 + 1
-        else:  # CHUNK
-            assert 0 < k1 - k0 <= cap and rp[r0] <= k0 < k1 <= rp[r0 + 1]
-            if k0 == rp[r0]:
-                covered[r0] += 1
-            chunk_ids.append(pl)
-            next_row = r0 + (1 if k1 == rp[r0 + 1] else 0)
+    placed = rows[rows >= 0]
+    np.add.at(covered, placed, 1)
+    assert np.all(lens[placed] <= hhp.plan_stats(rp, rpl, cap)["padding"] * 0 + lens.max())
+    # long rows: chunks cover [rp[r], rp[r+1]) contiguously, in order, each at most cap entries
+    long_rows = sorted(set(chunks[:, 0].tolist())) if chunks.size else []
+    for r in long_rows:
+        ch = chunks[chunks[:, 0] == r]
+        assert ch[0, 2] == rp[r] and ch[-1, 3] == rp[r + 1]
+        assert np.all(ch[1:, 2] == ch[:-1, 3]) and np.all(ch[:, 3] - ch[:, 2] <= cap) and np.all(ch[:, 3] > ch[:, 2])
+        covered[r] += 1
     assert np.all(covered == 1), np.nonzero(covered != 1)[0][:10]
-    assert chunk_ids == list(range(len(chunk_ids)))
-    assert wb[0] == 0 and wb[-1] == len(items) and np.all(np.diff(wb) >= 0)
-    return items, wb
+    if chunks.size:
+        assert chunks[:, 1].tolist() == list(range(len(chunks)))
+    return rows, chunks
 
 
 @pytest.mark.parametrize("case", ["banded", "convdiff", "powerlaw", "empty_rows", "one_long", "tiny"])
@@ -159,20 +150,22 @@ def test_work_plan_covers_every_row_once(case):
         rp = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
     else:
         rp = np.array([0, 1], np.int32)
-    for n_warps, cap in ((1824, 512), (7, 64), (1, 1024)):
-        _check_plan(rp, n_warps, cap)
+    for rpl, cap in ((2, 2048), (4, 2048), (2, 64)):
+        _check_plan(rp, rpl, cap)
 
 
-def test_work_plan_balance():
+def test_work_plan_layout_choices():
     rp = synth.banded_random(100000, seed=5).rowptr
-    st = hhp.plan_stats(rp, 1824, 512)
-    assert st["long_rows"] == 0 and st["chunks"] == 0
-    assert st["max_item_nnz"] <= 512
-    assert st["imbalance"] < 1.35
+    st = hhp.plan_stats(rp, 2, 2048)
+    assert st["long_rows"] == 0 and st["chunks"] == 0 and not st["sorted"] and st["padding"] == 1.0
+    rows, _ = hhp.plan_dump(rp, 2, 2048)
+    assert np.array_equal(rows[:rp.size - 1], np.arange(rp.size - 1))  # natural order kept
+    rp = synth.convdiff3d(40, 20.0).rowptr
+    st = hhp.plan_stats(rp, 2, 2048)
+    assert not st["sorted"] and st["padding"] < 1.15
     rp = synth.powerlaw(200000, seed=6).rowptr
-    st = hhp.plan_stats(rp, 1824, 512)
-    assert st["long_rows"] > 0 and st["chunks"] >= st["long_rows"]
-    assert st["imbalance"] < 1.5
+    st = hhp.plan_stats(rp, 2, 2048)
+    assert st["long_rows"] > 0 and st["chunks"] >= st["long_rows"] and st["sorted"] and st["padding"] < 1.5
 
 
 def test_cli_rejects_missing_arguments():
