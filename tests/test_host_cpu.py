@@ -157,7 +157,7 @@ def test_work_plan_covers_every_row_once(case):
 def test_work_plan_layout_choices():
     rp = synth.banded_random(100000, seed=5).rowptr
     st = hhp.plan_stats(rp, 2, 2048)
-    assert st["long_rows"] == 0 and st["chunks"] == 0 and not st["sorted"] and st["padding"] == 1.0
+    assert st["long_rows"] == 0 and st["chunks"] == 0 and not st["sorted"] and st["padding"] < 1.001
     rows, _ = hhp.plan_dump(rp, 2, 2048)
     assert np.array_equal(rows[:rp.size - 1], np.arange(rp.size - 1))  # natural order kept
     rp = synth.convdiff3d(40, 20.0).rowptr
