@@ -162,7 +162,8 @@ __global__ void __launch_bounds__(512) k_init(DevScal *sc, const T *R, T *R0, T 
 template <typename T>
 __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const T *R, int nu, const double *part_xr,
                                            const double *part_s, int nparts, double *hist, int hist_cap,
-                                           cudaGraphConditionalHandle cond, int first_in_body, const int *dev_err) {
+                                           cudaGraphConditionalHandle cond, int first_in_body, const int *dev_err,
+                                           int use_cond) {
     __shared__ double red[64];
     double v[2], w[2];
     reduce_partials<2>(part_xr, nparts, nullptr, 0, v, red);
@@ -170,7 +171,7 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
     const double rho_new = v[0], rr = v[1], ss = w[0];
     const int st = sc->status;
     if (st != ST_RUNNING) {
-        if (b0t0()) cudaGraphSetConditional(cond, 0);
+        if (b0t0() && use_cond) cudaGraphSetConditional(cond, 0);
         return;
     }
     if (b0t0() && first_in_body) sc->bodies += 1;
@@ -187,7 +188,7 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
         if (b0t0()) {
             sc->status = term;
             sc->rr_last = rr;
-            cudaGraphSetConditional(cond, 0);
+            if (use_cond) cudaGraphSetConditional(cond, 0);
         }
         return;
     }
@@ -522,7 +523,7 @@ hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R,
     hhp_status st = HHP_OK;
     for (int k = 0; k < s->unroll && st == HHP_OK; ++k) {
         k_p<T><<<s->nblk, s->nthr, 0, s->s2>>>(sc, P, V, R, nu, part_xr, part_s, s->nblk, s->hist, s->hist_cap, cond,
-                                               k == 0 ? 1 : 0, A->ctx->dev_err);
+                                               k == 0 ? 1 : 0, A->ctx->dev_err, 1);
         if (fp32)
             st = launch_spmv32(A, s->s2, EP_DOT1, reinterpret_cast<const float *>(P), reinterpret_cast<float *>(V),
                                reinterpret_cast<const float *>(R0));
@@ -546,6 +547,42 @@ hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R,
     HHP_CUDA(e);
     HHP_CUDA(cudaGetLastError());
     *cond_out = cond;
+    return HHP_OK;
+}
+
+// The FP64 loop launched kernel by kernel (no graph), for profilers that cannot see inside
+// conditional graph nodes: same kernels and order; the host reads the status every `unroll`
+// iterations. Selected with HHP_SOLVE_GRAPH=0.
+hhp_status run_direct64(Solver *s) {
+    hhp_mat *A = s->A;
+    cudaStream_t st = A->ctx->stream;
+    const int nu = s->n_pad / 2;
+    HHP_CUDA(cudaMemcpyAsync(s->sc, s->h_sc, kCtlBytes, cudaMemcpyHostToDevice, st));
+    HHP_TRY(launch_spmv64(A, st, EP_RESID, s->X, s->R, s->B, 1.0, 0.0));
+    k_init<double><<<s->nblk, s->nthr, 0, st>>>(s->sc, s->R, s->R0, s->P, s->V, nu, parts_of(A->plan64), s->part_xr,
+                                                 s->part_s);
+    A->ctx->kernel_launches += 1;
+    const PlanDev &pl = A->plan64;
+    for (;;) {
+        for (int k = 0; k < s->unroll; ++k) {
+            k_p<double><<<s->nblk, s->nthr, 0, st>>>(s->sc, s->P, s->V, s->R, nu, s->part_xr, s->part_s, s->nblk,
+                                                      s->hist, s->hist_cap, cudaGraphConditionalHandle(), k == 0,
+                                                      A->ctx->dev_err, 0);
+            HHP_TRY(launch_spmv64(A, st, EP_DOT1, s->P, s->V, s->R0, 1.0, 0.0));
+            k_s<double><<<s->nblk, s->nthr, 0, st>>>(s->sc, s->S, s->R, s->V, nu, parts_of(pl), s->part_s);
+            HHP_TRY(launch_spmv64(A, st, EP_DOT2, s->S, s->T, s->S, 1.0, 0.0));
+            k_xr<double><<<s->nblk, s->nthr, 0, st>>>(s->sc, s->X, s->R, s->P, s->S, s->T, s->R0, nu, parts_of(pl),
+                                                       s->part_s, s->nblk, s->part_xr);
+            A->ctx->kernel_launches += 3;
+        }
+        HHP_CUDA(cudaMemcpyAsync(s->h_sc, s->sc, sizeof(DevScal), cudaMemcpyDeviceToHost, st));
+        HHP_CUDA(cudaStreamSynchronize(st));
+        if (s->h_sc->status != ST_RUNNING) break;
+    }
+    HHP_TRY(launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0));
+    k_finish<<<1, 32, 0, st>>>(s->sc, parts_of(A->plan64));
+    A->ctx->kernel_launches += 1;
+    HHP_CUDA(cudaGetLastError());
     return HHP_OK;
 }
 
@@ -655,7 +692,7 @@ hhp_status build_gmix(Solver *s) {
         for (int k = 0; k < s->unroll && rc == HHP_OK; ++k) {
             k_p<float><<<s->nblk, s->nthr, 0, s->s2>>>(s->sc32, s->P32, s->V32, s->R32, nu, s->part_xr32,
                                                        s->part_s32, s->nblk, s->hist, s->hist_cap, cond, k == 0,
-                                                       A->ctx->dev_err);
+                                                       A->ctx->dev_err, 1);
             rc = launch_spmv32(A, s->s2, EP_DOT1, s->P32, s->V32, s->R0_32);
             if (rc != HHP_OK) break;
             k_s<float><<<s->nblk, s->nthr, 0, s->s2>>>(s->sc32, s->S32, s->R32, s->V32, nu, parts_of(A->plan32),
@@ -755,16 +792,21 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
     double rel_true = NAN, rel_rec = NAN;
 
     if (!mixed) {
-        if (!s->g64) HHP_TRY(build_g64(s));
+        const bool use_graph = env_int("HHP_SOLVE_GRAPH", 1) != 0;
+        if (use_graph && !s->g64) HHP_TRY(build_g64(s));
         int dev_status = ST_RUNNING;
         for (int pass = 0; pass < max_outer; ++pass) {
             h.restart = pass > 0 ? 1 : 0;
             h.first_outer = 0;
-            HHP_CUDA(cudaGraphLaunch(s->g64, st));
+            if (use_graph) {
+                HHP_CUDA(cudaGraphLaunch(s->g64, st));
+            } else {
+                HHP_TRY(run_direct64(s));
+            }
             HHP_CUDA(cudaMemcpyAsync(s->h_sc, s->sc, sizeof(DevScal), cudaMemcpyDeviceToHost, st));
             HHP_CUDA(cudaStreamSynchronize(st));
             ++outer;
-            ctx->kernel_launches += s->g64_kernels_pro + s->g64_kernels_epi + 5LL * s->unroll * h.bodies;
+            if (use_graph) ctx->kernel_launches += s->g64_kernels_pro + s->g64_kernels_epi + 5LL * s->unroll * h.bodies;
             dev_status = h.status;
             // Residual replacement: the recursive residual met the threshold but the true one
             // did not (rounding drift); restart from the current iterate with the original r0.

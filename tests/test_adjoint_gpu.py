@@ -39,7 +39,8 @@ def test_finite_differences(ctx):
     """Central differences of L on 8 entries of b and 8 stored entries of A, every solve at
     rtol 1e-13. L is exactly quadratic in b, so for b the step can be large (h = 1e-2) and the
     difference is exact up to the solver error / h. For A the truncation error is removed by
-    Richardson extrapolation of the h and h/2 central differences (h = 1e-4, O(h^4) remainder).
+    Richardson extrapolation of the h and h/2 central differences (h = 2e-2 on entries of size
+    1..5, O(h^4) remainder), which keeps the solver error / h below 1e-7.
     The difference of L is formed as 1/2 (x+ - x-).(x+ + x- - 2 x_t) to avoid cancellation.
     (With h = 1e-6 the check would measure the solver: its error rtol*cond(A)*|x| over h.)"""
     s = synth.convdiff2d(64, 30.0, (1.0, 0.5), seed=4, target="normal")
@@ -67,7 +68,7 @@ def test_finite_differences(ctx):
         bm[i] -= hb
         g = cd(solve(bp, s.val), solve(bm, s.val), hb)
         assert abs(g - dldb[i]) <= 1e-6 * max(abs(dldb[i]), 1e-2 * np.max(np.abs(dldb))), (i, g, dldb[i])
-    ha = 1e-4
+    ha = 2e-2
     for kk in rng.choice(s.nnz, 8, replace=False):
         est = []
         for h in (ha, ha / 2):
