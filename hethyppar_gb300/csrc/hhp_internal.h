@@ -149,7 +149,7 @@ inline int pad4(int n) { return (n + 3) & ~3; }
 
 // Kernel tuning knobs (environment overrides read once).
 struct Tuning {
-    int cap = 2048, long_thr = 256, window = 8192, wpc = 16, ctas_per_sm = 2, vec_blocks_per_sm = 2,
+    int cap = 2048, long_thr = 256, window = 8192, wpc = 8, ctas_per_sm = 3, vec_blocks_per_sm = 2,
         unroll_iters = 4;
 };
 const Tuning &tuning();

@@ -128,14 +128,25 @@ __device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, int lane,
     VT acc[R];
 #pragma unroll
     for (int t = 0; t < R; ++t) acc[t] = VT(0);
-    int j = 0;
-    for (; j + kUnroll <= maxlen; j += kUnroll) {
-        VV v[kUnroll];
-        IV c[kUnroll];
+    // Software pipeline over groups of kUnroll steps: the values and indices of group g+1 are
+    // requested before the gathers and multiply-adds of group g, so the HBM latency of the
+    // streams overlaps the L1/L2 latency of the gathers (warps issue in order: a load placed
+    // after a stalled FMA would wait for it).
+    VV v[kUnroll];
+    IV c[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+        v[u] = u < maxlen ? __ldg(vp + static_cast<size_t>(u) * 32) : VV();
+        c[u] = u < maxlen ? __ldg(cp + static_cast<size_t>(u) * 32) : IV();
+    }
+    for (int j = 0; j < maxlen; j += kUnroll) {
+        VV vn[kUnroll];
+        IV cn[kUnroll];
 #pragma unroll
         for (int u = 0; u < kUnroll; ++u) {
-            v[u] = __ldg(vp + static_cast<size_t>(j + u) * 32);
-            c[u] = __ldg(cp + static_cast<size_t>(j + u) * 32);
+            const int jn = j + kUnroll + u;
+            vn[u] = jn < maxlen ? __ldg(vp + static_cast<size_t>(jn) * 32) : VV();
+            cn[u] = jn < maxlen ? __ldg(cp + static_cast<size_t>(jn) * 32) : IV();
         }
         VT xv[kUnroll][R];
 #pragma unroll
@@ -147,13 +158,11 @@ __device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, int lane,
 #pragma unroll
             for (int t = 0; t < R; ++t)
                 if (j + u < len[t]) acc[t] = vfma(comp<VV, VT>(v[u], t), xv[u][t], acc[t]);
-    }
-    for (; j < maxlen; ++j) {
-        const VV v = __ldg(vp + static_cast<size_t>(j) * 32);
-        const IV c = __ldg(cp + static_cast<size_t>(j) * 32);
 #pragma unroll
-        for (int t = 0; t < R; ++t)
-            if (j < len[t]) acc[t] = vfma(comp<VV, VT>(v, t), __ldg(a.x + comp<IV, int>(c, t)), acc[t]);
+        for (int u = 0; u < kUnroll; ++u) {
+            v[u] = vn[u];
+            c[u] = cn[u];
+        }
     }
 #pragma unroll
     for (int t = 0; t < R; ++t) {
@@ -206,7 +215,7 @@ __device__ __forceinline__ void do_chunk(const SellArgs<VT> &a, int c, int lane)
 }
 
 template <typename VT, int EP>
-__global__ void __launch_bounds__(512, 2) k_spmv(const SellArgs<VT> a) {
+__global__ void __launch_bounds__(256, 3) k_spmv(const SellArgs<VT> a) {
     // After a recorded device error every later launch returns at once (uniform across the grid).
     if (*reinterpret_cast<volatile const int *>(a.err) != DEV_OK) return;
     __shared__ double red[32 * 2];
@@ -308,7 +317,7 @@ hhp_status build_plan_dev(hhp_mat *A, PlanDev &p) {
     p.sorted = h.sorted;
     p.total = h.total;
     p.padding = h.padding;
-    p.warps_per_cta = std::min(std::max(t.wpc, 1), 16);
+    p.warps_per_cta = std::min(std::max(t.wpc, 1), 8);
     p.ctas = ctx->num_sms * std::min(std::max(t.ctas_per_sm, 1), 8);
     HHP_TRY(upload(&p.slice_ptr, h.slice_ptr));
     HHP_TRY(upload(&p.pos_row, h.pos_row, 4));
