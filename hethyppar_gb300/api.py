@@ -207,7 +207,7 @@ def _opts(rtol, maxit, precision, inner_rtol, max_outer, fixed_iters, print_ever
 
 
 def bicgstab(ctx: Context, A: Matrix, b, x=None, x_target=None, *, rtol: float = 1e-10, maxit: int = 2000,
-             precision: str = "fp64", inner_rtol: float = 1e-5, max_outer: int = 50, fixed_iters: bool = False,
+             precision: str = "fp64", inner_rtol: float = 0.1, max_outer: int = 50, fixed_iters: bool = False,
              record_history: bool = False, callback: Optional[Callable[[int, float], None]] = None,
              print_every: int = 1, raise_on_error: bool = True):
     """Solves A x = b. Host numpy arrays use hhp_bicgstab (copies in/out); CUDA tensors use
@@ -247,7 +247,7 @@ def bicgstab(ctx: Context, A: Matrix, b, x=None, x_target=None, *, rtol: float =
 def bicgstab_backward(ctx: Context, A: Matrix, x, dldx, *, rtol: float = 1e-12, maxit: int = 20000,
                       precision: str = "fp64", want_dlda: bool = True):
     """Adjoint of x = A^-1 b: returns (dL/db, dL/dA over A's stored entries, SolveResult)."""
-    o = _opts(rtol, maxit, precision, 1e-5, 50, False, 0, None)
+    o = _opts(rtol, maxit, precision, 0.1, 50, False, 0, None)
     info = SolveInfo()
     if _is_dev(x):
         import torch

@@ -124,37 +124,54 @@ __device__ __forceinline__ void block_sum(double (&v)[NC], double *scratch /* >=
 }
 
 // Sum of per-block partials part[i*NC + c] for i in [0, n), plus extra[j*NC + c] for j in
-// [0, n_extra), computed identically by every calling block (fixed order: lane-strided
-// sequential sums, then a butterfly). Must be called by all threads of the block; the result is
-// returned to every thread. Reads use ld.global.cg so values written by earlier kernels (or by
-// other blocks before a fence) are seen.
+// [0, n_extra), computed identically by every calling block: every thread first loads its
+// share (thread t takes entries t, t + blockDim.x, ...; all loads are issued before any add,
+// so the whole reduction costs one memory round trip), then a warp butterfly and a sum of the
+// warp results in warp order. The order is fixed, so every block gets the same bits. Must be
+// called by all threads; the result is returned to every thread. Loads use ld.global.cg so values
+// written by earlier kernels are read from L2.
 template <int NC>
 __device__ __forceinline__ void reduce_partials(const double *__restrict__ part, int n,
                                                 const double *__restrict__ extra, int n_extra,
-                                                double (&out)[NC], double *scratch /* >= NC doubles */) {
-    if (threadIdx.x < 32) {
-        const int lane = threadIdx.x;
-        double s[NC];
+                                                double (&out)[NC], double *scratch /* >= 32*NC doubles */) {
+    double s[NC];
 #pragma unroll
-        for (int c = 0; c < NC; ++c) s[c] = 0.0;
-        for (int i = lane; i < n; i += 32) {
+    for (int c = 0; c < NC; ++c) s[c] = 0.0;
+    const int T = blockDim.x, t = threadIdx.x;
+    double a[2][NC], b[2][NC];
 #pragma unroll
-            for (int c = 0; c < NC; ++c) s[c] += __ldcg(part + (size_t)i * NC + c);
+    for (int q = 0; q < 2; ++q) {
+        const int i = t + q * T;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            a[q][c] = i < n ? __ldcg(part + (size_t)i * NC + c) : 0.0;
+            b[q][c] = i < n_extra ? __ldcg(extra + (size_t)i * NC + c) : 0.0;
         }
-        for (int i = lane; i < n_extra; i += 32) {
+    }
 #pragma unroll
-            for (int c = 0; c < NC; ++c) s[c] += __ldcg(extra + (size_t)i * NC + c);
-        }
+    for (int c = 0; c < NC; ++c) s[c] = (a[0][c] + a[1][c]) + (b[0][c] + b[1][c]);
+    for (int i = t + 2 * T; i < n; i += T) {  // only for more than 2*blockDim partials
 #pragma unroll
-        for (int c = 0; c < NC; ++c) s[c] = warp_sum(s[c]);
-        if (lane == 0) {
+        for (int c = 0; c < NC; ++c) s[c] += __ldcg(part + (size_t)i * NC + c);
+    }
+    for (int i = t + 2 * T; i < n_extra; i += T) {
 #pragma unroll
-            for (int c = 0; c < NC; ++c) scratch[c] = s[c];
-        }
+        for (int c = 0; c < NC; ++c) s[c] += __ldcg(extra + (size_t)i * NC + c);
+    }
+    const int lane = t & 31, warp = t >> 5, nw = (T + 31) >> 5;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) s[c] = warp_sum(s[c]);
+    if (lane == 0) {
+#pragma unroll
+        for (int c = 0; c < NC; ++c) scratch[warp * NC + c] = s[c];
     }
     __syncthreads();
 #pragma unroll
-    for (int c = 0; c < NC; ++c) out[c] = scratch[c];
+    for (int c = 0; c < NC; ++c) {
+        double v = 0.0;
+        for (int w = 0; w < nw; ++w) v += scratch[w * NC + c];
+        out[c] = v;
+    }
     __syncthreads();
 }
 

@@ -114,8 +114,9 @@ hhp_status ensure_plan(hhp_mat *A, bool fp32);
 // Rewrites the slice values of existing plans from the CSR values (after a value change).
 hhp_status refresh_plan_values(hhp_mat *A);
 // Launches the FP64 SpMV with an epilogue on `stream` (x, y, w1 length-padded device vectors).
+// gate (nullable, device int): the launch does nothing when *gate == 0 at kernel start.
 hhp_status launch_spmv64(hhp_mat *A, cudaStream_t stream, EpKind ep, const double *x, double *y, const double *w1,
-                         double alpha, double beta);
+                         double alpha, double beta, const int *gate = nullptr);
 hhp_status launch_spmv32(hhp_mat *A, cudaStream_t stream, EpKind ep, const float *x, float *y, const float *w1);
 // Number of partial records (ctas) and long-row records of the last-used plan, for the reducers.
 inline int plan_ctas(const hhp_mat *A, bool fp32) { return fp32 ? A->plan32.ctas : A->plan64.ctas; }

@@ -44,7 +44,10 @@ struct DevScal {
     double rho_prev, rho_cur, alpha, omega, beta;
     double rr0, thr2, bb, rr_last, true_rr;
     double rd2, hist_scale;
-    int iter, iter_start, status, bodies, outer_conv, pad_;
+    double thr2_rec;      // threshold for the recursive-residual tests (-1: none, mixed form)
+    double rr_max[2];     // mixed form: largest recursive ||r||^2 since the last FP64 update,
+                          // double-buffered by iteration parity (read one, write the other)
+    int iter, iter_start, status, bodies, outer_conv, ru_flag, updates, pad_;
 };
 constexpr size_t kCtlBytes = offsetof(DevScal, rho_prev);
 
@@ -143,6 +146,7 @@ __global__ void __launch_bounds__(512) k_init(DevScal *sc, const T *R, T *R0, T 
             // gpu_BiCGStab's threshold rtol ||r0|| (bicgstab_gpu.c:149-150) is the same for x0 = 0.
             sc->rr0 = bb;
             sc->thr2 = sc->fixed ? -1.0 : sc->rtol2 * bb;
+            sc->thr2_rec = sc->thr2;
             sc->iter = 0;
             sc->bb = bb;
             sc->hist_scale = 1.0;
@@ -176,7 +180,7 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
     }
     if (b0t0() && first_in_body) sc->bodies += 1;
     const int iter = sc->iter, it0 = sc->iter_start;
-    const double thr2 = sc->thr2;
+    const double thr2 = sc->thr2_rec;
     if (b0t0() && iter > it0 && iter - 1 < hist_cap) hist[iter - 1] = sc->hist_scale * sqrt(rr / sc->rr0);
     int term = ST_RUNNING;
     if (*reinterpret_cast<volatile const int *>(dev_err) != DEV_OK) term = ST_DEVICE_ERROR;
@@ -262,7 +266,7 @@ __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P,
     reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
     reduce_partials<2>(part_s, nparts, nullptr, 0, w, red);
     if (sc->status != ST_RUNNING) return;
-    const double thr2 = sc->thr2;
+    const double thr2 = sc->thr2_rec;
     const bool half = thr2 >= 0.0 && w[0] <= thr2;
     const double alpha = sc->alpha;
     double omega = 0.0;
@@ -324,47 +328,32 @@ __global__ void k_finish(DevScal *sc, SpmvParts sp) {
     }
 }
 
-// Mixed form, outer step: given the FP64 residual Rd = B - A X (partials ||Rd||^2, ||B||^2),
-// decide convergence; otherwise scale Rd to unit norm into the FP32 right-hand side and reset
-// the FP32 inner solver (initial guess 0, so r = r0 = rhs).
-__global__ void __launch_bounds__(512) k_mix_prep(DevScal *sc, DevScal *sc32, const double *Rd, float *D32,
-                                                  float *R32, float *R0_32, float *P32, float *V32, int nu4,
-                                                  SpmvParts sp, double *part_xr32, double *part_s32,
-                                                  cudaGraphConditionalHandle inner_cond) {
+// Mixed form (reliable updates). The BiCGStab recurrences run in FP32 on A32 = float(A) and FP32
+// vectors, with the increment d of the solution accumulated in FP32; the FP64 iterate x, the
+// FP64 true residual and the dot-product partials stay FP64. Whenever the FP32 recursive
+// residual has dropped by a factor delta since the last update (or looks converged, or the
+// iteration budget is spent), the update step runs in FP64:
+//     x += d, d = 0, r_true = b - A x (FP64 SpMV), r = float(r_true)
+// and the recurrences continue from the replaced residual with the same directions p and
+// shadow r0 (residual replacement), so no Krylov information is thrown away. Convergence is
+// decided on the FP64 true residual only.
+
+// After the FP64 residual SpMV (Rd = B - A X; partials ||Rd||^2, ||B||^2): start the FP32 loop.
+__global__ void __launch_bounds__(512) k_mix_init(DevScal *sc, const double *Rd, float *R32, float *R0_32,
+                                                  float *D32, float *P32, float *V32, int nu4, SpmvParts sp,
+                                                  double *part_xr32, double *part_s32) {
     __shared__ double red[64];
     double v[2];
     reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
     const double rd2 = v[0], bb = v[1];
-    const bool first = sc->first_outer != 0;
-    const double rr0 = first ? bb : sc->rr0;
-    const double thr2 = sc->rtol2 * rr0;
-    if (b0t0()) {
-        if (first) {
-            sc->rr0 = bb;
-            sc->bb = bb;
-            sc->thr2 = thr2;
-            sc->iter = 0;
-            sc32->iter = 0;
-        }
-        sc->rd2 = rd2;
-    }
-    if (rd2 <= thr2 || !isfinite(rd2)) {
-        if (b0t0()) {
-            sc->outer_conv = isfinite(rd2) ? 1 : -1;
-            cudaGraphSetConditional(inner_cond, 0);
-        }
-        return;
-    }
-    if (b0t0()) sc->outer_conv = 0;
-    const double scale = 1.0 / sqrt(rd2);
     double acc[1] = {0.0};
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu4; u += gridDim.x * blockDim.x) {
         const double2 a = reinterpret_cast<const double2 *>(Rd)[2 * u];
         const double2 b = reinterpret_cast<const double2 *>(Rd)[2 * u + 1];
-        float4 r = make_float4(static_cast<float>(a.x * scale), static_cast<float>(a.y * scale),
-                               static_cast<float>(b.x * scale), static_cast<float>(b.y * scale));
+        const float4 r = make_float4(static_cast<float>(a.x), static_cast<float>(a.y), static_cast<float>(b.x),
+                                     static_cast<float>(b.y));
         acc[0] = dacc(dacc(dacc(dacc(acc[0], r.x, r.x), r.y, r.y), r.z, r.z), r.w, r.w);
-        const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
         reinterpret_cast<float4 *>(R32)[u] = r;
         reinterpret_cast<float4 *>(R0_32)[u] = r;
         reinterpret_cast<float4 *>(D32)[u] = z;
@@ -379,33 +368,109 @@ __global__ void __launch_bounds__(512) k_mix_prep(DevScal *sc, DevScal *sc32, co
         part_s32[2 * blockIdx.x + 1] = 0.0;
     }
     if (b0t0()) {
-        sc32->rr0 = 1.0;
-        sc32->thr2 = sc->inner_rtol2;
-        sc32->iter_start = sc32->iter;
-        sc32->maxit = sc->maxit;
-        sc32->hist_scale = sqrt(rd2 / rr0);
-        sc32->rho_prev = 1.0;
-        sc32->alpha = 1.0;
-        sc32->omega = 1.0;
-        sc32->status = ST_RUNNING;
-        sc32->bodies = 0;
+        sc->rr0 = bb;
+        sc->bb = bb;
+        sc->thr2 = sc->rtol2 * bb;
+        sc->thr2_rec = -1.0;
+        sc->iter = 0;
+        sc->iter_start = 0;
+        sc->hist_scale = 1.0;
+        sc->rho_prev = 1.0;
+        sc->alpha = 1.0;
+        sc->omega = 1.0;
+        sc->bodies = 0;
+        sc->rr_max[0] = sc->rr_max[1] = rd2;
+        sc->true_rr = rd2;
+        sc->rr_last = rd2;
+        sc->updates = 0;
+        sc->ru_flag = 0;
+        sc->status = (rd2 <= sc->rtol2 * bb) ? ST_CONVERGED : (isfinite(rd2) ? ST_RUNNING : ST_BREAKDOWN);
     }
 }
 
-// Mixed form: x += ||Rd|| * d (FP64 update of the FP64 iterate).
-__global__ void __launch_bounds__(512) k_mix_update(const DevScal *sc, double *X, const float *D32, int nu4) {
-    if (sc->outer_conv != 0) return;
-    const double s = sqrt(sc->rd2);
+// After K_XR: decide whether this iteration ends with an FP64 update; if so x += d, d = 0.
+__global__ void __launch_bounds__(512) k_ru_check(DevScal *sc, double *X, float *D32, int nu4,
+                                                  const double *part_xr32, int nparts) {
+    __shared__ double red[64];
+    double v[2];
+    reduce_partials<2>(part_xr32, nparts, nullptr, 0, v, red);
+    if (sc->status != ST_RUNNING) {
+        if (b0t0()) sc->ru_flag = 0;
+        return;
+    }
+    const double rr = v[1];
+    const int it = sc->iter;
+    const double mx = sc->rr_max[it & 1];
+    const bool update = rr <= sc->thr2 || rr < sc->inner_rtol2 * mx || it >= sc->maxit || !isfinite(rr);
+    if (b0t0()) {
+        sc->rr_max[(it + 1) & 1] = update ? mx : fmax(mx, rr);
+        sc->ru_flag = update ? 1 : 0;
+    }
+    if (!update) return;
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu4; u += gridDim.x * blockDim.x) {
         const float4 d = reinterpret_cast<const float4 *>(D32)[u];
         double2 a = reinterpret_cast<double2 *>(X)[2 * u];
         double2 b = reinterpret_cast<double2 *>(X)[2 * u + 1];
-        a.x = fma(s, static_cast<double>(d.x), a.x);
-        a.y = fma(s, static_cast<double>(d.y), a.y);
-        b.x = fma(s, static_cast<double>(d.z), b.x);
-        b.y = fma(s, static_cast<double>(d.w), b.y);
+        a.x += static_cast<double>(d.x);
+        a.y += static_cast<double>(d.y);
+        b.x += static_cast<double>(d.z);
+        b.y += static_cast<double>(d.w);
         reinterpret_cast<double2 *>(X)[2 * u] = a;
         reinterpret_cast<double2 *>(X)[2 * u + 1] = b;
+        reinterpret_cast<float4 *>(D32)[u] = z;
+    }
+}
+
+// After the gated FP64 residual SpMV: replace the FP32 residual, recompute its dot partials,
+// test convergence on the FP64 true residual.
+__global__ void __launch_bounds__(512) k_ru_apply(DevScal *sc, const double *Rd, float *R32, const float *R0_32,
+                                                  int nu4, SpmvParts sp, double *part_xr32) {
+    __shared__ double red[64];
+    if (!sc->ru_flag) return;
+    double v[2];
+    reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
+    const double rd2 = v[0];
+    double acc[2] = {0.0, 0.0};
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu4; u += gridDim.x * blockDim.x) {
+        const double2 a = reinterpret_cast<const double2 *>(Rd)[2 * u];
+        const double2 b = reinterpret_cast<const double2 *>(Rd)[2 * u + 1];
+        const float4 r = make_float4(static_cast<float>(a.x), static_cast<float>(a.y), static_cast<float>(b.x),
+                                     static_cast<float>(b.y));
+        const float4 r0 = reinterpret_cast<const float4 *>(R0_32)[u];
+        acc[0] = dacc(dacc(dacc(dacc(acc[0], r.x, r0.x), r.y, r0.y), r.z, r0.z), r.w, r0.w);
+        acc[1] = dacc(dacc(dacc(dacc(acc[1], r.x, r.x), r.y, r.y), r.z, r.z), r.w, r.w);
+        reinterpret_cast<float4 *>(R32)[u] = r;
+    }
+    block_sum<2>(acc, red);
+    if (threadIdx.x == 0) {
+        part_xr32[2 * blockIdx.x] = acc[0];
+        part_xr32[2 * blockIdx.x + 1] = acc[1];
+    }
+    if (b0t0()) {
+        const int it = sc->iter;
+        sc->rr_max[(it + 1) & 1] = rd2;
+        sc->updates = sc->updates + 1;
+        sc->true_rr = rd2;
+        if (rd2 <= sc->thr2) sc->status = ST_CONVERGED;
+        else if (!isfinite(rd2)) sc->status = ST_BREAKDOWN;
+        else if (it >= sc->maxit) sc->status = ST_MAXIT;
+    }
+}
+
+// After the loop: fold any increment not yet absorbed by an update into x.
+__global__ void __launch_bounds__(512) k_mix_final(double *X, float *D32, int nu4) {
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu4; u += gridDim.x * blockDim.x) {
+        const float4 d = reinterpret_cast<const float4 *>(D32)[u];
+        double2 a = reinterpret_cast<double2 *>(X)[2 * u];
+        double2 b = reinterpret_cast<double2 *>(X)[2 * u + 1];
+        a.x += static_cast<double>(d.x);
+        a.y += static_cast<double>(d.y);
+        b.x += static_cast<double>(d.z);
+        b.y += static_cast<double>(d.w);
+        reinterpret_cast<double2 *>(X)[2 * u] = a;
+        reinterpret_cast<double2 *>(X)[2 * u + 1] = b;
+        reinterpret_cast<float4 *>(D32)[u] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
 }
 
@@ -628,8 +693,8 @@ hhp_status build_g64(Solver *s) {
     return HHP_OK;
 }
 
-// Mixed outer-step graph: FP64 residual, prep (convergence test + FP32 RHS), WHILE{FP32 loop},
-// FP64 update.
+// Mixed-form graph: FP64 residual, init, WHILE{ unroll x [FP32 iteration, update check, gated
+// FP64 residual, gated residual replacement] }, fold d into x, FP64 true residual, finish.
 hhp_status build_gmix(Solver *s) {
     hhp_mat *A = s->A;
     cudaStream_t st = A->ctx->stream;
@@ -639,13 +704,14 @@ hhp_status build_gmix(Solver *s) {
     HHP_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
     hhp_status rc = HHP_OK;
     do {
-        if (cudaMemcpyAsync(s->sc, s->h_sc, kCtlBytes, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+        if (cudaMemcpyAsync(s->sc32, s->h_sc32, kCtlBytes, cudaMemcpyHostToDevice, st) != cudaSuccess) {
             rc = HHP_ERR_CUDA;
             break;
         }
         rc = launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0);
         if (rc != HHP_OK) break;
-        // k_mix_prep may skip the inner loop, so the loop's condition handle is created first.
+        k_mix_init<<<s->nblk, s->nthr, 0, st>>>(s->sc32, s->Y, s->R32, s->R0_32, s->D32, s->P32, s->V32, nu4,
+                                                 parts_of(A->plan64), s->part_xr32, s->part_s32);
         cudaStreamCaptureStatus cs;
         cudaGraph_t g = nullptr;
         const cudaGraphNode_t *deps = nullptr;
@@ -656,13 +722,6 @@ hhp_status build_gmix(Solver *s) {
         }
         cudaGraphConditionalHandle cond;
         if (cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) {
-            rc = HHP_ERR_CUDA;
-            break;
-        }
-        k_mix_prep<<<s->nblk, s->nthr, 0, st>>>(s->sc, s->sc32, s->Y, s->D32, s->R32, s->R0_32, s->P32, s->V32, nu4,
-                                                 parts_of(A->plan64), s->part_xr32, s->part_s32, cond);
-        // WHILE node using the pre-created handle.
-        if (cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd) != cudaSuccess) {
             rc = HHP_ERR_CUDA;
             break;
         }
@@ -702,6 +761,11 @@ hhp_status build_gmix(Solver *s) {
             k_xr<float><<<s->nblk, s->nthr, 0, s->s2>>>(s->sc32, s->D32, s->R32, s->P32, s->S32, s->T32, s->R0_32,
                                                         nu, parts_of(A->plan32), s->part_s32, s->nblk,
                                                         s->part_xr32);
+            k_ru_check<<<s->nblk, s->nthr, 0, s->s2>>>(s->sc32, s->X, s->D32, nu4, s->part_xr32, s->nblk);
+            rc = launch_spmv64(A, s->s2, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0, &s->sc32->ru_flag);
+            if (rc != HHP_OK) break;
+            k_ru_apply<<<s->nblk, s->nthr, 0, s->s2>>>(s->sc32, s->Y, s->R32, s->R0_32, nu4, parts_of(A->plan64),
+                                                       s->part_xr32);
         }
         cudaGraph_t body_out = body;
         cudaError_t e2 = cudaStreamEndCapture(s->s2, &body_out);
@@ -710,7 +774,10 @@ hhp_status build_gmix(Solver *s) {
             rc = HHP_ERR_CUDA;
             break;
         }
-        k_mix_update<<<s->nblk, s->nthr, 0, st>>>(s->sc, s->X, s->D32, nu4);
+        k_mix_final<<<s->nblk, s->nthr, 0, st>>>(s->X, s->D32, nu4);
+        rc = launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0);
+        if (rc != HHP_OK) break;
+        k_finish<<<1, 32, 0, st>>>(s->sc32, parts_of(A->plan64));
     } while (0);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(st, &g);
@@ -725,8 +792,9 @@ hhp_status build_gmix(Solver *s) {
     cudaGraphDestroy(g);
     HHP_CUDA(ie);
     s->gmix_kernels_pro = 2;
-    s->gmix_kernels_epi = 1;
-    A->ctx->kernel_launches -= 1 + 2 * s->unroll;
+    s->gmix_kernels_epi = 3;
+    // launch_spmv* counted their captured launches; graph launches are counted when executed.
+    A->ctx->kernel_launches -= 2 + 3 * s->unroll;
     return HHP_OK;
 }
 
@@ -825,46 +893,24 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
     } else {
         if (!s->gmix) HHP_TRY(build_gmix(s));
         DevScal &h32 = *s->h_sc32;
-        result = HHP_ERR_MAXIT;
-        bool need_final = true;
-        for (int k = 0; k < max_outer; ++k) {
-            h.first_outer = k == 0 ? 1 : 0;
-            h.restart = 0;
-            HHP_CUDA(cudaGraphLaunch(s->gmix, st));
-            HHP_CUDA(cudaMemcpyAsync(s->h_sc, s->sc, sizeof(DevScal), cudaMemcpyDeviceToHost, st));
-            HHP_CUDA(cudaMemcpyAsync(s->h_sc32, s->sc32, sizeof(DevScal), cudaMemcpyDeviceToHost, st));
-            HHP_CUDA(cudaStreamSynchronize(st));
-            ctx->kernel_launches += s->gmix_kernels_pro + s->gmix_kernels_epi + 5LL * s->unroll * h32.bodies;
-            ++outer;
-            if (h.outer_conv == 1) {
-                result = HHP_OK;
-                need_final = false;
-                break;
-            }
-            if (h.outer_conv < 0) {
-                result = HHP_ERR_BREAKDOWN;
-                need_final = false;
-                break;
-            }
-            if (h32.iter >= o->maxit) break;  // budget spent (this step's update was applied)
-            if (h32.status == ST_BREAKDOWN && h32.iter == h32.iter_start) {
-                result = HHP_ERR_BREAKDOWN;
-                break;
-            }
-        }
+        h32.rtol2 = o->rtol * o->rtol;
+        const double delta = o->inner_rtol > 0.0 ? o->inner_rtol : 0.1;
+        h32.inner_rtol2 = delta * delta;
+        h32.maxit = o->maxit;
+        h32.fixed = 0;
+        h32.restart = 0;
+        h32.first_outer = 1;
+        HHP_CUDA(cudaGraphLaunch(s->gmix, st));
+        HHP_CUDA(cudaMemcpyAsync(s->h_sc32, s->sc32, sizeof(DevScal), cudaMemcpyDeviceToHost, st));
+        HHP_CUDA(cudaStreamSynchronize(st));
+        ctx->kernel_launches += s->gmix_kernels_pro + s->gmix_kernels_epi + 8LL * s->unroll * h32.bodies;
         total_iters = h32.iter;
-        half = h32.status == ST_CONVERGED_HALF;
-        if (need_final) {
-            HHP_TRY(launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0));
-            k_finish<<<1, 32, 0, st>>>(s->sc, parts_of(A->plan64));
-            ctx->kernel_launches += 1;
-            HHP_CUDA(cudaMemcpyAsync(s->h_sc, s->sc, sizeof(DevScal), cudaMemcpyDeviceToHost, st));
-            HHP_CUDA(cudaStreamSynchronize(st));
-            rel_true = sqrt(h.true_rr / h.bb);
-        } else {
-            rel_true = sqrt(h.rd2 / h.bb);
-        }
-        rel_rec = rel_true;
+        outer = h32.updates;
+        half = 0;
+        result = status_of(h32.status);
+        rel_true = sqrt(h32.true_rr / h32.bb);
+        if (result == HHP_OK && !(h32.true_rr <= h32.thr2)) result = HHP_ERR_MAXIT;
+        rel_rec = sqrt(h32.rr_last / h32.rr0);
     }
     HHP_CUDA(cudaEventRecord(ctx->ev1, st));
     HHP_CUDA(cudaMemcpyAsync(x_io, s->X, sizeof(double) * static_cast<size_t>(A->n),

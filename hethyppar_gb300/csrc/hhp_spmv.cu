@@ -71,6 +71,8 @@ struct SellArgs {
     VT *y;
     const VT *w1;
     double alpha, beta;
+    int scale, accum;  // alpha != 1, beta != 0 (decided on the host)
+    const int *gate;   // nullable: skip the whole launch when *gate == 0
     int *err;
     int m, n_slices, n_chunks;
     bool has_perm;
@@ -89,8 +91,8 @@ template <typename VT, int EP>
 __device__ __forceinline__ void row_epilogue(const SellArgs<VT> &a, int r, VT acc, double &d0, double &d1) {
     if (EP == EP_AXPBY) {
         VT out = acc;
-        if (a.alpha != 1.0) out = static_cast<VT>(a.alpha) * out;
-        if (a.beta != 0.0) out = vfma(static_cast<VT>(a.beta), a.y[r], out);
+        if (a.scale) out = static_cast<VT>(a.alpha) * out;  // integer flags: no FP64 compares per row
+        if (a.accum) out = vfma(static_cast<VT>(a.beta), a.y[r], out);
         a.y[r] = out;
     } else if (EP == EP_DOT1) {
         a.y[r] = acc;
@@ -218,6 +220,7 @@ template <typename VT, int EP>
 __global__ void __launch_bounds__(256, 3) k_spmv(const SellArgs<VT> a) {
     // After a recorded device error every later launch returns at once (uniform across the grid).
     if (*reinterpret_cast<volatile const int *>(a.err) != DEV_OK) return;
+    if (a.gate && *a.gate == 0) return;
     __shared__ double red[32 * 2];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int gw = blockIdx.x * nw + warp, W = gridDim.x * nw;
@@ -365,6 +368,9 @@ SellArgs<VT> make_args(hhp_mat *A, const PlanDev &p, const VT *csr_val, const VT
     a.w1 = w1;
     a.alpha = alpha;
     a.beta = beta;
+    a.scale = alpha != 1.0 ? 1 : 0;
+    a.accum = beta != 0.0 ? 1 : 0;
+    a.gate = nullptr;
     a.err = A->ctx->dev_err;
     a.m = A->m;
     a.n_slices = p.n_slices;
@@ -405,10 +411,11 @@ hhp_status refresh_plan_values(hhp_mat *A) {
 }
 
 hhp_status launch_spmv64(hhp_mat *A, cudaStream_t stream, EpKind ep, const double *x, double *y, const double *w1,
-                         double alpha, double beta) {
+                         double alpha, double beta, const int *gate) {
     HHP_TRY(ensure_plan(A, false));
     const PlanDev &p = A->plan64;
     SellArgs<double> a = make_args<double>(A, p, A->val, x, y, w1, alpha, beta);
+    a.gate = gate;
     HHP_CUDA(launch_ep<double>(ep, p, a, stream));
     A->ctx->kernel_launches += 1;
     return HHP_OK;

@@ -52,8 +52,10 @@ typedef struct {
                            tol * ||r0||, bicgstab_gpu.c:149-150, when x0 = 0)                   */
     int maxit;          /* iteration cap (maxIterations, bicgstab_gpu.c:120); >= 0                */
     int precision;      /* hhp_precision                                                          */
-    double inner_rtol;  /* mixed form: relative tolerance of each FP32 inner solve (<= 0: 1e-5)   */
-    int max_outer;      /* mixed form: cap on FP64 refinement steps (<= 0: 50)                    */
+    double inner_rtol;  /* mixed form: the FP32 recurrences run until their residual has dropped by
+                           this factor since the last FP64 refinement step x += d,
+                           r = b - A x (<= 0: 0.1)                                               */
+    int max_outer;      /* FP64 form: cap on residual-replacement restarts (<= 0: 50)            */
     int fixed_iters;    /* 1: run exactly maxit iterations with no stop test, like the reference's
                            executables (src/entry/bicgstab_cpu.c:200); FP64 only                  */
     int print_every;    /* callback stride; 0 = no callback                                       */
@@ -63,7 +65,7 @@ typedef struct {
 
 typedef struct {
     int iters;                 /* BiCGStab iterations (mixed: total inner iterations)            */
-    int outer_iters;           /* mixed: FP64 refinement steps; FP64: residual replacements + 1  */
+    int outer_iters;           /* mixed: FP64 refinement steps; FP64: graph passes (restarts + 1) */
     int half_step;             /* 1 if the last iteration stopped at the ||s|| test              */
     double rel_res_true;       /* ||b - A x|| / ||b||, recomputed in FP64 after the solve         */
     double rel_res_recursive;  /* the solver's own ||r_k|| / ||b||                                */

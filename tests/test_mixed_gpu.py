@@ -1,6 +1,7 @@
-"""Mixed precision: FP32 inner BiCGStab (FP32 A and Krylov vectors, FP64 dot partials) inside an
-FP64 refinement loop. Bar: true relative residual <= 1e-10 in FP64, error against the known
-solution and against a plain FP64 solve reported and bounded."""
+"""Mixed precision: BiCGStab recurrences in FP32 (FP32 A and Krylov vectors, FP64 dot partials)
+with FP64 refinement updates x += d, r = b - A x (reliable updates). Bar: true relative residual
+<= 1e-10 in FP64, iteration count close to the FP64 solve's, error against the known solution
+and against a plain FP64 solve bounded."""
 import numpy as np
 import pytest
 
@@ -22,7 +23,8 @@ def test_mixed_reaches_fp64_tolerance(ctx, sysname):
     x64, r64 = bicgstab(ctx, A, s.b, s.x0, s.x_target, rtol=1e-10, maxit=5000)
     xm, rm = bicgstab(ctx, A, s.b, s.x0, s.x_target, rtol=1e-10, maxit=5000, precision="mixed")
     assert r64.status == 0 and rm.status == 0
-    assert rm.rel_res_true <= 1e-10 and rm.outer_iters >= 2
+    assert rm.rel_res_true <= 1e-10 and rm.outer_iters >= 1
+    assert rm.iters <= 1.35 * r64.iters + 5, (rm.iters, r64.iters)
     # independent FP64 residual from the oracle
     res = s.b - orc.spmv(s.rowptr, s.col, s.val, xm)
     assert np.sqrt(orc.dot(res, res) / orc.dot(s.b, s.b)) <= 1.0000001e-10
