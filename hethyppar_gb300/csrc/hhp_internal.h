@@ -46,6 +46,10 @@ struct SellHost {
 // Builds the plan from a host rowptr: rpl rows per lane (H = 32*rpl rows per slice), rows longer
 // than long_thr go to chunks of at most cap nonzeros, `window` rows per length-sort window.
 void build_plan(int m, const int *rowptr, int rpl, int long_thr, int cap, int window, SellHost &out);
+// Deals the plan's units (slices, then chunks) to n_warps warps, balancing their step counts;
+// warp w processes warp_units[warp_ptr[w] .. warp_ptr[w+1]) in ascending order.
+void assign_units(const SellHost &P, int n_warps, std::vector<int> &warp_ptr, std::vector<int> &warp_units,
+                  double *imbalance);
 
 struct PlanDev {
     int rpl = 0, H = 0, n_slices = 0, n_long = 0, n_chunks = 0, ctas = 0, warps_per_cta = 0;
@@ -55,6 +59,9 @@ struct PlanDev {
     long long *slice_ptr = nullptr;   // n_slices + 1
     int *pos_row = nullptr;           // n_slices * H (original row, -1 = padding)
     int *pos_len = nullptr;           // n_slices * H
+    int *warp_ptr = nullptr;          // n_warps + 1
+    int *warp_units = nullptr;        // unit ids (slice s < n_slices, else chunk n_slices + c)
+    double imbalance = 1.0;           // max warp cost / mean warp cost
     void *sval = nullptr;             // total values (double or float), padding zero
     int *scol = nullptr;              // total column indices
     int4 *chunks = nullptr;

@@ -100,10 +100,27 @@ __device__ __forceinline__ void stu(T *p, int u, const T (&o)[Unit<T>::E]) {
 
 __device__ __forceinline__ double tfma(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ float tfma(float a, float b, float c) { return fmaf(a, b, c); }
-// Dot-product accumulation in FP64: one FP64 FMA for FP64 data; for FP32 data the product is
-// formed in FP32 and accumulated in FP64 (the partials stay FP64).
-__device__ __forceinline__ double dacc(double acc, double a, double b) { return fma(a, b, acc); }
-__device__ __forceinline__ double dacc(double acc, float a, float b) { return acc + static_cast<double>(a * b); }
+// Dot-product accumulation into an FP64 partial over one 128-bit unit of E elements: for FP64
+// data one FP64 FMA per element; for FP32 data the unit's E products are summed in FP32 and the
+// unit sum is added in FP64 (one conversion and one FP64 add per 4 elements: GB300's FP64 pipe
+// is ~58x slower than its FP32 pipe, so FP64 work is kept to the cross-unit accumulation).
+template <int E>
+__device__ __forceinline__ double dunit(double acc, const double (&a)[E], const double (&b)[E]) {
+#pragma unroll
+    for (int e = 0; e < E; ++e) acc = fma(a[e], b[e], acc);
+    return acc;
+}
+template <int E>
+__device__ __forceinline__ double dunit(double acc, const float (&a)[E], const float (&b)[E]) {
+    float u = a[0] * b[0];
+#pragma unroll
+    for (int e = 1; e < E; ++e) u = fmaf(a[e], b[e], u);
+    return acc + static_cast<double>(u);
+}
+__device__ __forceinline__ double dunit4(double acc, float4 a, float4 b) {
+    const float u = fmaf(a.w, b.w, fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)));
+    return acc + static_cast<double>(u);
+}
 
 __device__ __forceinline__ bool b0t0() { return blockIdx.x == 0 && threadIdx.x == 0; }
 
@@ -242,10 +259,8 @@ __global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const 
         ldu(r, R, u);
         ldu(vv, V, u);
 #pragma unroll
-        for (int e = 0; e < E; ++e) {
-            s[e] = tfma(ta, vv[e], r[e]);
-            acc[0] = dacc(acc[0], s[e], s[e]);
-        }
+        for (int e = 0; e < E; ++e) s[e] = tfma(ta, vv[e], r[e]);
+        acc[0] = dunit<E>(acc[0], s, s);
         stu(S, u, s);
     }
     block_sum<1>(acc, red);
@@ -302,11 +317,8 @@ __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P,
                 r[e] = s[e];
             }
         }
-#pragma unroll
-        for (int e = 0; e < E; ++e) {
-            acc[0] = dacc(acc[0], r[e], r0[e]);
-            acc[1] = dacc(acc[1], r[e], r[e]);
-        }
+        acc[0] = dunit<E>(acc[0], r, r0);
+        acc[1] = dunit<E>(acc[1], r, r);
         stu(X, u, x);
         stu(R, u, r);
     }
@@ -353,7 +365,7 @@ __global__ void __launch_bounds__(512) k_mix_init(DevScal *sc, const double *Rd,
         const double2 b = reinterpret_cast<const double2 *>(Rd)[2 * u + 1];
         const float4 r = make_float4(static_cast<float>(a.x), static_cast<float>(a.y), static_cast<float>(b.x),
                                      static_cast<float>(b.y));
-        acc[0] = dacc(dacc(dacc(dacc(acc[0], r.x, r.x), r.y, r.y), r.z, r.z), r.w, r.w);
+        acc[0] = dunit4(acc[0], r, r);
         reinterpret_cast<float4 *>(R32)[u] = r;
         reinterpret_cast<float4 *>(R0_32)[u] = r;
         reinterpret_cast<float4 *>(D32)[u] = z;
@@ -438,8 +450,8 @@ __global__ void __launch_bounds__(512) k_ru_apply(DevScal *sc, const double *Rd,
         const float4 r = make_float4(static_cast<float>(a.x), static_cast<float>(a.y), static_cast<float>(b.x),
                                      static_cast<float>(b.y));
         const float4 r0 = reinterpret_cast<const float4 *>(R0_32)[u];
-        acc[0] = dacc(dacc(dacc(dacc(acc[0], r.x, r0.x), r.y, r0.y), r.z, r0.z), r.w, r0.w);
-        acc[1] = dacc(dacc(dacc(dacc(acc[1], r.x, r.x), r.y, r.y), r.z, r.z), r.w, r.w);
+        acc[0] = dunit4(acc[0], r, r0);
+        acc[1] = dunit4(acc[1], r, r);
         reinterpret_cast<float4 *>(R32)[u] = r;
     }
     block_sum<2>(acc, red);

@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cmath>
 #include <numeric>
+#include <queue>
 
 #include "hhp_internal.h"
 
@@ -100,6 +101,57 @@ void build_plan(int m, const int *rowptr, int rpl, int long_thr, int cap, int wi
     P.total = off;
     P.short_nnz = short_nnz;
     P.padding = short_nnz > 0 ? static_cast<double>(off) / static_cast<double>(short_nnz) : 1.0;
+}
+
+void assign_units(const SellHost &P, int n_warps, std::vector<int> &warp_ptr, std::vector<int> &warp_units,
+                  double *imbalance) {
+    // cost of a unit ~ the steps its warp walks: a slice's longest row, a chunk's nonzeros / 32,
+    // plus a fixed cost for loading lengths and writing results
+    const int ns = P.n_slices, nc = static_cast<int>(P.chunks.size()), nu = ns + nc;
+    std::vector<long long> cost(static_cast<size_t>(nu));
+    for (int s = 0; s < ns; ++s) {
+        const long long steps = (P.slice_ptr[static_cast<size_t>(s) + 1] - P.slice_ptr[static_cast<size_t>(s)]) / P.H;
+        cost[static_cast<size_t>(s)] = steps + 4;
+    }
+    for (int c = 0; c < nc; ++c) {
+        const int4 d = P.chunks[static_cast<size_t>(c)];
+        cost[static_cast<size_t>(ns + c)] = (d.w - d.z + 31) / 32 + 8;
+    }
+    // longest processing time first: each unit, largest first (ties by id), goes to the least
+    // loaded warp (ties by warp id); deterministic, and for equal costs it deals round-robin
+    std::vector<int> order(static_cast<size_t>(nu));
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[static_cast<size_t>(a)] > cost[static_cast<size_t>(b)]; });
+    using Load = std::pair<long long, int>;
+    std::priority_queue<Load, std::vector<Load>, std::greater<Load>> heap;
+    for (int w = 0; w < n_warps; ++w) heap.push({0LL, w});
+    std::vector<int> owner(static_cast<size_t>(nu));
+    std::vector<long long> load(static_cast<size_t>(n_warps), 0);
+    for (int u : order) {
+        Load l = heap.top();
+        heap.pop();
+        owner[static_cast<size_t>(u)] = l.second;
+        l.first += cost[static_cast<size_t>(u)];
+        load[static_cast<size_t>(l.second)] = l.first;
+        heap.push(l);
+    }
+    warp_ptr.assign(static_cast<size_t>(n_warps) + 1, 0);
+    for (int u = 0; u < nu; ++u) warp_ptr[static_cast<size_t>(owner[static_cast<size_t>(u)]) + 1]++;
+    for (int w = 0; w < n_warps; ++w) warp_ptr[static_cast<size_t>(w) + 1] += warp_ptr[static_cast<size_t>(w)];
+    warp_units.assign(static_cast<size_t>(nu), 0);
+    std::vector<int> fill(warp_ptr.begin(), warp_ptr.end() - 1);
+    for (int u = 0; u < nu; ++u) {  // ascending unit id within each warp
+        const int w = owner[static_cast<size_t>(u)];
+        warp_units[static_cast<size_t>(fill[static_cast<size_t>(w)]++)] = u;
+    }
+    if (imbalance) {
+        long long tot = 0, mx = 0;
+        for (long long v : load) {
+            tot += v;
+            mx = std::max(mx, v);
+        }
+        *imbalance = tot > 0 ? static_cast<double>(mx) * n_warps / static_cast<double>(tot) : 1.0;
+    }
 }
 
 }  // namespace hhp

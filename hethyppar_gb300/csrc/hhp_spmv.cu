@@ -20,8 +20,9 @@
 //    to the same order computed with fma() on a CPU.
 //  * Long rows (> long_thr nonzeros) are cut into chunks that one warp sums (lane-strided, then a
 //    fixed butterfly); chunk sums are combined in chunk order by the warp finishing a row's last
-//    chunk. Work (slices, then chunks) is dealt to warps round-robin, so every reduction has a
-//    fixed order and results are reproducible run to run.
+//    chunk. Work units (slices and chunks) are dealt to warps at plan time, longest first to the
+//    least-loaded warp, so power-law matrices stay balanced; every warp walks a fixed list, so
+//    every reduction has a fixed order and results are reproducible run to run.
 //  * Epilogues fuse the BiCGStab dot products (r0.v, t.s, t.t) and the residual r = b - A x into
 //    the store of y; one partial per CTA, summed in a fixed order by the consumer.
 #include <algorithm>
@@ -56,6 +57,8 @@ struct SellArgs {
     const long long *slice_ptr;
     const int *pos_row;
     const int *pos_len;
+    const int *warp_ptr;
+    const int *warp_units;
     const VT *sval;
     const int *scol;
     const VT *csr_val;  // CSR values (FP64, or the FP32 copy) for long-row chunks
@@ -86,9 +89,10 @@ __device__ __forceinline__ T comp(const V &v, int t) {
     return reinterpret_cast<const T *>(&v)[t];
 }
 
-// Row epilogue: stores y[r]; accumulates dot partials into (d0, d1).
-template <typename VT, int EP>
-__device__ __forceinline__ void row_epilogue(const SellArgs<VT> &a, int r, VT acc, double &d0, double &d1) {
+// Row epilogue: stores y[r]; accumulates dot partials into (d0, d1), in the value type (the
+// caller folds them into FP64 once per slice for FP32 data).
+template <typename VT, int EP, typename DT>
+__device__ __forceinline__ void row_epilogue(const SellArgs<VT> &a, int r, VT acc, DT &d0, DT &d1) {
     if (EP == EP_AXPBY) {
         VT out = acc;
         if (a.scale) out = static_cast<VT>(a.alpha) * out;  // integer flags: no FP64 compares per row
@@ -96,17 +100,17 @@ __device__ __forceinline__ void row_epilogue(const SellArgs<VT> &a, int r, VT ac
         a.y[r] = out;
     } else if (EP == EP_DOT1) {
         a.y[r] = acc;
-        d0 += static_cast<double>(acc * __ldg(a.w1 + r));
+        d0 = vfma(static_cast<DT>(acc), static_cast<DT>(__ldg(a.w1 + r)), d0);
     } else if (EP == EP_DOT2) {
         a.y[r] = acc;
-        d0 += static_cast<double>(acc * __ldg(a.w1 + r));
-        d1 += static_cast<double>(acc * acc);
+        d0 = vfma(static_cast<DT>(acc), static_cast<DT>(__ldg(a.w1 + r)), d0);
+        d1 = vfma(static_cast<DT>(acc), static_cast<DT>(acc), d1);
     } else {  // EP_RESID
         const VT b = __ldg(a.w1 + r);
         const VT res = b - acc;
         a.y[r] = res;
-        d0 += static_cast<double>(res * res);
-        d1 += static_cast<double>(b * b);
+        d0 = vfma(static_cast<DT>(res), static_cast<DT>(res), d0);
+        d1 = vfma(static_cast<DT>(b), static_cast<DT>(b), d1);
     }
 }
 
@@ -166,11 +170,16 @@ __device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, int lane,
             c[u] = cn[u];
         }
     }
+    VT e0 = VT(0), e1 = VT(0);
 #pragma unroll
     for (int t = 0; t < R; ++t) {
         const int p = q0 + t;
         const int r = a.has_perm ? a.pos_row[p] : p;
-        if (r >= 0 && r < a.m) row_epilogue<VT, EP>(a, r, acc[t], d0, d1);
+        if (r >= 0 && r < a.m) row_epilogue<VT, EP>(a, r, acc[t], e0, e1);
+    }
+    if (EP != EP_AXPBY) {
+        d0 += static_cast<double>(e0);
+        d1 += static_cast<double>(e1);
     }
 }
 
@@ -207,7 +216,7 @@ __device__ __forceinline__ void do_chunk(const SellArgs<VT> &a, int c, int lane)
             for (int q = 0; q < nch; ++q) tot += __ldcg(a.chunk_part + c_first + q);
             a.long_cnt[l] = 0u;  // ready for the next launch
             double e0 = 0.0, e1 = 0.0;
-            row_epilogue<VT, EP>(a, d.x, static_cast<VT>(tot), e0, e1);
+            row_epilogue<VT, EP, double>(a, d.x, static_cast<VT>(tot), e0, e1);
             if (EP != EP_AXPBY) {
                 a.long_dot[2 * l] = e0;
                 a.long_dot[2 * l + 1] = e1;
@@ -223,10 +232,12 @@ __global__ void __launch_bounds__(256, 3) k_spmv(const SellArgs<VT> a) {
     if (a.gate && *a.gate == 0) return;
     __shared__ double red[32 * 2];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int gw = blockIdx.x * nw + warp, W = gridDim.x * nw;
+    const int gw = blockIdx.x * nw + warp;
     double d0 = 0.0, d1 = 0.0;
-    const int units = a.n_slices + a.n_chunks;
-    for (int u = gw; u < units; u += W) {
+    // this warp's units, balanced at plan time (fixed order: reductions are reproducible)
+    const int ub = a.warp_ptr[gw], ue = a.warp_ptr[gw + 1];
+    for (int i = ub; i < ue; ++i) {
+        const int u = __ldg(a.warp_units + i);
         if (u < a.n_slices) do_slice<VT, EP>(a, u, lane, d0, d1);
         else do_chunk<VT, EP>(a, u - a.n_slices, lane);
     }
@@ -322,6 +333,10 @@ hhp_status build_plan_dev(hhp_mat *A, PlanDev &p) {
     p.padding = h.padding;
     p.warps_per_cta = std::min(std::max(t.wpc, 1), 8);
     p.ctas = ctx->num_sms * std::min(std::max(t.ctas_per_sm, 1), 8);
+    std::vector<int> wptr, wunits;
+    assign_units(h, p.ctas * p.warps_per_cta, wptr, wunits, &p.imbalance);
+    HHP_TRY(upload(&p.warp_ptr, wptr));
+    HHP_TRY(upload(&p.warp_units, wunits));
     HHP_TRY(upload(&p.slice_ptr, h.slice_ptr));
     HHP_TRY(upload(&p.pos_row, h.pos_row, 4));
     HHP_TRY(upload(&p.pos_len, h.pos_len, 4));
@@ -352,6 +367,8 @@ SellArgs<VT> make_args(hhp_mat *A, const PlanDev &p, const VT *csr_val, const VT
     a.slice_ptr = p.slice_ptr;
     a.pos_row = p.pos_row;
     a.pos_len = p.pos_len;
+    a.warp_ptr = p.warp_ptr;
+    a.warp_units = p.warp_units;
     a.sval = static_cast<const VT *>(p.sval);
     a.scol = p.scol;
     a.csr_val = csr_val;
@@ -385,6 +402,8 @@ void PlanDev::release() {
     cudaFree(slice_ptr);
     cudaFree(pos_row);
     cudaFree(pos_len);
+    cudaFree(warp_ptr);
+    cudaFree(warp_units);
     cudaFree(sval);
     cudaFree(scol);
     cudaFree(chunks);
