@@ -208,7 +208,7 @@ def run_ours(args, rk):
     launches0 = ctx.kernel_launches
     dist.barrier(rk)
     torch.cuda.synchronize()
-    step_ms = []
+    step_ms, lib_ms = [], []
     for _ in range(args.steps):
         x_d.zero_()
         flush_l2()
@@ -218,6 +218,7 @@ def run_ours(args, rk):
         e1.record(stream)
         e1.synchronize()
         step_ms.append(e0.elapsed_time(e1))
+        lib_ms.append(res.t_solve_s * 1e3)
     torch.cuda.synchronize()
     dist.barrier(rk)
     launches = ctx.kernel_launches - launches0
@@ -277,6 +278,8 @@ def run_ours(args, rk):
                       "l2": "flushed before every timed step (256 MiB write, then 256 MiB read)",
                       "parallelism": f"replicas x{rk.world}" if rk.world > 1 else "single GPU"},
            "iters": res.iters, "iters_per_s": res.iters / (statistics.mean(step_ms) / 1e3),
+           "us_per_iter": statistics.mean(step_ms) * 1e3 / max(res.iters, 1),
+           "solve_graph_ms": statistics.mean(lib_ms),
            "rel_res_true": res.rel_res_true, "err_vs_target": res.err_vs_target,
            "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": 2 * 8 * s.n, "d2h_bytes_per_step": 8 * s.n},
            "roofline": roof,
