@@ -100,78 +100,79 @@ __device__ __forceinline__ float warp_sum(float v) {
     return v;
 }
 
-// Block-wide sum of NC values per thread; result valid in thread 0 of the block. Warp sums are
-// combined in warp order by thread 0, so the result does not depend on scheduling.
+// Block-wide sum of NC values per thread; result valid in thread 0 of the block. Every thread
+// parks its values in shared memory and warp 0 alone adds them (lane l: threads l, l+32, ... in
+// order, then a butterfly), so the FP64 work is ~blockDim adds rather than a butterfly in every
+// warp. Fixed order: the result does not depend on scheduling. scratch: blockDim.x * NC doubles.
 template <int NC>
-__device__ __forceinline__ void block_sum(double (&v)[NC], double *scratch /* >= 32*NC doubles */) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+__device__ __forceinline__ void block_sum(double (&v)[NC], double *scratch) {
+    const int t = threadIdx.x, T = blockDim.x;
 #pragma unroll
-    for (int c = 0; c < NC; ++c) v[c] = warp_sum(v[c]);
-    if (lane == 0) {
-#pragma unroll
-        for (int c = 0; c < NC; ++c) scratch[warp * NC + c] = v[c];
-    }
+    for (int c = 0; c < NC; ++c) scratch[c * T + t] = v[c];
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (t < 32) {
+        double s[NC];
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
-            double s = 0.0;
-            for (int w = 0; w < nw; ++w) s += scratch[w * NC + c];
-            v[c] = s;
+            s[c] = 0.0;
+            for (int i = t; i < T; i += 32) s[c] += scratch[c * T + i];
+            s[c] = warp_sum(s[c]);
+        }
+        if (t == 0) {
+#pragma unroll
+            for (int c = 0; c < NC; ++c) v[c] = s[c];
         }
     }
     __syncthreads();
 }
 
+// Shared-memory doubles a kernel provides to reduce_partials (records are staged in chunks).
+constexpr int kRedScratch = 2048;
+
 // Sum of per-block partials part[i*NC + c] for i in [0, n), plus extra[j*NC + c] for j in
-// [0, n_extra), computed identically by every calling block: every thread first loads its
-// share (thread t takes entries t, t + blockDim.x, ...; all loads are issued before any add,
-// so the whole reduction costs one memory round trip), then a warp butterfly and a sum of the
-// warp results in warp order. The order is fixed, so every block gets the same bits. Must be
-// called by all threads; the result is returned to every thread. Loads use ld.global.cg so values
-// written by earlier kernels are read from L2.
+// [0, n_extra), computed identically by every calling block. Records are staged through shared
+// memory in chunks of kRedScratch/NC: all threads load a chunk at once (one memory round trip per
+// chunk), then warp 0 alone adds it (lane l: records l, l+32, ... in order, continuing its running
+// sums), and a final butterfly combines the lanes. Only warp 0 does FP64 adds, keeping the FP64
+// work per block near the record count (the FP64 pipe is GB300's scarcest unit). The order is
+// fixed, so every block gets the same bits. Must be called by all threads; the result is
+// returned to every thread. Loads use ld.global.cg (values written by earlier kernels).
 template <int NC>
 __device__ __forceinline__ void reduce_partials(const double *__restrict__ part, int n,
                                                 const double *__restrict__ extra, int n_extra,
-                                                double (&out)[NC], double *scratch /* >= 32*NC doubles */) {
+                                                double (&out)[NC], double *scratch /* kRedScratch */) {
+    const int T = blockDim.x, t = threadIdx.x;
+    constexpr int kRec = kRedScratch / NC;
+    const int tot = n + n_extra;
     double s[NC];
 #pragma unroll
     for (int c = 0; c < NC; ++c) s[c] = 0.0;
-    const int T = blockDim.x, t = threadIdx.x;
-    double a[2][NC], b[2][NC];
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-        const int i = t + q * T;
-#pragma unroll
-        for (int c = 0; c < NC; ++c) {
-            a[q][c] = i < n ? __ldcg(part + (size_t)i * NC + c) : 0.0;
-            b[q][c] = i < n_extra ? __ldcg(extra + (size_t)i * NC + c) : 0.0;
+    for (int r0 = 0; r0 < tot; r0 += kRec) {
+        const int cnt = min(kRec, tot - r0);
+        for (int i = t; i < cnt * NC; i += T) {
+            const int g = r0 * NC + i;
+            scratch[i] = g < n * NC ? __ldcg(part + g) : __ldcg(extra + (g - n * NC));
         }
+        __syncthreads();
+        if (t < 32) {
+            for (int i = t; i < cnt; i += 32) {
+#pragma unroll
+                for (int c = 0; c < NC; ++c) s[c] += scratch[i * NC + c];
+            }
+        }
+        __syncthreads();
     }
+    if (t < 32) {
 #pragma unroll
-    for (int c = 0; c < NC; ++c) s[c] = (a[0][c] + a[1][c]) + (b[0][c] + b[1][c]);
-    for (int i = t + 2 * T; i < n; i += T) {  // only for more than 2*blockDim partials
+        for (int c = 0; c < NC; ++c) s[c] = warp_sum(s[c]);
+        if (t == 0) {
 #pragma unroll
-        for (int c = 0; c < NC; ++c) s[c] += __ldcg(part + (size_t)i * NC + c);
-    }
-    for (int i = t + 2 * T; i < n_extra; i += T) {
-#pragma unroll
-        for (int c = 0; c < NC; ++c) s[c] += __ldcg(extra + (size_t)i * NC + c);
-    }
-    const int lane = t & 31, warp = t >> 5, nw = (T + 31) >> 5;
-#pragma unroll
-    for (int c = 0; c < NC; ++c) s[c] = warp_sum(s[c]);
-    if (lane == 0) {
-#pragma unroll
-        for (int c = 0; c < NC; ++c) scratch[warp * NC + c] = s[c];
+            for (int c = 0; c < NC; ++c) scratch[c] = s[c];
+        }
     }
     __syncthreads();
 #pragma unroll
-    for (int c = 0; c < NC; ++c) {
-        double v = 0.0;
-        for (int w = 0; w < nw; ++w) v += scratch[w * NC + c];
-        out[c] = v;
-    }
+    for (int c = 0; c < NC; ++c) out[c] = scratch[c];
     __syncthreads();
 }
 

@@ -137,7 +137,7 @@ struct SpmvParts {
 template <typename T>
 __global__ void __launch_bounds__(512) k_init(DevScal *sc, const T *R, T *R0, T *P, T *V, int nu, SpmvParts sp,
                                               double *part_xr, double *part_s) {
-    __shared__ double red[64];
+    __shared__ double red[kRedScratch];
     double v[2];
     reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
     const double rr = v[0], bb = v[1];
@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
                                            const double *part_s, int nparts, double *hist, int hist_cap,
                                            cudaGraphConditionalHandle cond, int first_in_body, const int *dev_err,
                                            int use_cond) {
-    __shared__ double red[64];
+    __shared__ double red[kRedScratch];
     double v[2], w[2];
     reduce_partials<2>(part_xr, nparts, nullptr, 0, v, red);
     reduce_partials<2>(part_s, nparts, nullptr, 0, w, red);
@@ -236,7 +236,7 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
 template <typename T>
 __global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const T *V, int nu, SpmvParts sp,
                                            double *part_s) {
-    __shared__ double red[64];
+    __shared__ double red[kRedScratch];
     double v[2];
     reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
     if (sc->status != ST_RUNNING) return;
@@ -276,7 +276,7 @@ template <typename T>
 __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P, const T *S, const T *Tv,
                                             const T *R0, int nu, SpmvParts sp, const double *part_s, int nparts,
                                             double *part_xr) {
-    __shared__ double red[64];
+    __shared__ double red[kRedScratch];
     double v[2], w[2];
     reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
     reduce_partials<2>(part_s, nparts, nullptr, 0, w, red);
@@ -331,7 +331,7 @@ __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P,
 
 // Final true residual (SpMV EP_RESID into Y already done): ||b - A x||^2, ||b||^2.
 __global__ void k_finish(DevScal *sc, SpmvParts sp) {
-    __shared__ double red[64];
+    __shared__ double red[kRedScratch];
     double v[2];
     reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
     if (threadIdx.x == 0) {
@@ -354,7 +354,7 @@ __global__ void k_finish(DevScal *sc, SpmvParts sp) {
 __global__ void __launch_bounds__(512) k_mix_init(DevScal *sc, const double *Rd, float *R32, float *R0_32,
                                                   float *D32, float *P32, float *V32, int nu4, SpmvParts sp,
                                                   double *part_xr32, double *part_s32) {
-    __shared__ double red[64];
+    __shared__ double red[kRedScratch];
     double v[2];
     reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
     const double rd2 = v[0], bb = v[1];
@@ -403,7 +403,7 @@ __global__ void __launch_bounds__(512) k_mix_init(DevScal *sc, const double *Rd,
 // After K_XR: decide whether this iteration ends with an FP64 update; if so x += d, d = 0.
 __global__ void __launch_bounds__(512) k_ru_check(DevScal *sc, double *X, float *D32, int nu4,
                                                   const double *part_xr32, int nparts) {
-    __shared__ double red[64];
+    __shared__ double red[kRedScratch];
     double v[2];
     reduce_partials<2>(part_xr32, nparts, nullptr, 0, v, red);
     if (sc->status != ST_RUNNING) {
@@ -438,7 +438,7 @@ __global__ void __launch_bounds__(512) k_ru_check(DevScal *sc, double *X, float 
 // test convergence on the FP64 true residual.
 __global__ void __launch_bounds__(512) k_ru_apply(DevScal *sc, const double *Rd, float *R32, const float *R0_32,
                                                   int nu4, SpmvParts sp, double *part_xr32) {
-    __shared__ double red[64];
+    __shared__ double red[kRedScratch];
     if (!sc->ru_flag) return;
     double v[2];
     reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);

@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(256, 3) k_spmv(const SellArgs<VT> a) {
     // After a recorded device error every later launch returns at once (uniform across the grid).
     if (*reinterpret_cast<volatile const int *>(a.err) != DEV_OK) return;
     if (a.gate && *a.gate == 0) return;
-    __shared__ double red[32 * 2];
+    __shared__ double red[2 * 256];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int gw = blockIdx.x * nw + warp;
     double d0 = 0.0, d1 = 0.0;
@@ -242,21 +242,24 @@ __global__ void __launch_bounds__(256, 3) k_spmv(const SellArgs<VT> a) {
         else do_chunk<VT, EP>(a, u - a.n_slices, lane);
     }
     if (EP != EP_AXPBY) {
-        d0 = warp_sum(d0);
-        d1 = warp_sum(d1);
-        if (lane == 0) {
-            red[2 * warp] = d0;
-            red[2 * warp + 1] = d1;
-        }
+        // per-CTA partial: lanes park their sums in shared memory, warp 0 adds them in thread
+        // order (fixed, and only one warp spends FP64 adds on it)
+        const int T = blockDim.x, t = threadIdx.x;
+        red[t] = d0;
+        red[T + t] = d1;
         __syncthreads();
-        if (threadIdx.x == 0) {
+        if (t < 32) {
             double s0 = 0.0, s1 = 0.0;
-            for (int w = 0; w < nw; ++w) {
-                s0 += red[2 * w];
-                s1 += red[2 * w + 1];
+            for (int i = t; i < T; i += 32) {
+                s0 += red[i];
+                s1 += red[T + i];
             }
-            a.cta_part[2 * blockIdx.x] = s0;
-            a.cta_part[2 * blockIdx.x + 1] = s1;
+            s0 = warp_sum(s0);
+            s1 = warp_sum(s1);
+            if (t == 0) {
+                a.cta_part[2 * blockIdx.x] = s0;
+                a.cta_part[2 * blockIdx.x + 1] = s1;
+            }
         }
     }
 }
