@@ -176,6 +176,65 @@ __device__ __forceinline__ void reduce_partials(const double *__restrict__ part,
     __syncthreads();
 }
 
+// Two independent reductions (A = part_a + extra_a, B = part_b) staged together, so they cost
+// one memory round trip and one pass of warp 0 instead of two. Same order guarantees as
+// reduce_partials.
+template <int NC>
+__device__ __forceinline__ void reduce_pair(const double *__restrict__ part_a, int na, const double *__restrict__ extra_a,
+                                            int nea, const double *__restrict__ part_b, int nb, double (&out_a)[NC],
+                                            double (&out_b)[NC], double *scratch /* kRedScratch */) {
+    const int T = blockDim.x, t = threadIdx.x;
+    constexpr int kRec = kRedScratch / NC;
+    const int ta = na + nea, tot = ta + nb;
+    double sa[NC], sb[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) sa[c] = sb[c] = 0.0;
+    for (int r0 = 0; r0 < tot; r0 += kRec) {
+        const int cnt = min(kRec, tot - r0);
+        for (int i = t; i < cnt * NC; i += T) {
+            const int g = r0 * NC + i;
+            double v;
+            if (g < na * NC) v = __ldcg(part_a + g);
+            else if (g < ta * NC) v = __ldcg(extra_a + (g - na * NC));
+            else v = __ldcg(part_b + (g - ta * NC));
+            scratch[i] = v;
+        }
+        __syncthreads();
+        if (t < 32) {
+            for (int i = t; i < cnt; i += 32) {
+                const bool in_a = r0 + i < ta;
+#pragma unroll
+                for (int c = 0; c < NC; ++c) {
+                    if (in_a) sa[c] += scratch[i * NC + c];
+                    else sb[c] += scratch[i * NC + c];
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (t < 32) {
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            sa[c] = warp_sum(sa[c]);
+            sb[c] = warp_sum(sb[c]);
+        }
+        if (t == 0) {
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                scratch[c] = sa[c];
+                scratch[NC + c] = sb[c];
+            }
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+        out_a[c] = scratch[c];
+        out_b[c] = scratch[NC + c];
+    }
+    __syncthreads();
+}
+
 __device__ __forceinline__ bool finite_nonzero(double v) { return isfinite(v) && v != 0.0; }
 
 }  // namespace hhp

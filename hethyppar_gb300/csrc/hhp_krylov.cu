@@ -179,6 +179,10 @@ __global__ void __launch_bounds__(512) k_init(DevScal *sc, const T *R, T *R0, T 
     }
 }
 
+// Scalar work (divisions, tests) is done once per block by thread 0 and broadcast through shared
+// memory: on GB300 an FP64 division is a sequence of FP64 instructions on the slowest pipe, so
+// evaluating the scalar recurrence in every thread would cost more than the vector update.
+
 // K_P: convergence test on the previous step, beta, p = r + beta (p - omega v).
 template <typename T>
 __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const T *R, int nu, const double *part_xr,
@@ -186,40 +190,50 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
                                            cudaGraphConditionalHandle cond, int first_in_body, const int *dev_err,
                                            int use_cond) {
     __shared__ double red[kRedScratch];
+    __shared__ double bc[2];
+    __shared__ int go;
     double v[2], w[2];
-    reduce_partials<2>(part_xr, nparts, nullptr, 0, v, red);
-    reduce_partials<2>(part_s, nparts, nullptr, 0, w, red);
-    const double rho_new = v[0], rr = v[1], ss = w[0];
-    const int st = sc->status;
-    if (st != ST_RUNNING) {
-        if (b0t0() && use_cond) cudaGraphSetConditional(cond, 0);
-        return;
-    }
-    if (b0t0() && first_in_body) sc->bodies += 1;
-    const int iter = sc->iter, it0 = sc->iter_start;
-    const double thr2 = sc->thr2_rec;
-    if (b0t0() && iter > it0 && iter - 1 < hist_cap) hist[iter - 1] = sc->hist_scale * sqrt(rr / sc->rr0);
-    int term = ST_RUNNING;
-    if (*reinterpret_cast<volatile const int *>(dev_err) != DEV_OK) term = ST_DEVICE_ERROR;
-    else if (thr2 >= 0.0 && iter > it0 && ss <= thr2) term = ST_CONVERGED_HALF;
-    else if (thr2 >= 0.0 && rr <= thr2) term = ST_CONVERGED;
-    else if (iter >= sc->maxit) term = ST_MAXIT;
-    else if (!finite_nonzero(rho_new) || !isfinite(rr)) term = ST_BREAKDOWN;
-    if (term != ST_RUNNING) {
-        if (b0t0()) {
-            sc->status = term;
-            sc->rr_last = rr;
-            if (use_cond) cudaGraphSetConditional(cond, 0);
+    reduce_pair<2>(part_xr, nparts, nullptr, 0, part_s, nparts, v, w, red);
+    if (threadIdx.x == 0) {
+        const double rho_new = v[0], rr = v[1], ss = w[0];
+        const bool lead = blockIdx.x == 0;
+        const int st = sc->status;
+        int term = ST_RUNNING;
+        if (st != ST_RUNNING) {
+            if (lead && use_cond) cudaGraphSetConditional(cond, 0);
+            term = st;
+        } else {
+            if (lead && first_in_body) sc->bodies += 1;
+            const int iter = sc->iter, it0 = sc->iter_start;
+            const double thr2 = sc->thr2_rec;
+            if (lead && iter > it0 && iter - 1 < hist_cap) hist[iter - 1] = sc->hist_scale * sqrt(rr / sc->rr0);
+            if (*reinterpret_cast<volatile const int *>(dev_err) != DEV_OK) term = ST_DEVICE_ERROR;
+            else if (thr2 >= 0.0 && iter > it0 && ss <= thr2) term = ST_CONVERGED_HALF;
+            else if (thr2 >= 0.0 && rr <= thr2) term = ST_CONVERGED;
+            else if (iter >= sc->maxit) term = ST_MAXIT;
+            else if (!finite_nonzero(rho_new) || !isfinite(rr)) term = ST_BREAKDOWN;
+            if (term != ST_RUNNING) {
+                if (lead) {
+                    sc->status = term;
+                    sc->rr_last = rr;
+                    if (use_cond) cudaGraphSetConditional(cond, 0);
+                }
+            } else {
+                const double beta = (rho_new / sc->rho_prev) * (sc->alpha / sc->omega);
+                bc[0] = beta;
+                bc[1] = -sc->omega;
+                if (lead) {
+                    sc->rho_cur = rho_new;
+                    sc->beta = beta;
+                    sc->rr_last = rr;
+                }
+            }
         }
-        return;
+        go = term == ST_RUNNING;
     }
-    const double beta = (rho_new / sc->rho_prev) * (sc->alpha / sc->omega);
-    if (b0t0()) {
-        sc->rho_cur = rho_new;
-        sc->beta = beta;
-        sc->rr_last = rr;
-    }
-    const T tb = static_cast<T>(beta), tw = static_cast<T>(-sc->omega);
+    __syncthreads();
+    if (!go) return;
+    const T tb = static_cast<T>(bc[0]), tw = static_cast<T>(bc[1]);
     constexpr int E = Unit<T>::E;
     for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += gridDim.x * blockDim.x) {
         T p[E], vv[E], r[E];
@@ -237,21 +251,32 @@ template <typename T>
 __global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const T *V, int nu, SpmvParts sp,
                                            double *part_s) {
     __shared__ double red[kRedScratch];
+    __shared__ double bc[1];
+    __shared__ int go;
     double v[2];
     reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
-    if (sc->status != ST_RUNNING) return;
-    const double rv = v[0];
-    const double alpha = sc->rho_cur / rv;
-    if (!finite_nonzero(rv) || !isfinite(alpha)) {
-        if (b0t0()) sc->status = ST_BREAKDOWN;
-        return;
+    if (threadIdx.x == 0) {
+        int ok = sc->status == ST_RUNNING;
+        if (ok) {
+            const double rv = v[0];
+            const double alpha = sc->rho_cur / rv;
+            if (!finite_nonzero(rv) || !isfinite(alpha)) {
+                if (blockIdx.x == 0) sc->status = ST_BREAKDOWN;
+                ok = 0;
+            } else {
+                bc[0] = -alpha;
+                if (blockIdx.x == 0) {
+                    sc->alpha = alpha;
+                    sc->rho_prev = sc->rho_cur;
+                    sc->iter = sc->iter + 1;
+                }
+            }
+        }
+        go = ok;
     }
-    if (b0t0()) {
-        sc->alpha = alpha;
-        sc->rho_prev = sc->rho_cur;
-        sc->iter = sc->iter + 1;
-    }
-    const T ta = static_cast<T>(-alpha);
+    __syncthreads();
+    if (!go) return;
+    const T ta = static_cast<T>(bc[0]);
     constexpr int E = Unit<T>::E;
     double acc[1] = {0.0};
     for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += gridDim.x * blockDim.x) {
@@ -277,23 +302,36 @@ __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P,
                                             const T *R0, int nu, SpmvParts sp, const double *part_s, int nparts,
                                             double *part_xr) {
     __shared__ double red[kRedScratch];
+    __shared__ double bc[2];
+    __shared__ int go, hf;
     double v[2], w[2];
-    reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
-    reduce_partials<2>(part_s, nparts, nullptr, 0, w, red);
-    if (sc->status != ST_RUNNING) return;
-    const double thr2 = sc->thr2_rec;
-    const bool half = thr2 >= 0.0 && w[0] <= thr2;
-    const double alpha = sc->alpha;
-    double omega = 0.0;
-    if (!half) {
-        omega = v[0] / v[1];
-        if (!finite_nonzero(v[1]) || !isfinite(omega)) {
-            if (b0t0()) sc->status = ST_BREAKDOWN;
-            return;
+    reduce_pair<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, part_s, nparts, v, w, red);
+    if (threadIdx.x == 0) {
+        int ok = sc->status == ST_RUNNING;
+        int half = 0;
+        if (ok) {
+            const double thr2 = sc->thr2_rec;
+            half = thr2 >= 0.0 && w[0] <= thr2;
+            bc[0] = sc->alpha;
+            bc[1] = 0.0;
+            if (!half) {
+                const double omega = v[0] / v[1];
+                if (!finite_nonzero(v[1]) || !isfinite(omega)) {
+                    if (blockIdx.x == 0) sc->status = ST_BREAKDOWN;
+                    ok = 0;
+                } else {
+                    bc[1] = omega;
+                    if (blockIdx.x == 0) sc->omega = omega;
+                }
+            }
         }
-        if (b0t0()) sc->omega = omega;
+        go = ok;
+        hf = half;
     }
-    const T ta = static_cast<T>(alpha), tw = static_cast<T>(omega), tnw = static_cast<T>(-omega);
+    __syncthreads();
+    if (!go) return;
+    const bool half = hf != 0;
+    const T ta = static_cast<T>(bc[0]), tw = static_cast<T>(bc[1]), tnw = static_cast<T>(-bc[1]);
     constexpr int E = Unit<T>::E;
     double acc[2] = {0.0, 0.0};
     for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += gridDim.x * blockDim.x) {
@@ -404,21 +442,23 @@ __global__ void __launch_bounds__(512) k_mix_init(DevScal *sc, const double *Rd,
 __global__ void __launch_bounds__(512) k_ru_check(DevScal *sc, double *X, float *D32, int nu4,
                                                   const double *part_xr32, int nparts) {
     __shared__ double red[kRedScratch];
+    __shared__ int go;
     double v[2];
     reduce_partials<2>(part_xr32, nparts, nullptr, 0, v, red);
-    if (sc->status != ST_RUNNING) {
-        if (b0t0()) sc->ru_flag = 0;
-        return;
+    if (threadIdx.x == 0) {
+        int update = 0;
+        if (sc->status == ST_RUNNING) {
+            const double rr = v[1];
+            const int it = sc->iter;
+            const double mx = sc->rr_max[it & 1];
+            update = rr <= sc->thr2 || rr < sc->inner_rtol2 * mx || it >= sc->maxit || !isfinite(rr);
+            if (blockIdx.x == 0) sc->rr_max[(it + 1) & 1] = update ? mx : fmax(mx, rr);
+        }
+        if (blockIdx.x == 0) sc->ru_flag = update;
+        go = update;
     }
-    const double rr = v[1];
-    const int it = sc->iter;
-    const double mx = sc->rr_max[it & 1];
-    const bool update = rr <= sc->thr2 || rr < sc->inner_rtol2 * mx || it >= sc->maxit || !isfinite(rr);
-    if (b0t0()) {
-        sc->rr_max[(it + 1) & 1] = update ? mx : fmax(mx, rr);
-        sc->ru_flag = update ? 1 : 0;
-    }
-    if (!update) return;
+    __syncthreads();
+    if (!go) return;
     const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu4; u += gridDim.x * blockDim.x) {
         const float4 d = reinterpret_cast<const float4 *>(D32)[u];
