@@ -94,6 +94,7 @@ SIGNATURES = [
     ("hhp_dp_update_beta", None, [_P, _P, _P, _P, _P, _P]),
     ("hhp_dp_update_alpha", None, [_P, _P, _P, _P, _P]),
     ("hhp_dp_update_omega", None, [_P, _P, _P, _P, _P]),
+    ("hhp_spmv_csr_noalloc", _I, [_I, _I, _I, _P, _P, _P, _D, _P, _D, _P, _P]),
 ]
 
 _lib = None

@@ -182,6 +182,22 @@ void hhp_dp_update_beta(double *beta, double *rho_old, const double *rho_new, co
 void hhp_dp_update_alpha(double *alpha, double *neg_alpha, const double *rho, const double *rv, void *s);
 void hhp_dp_update_omega(double *omega, double *neg_omega, const double *ts, const double *tt, void *s);
 
+/* ---- allocation-free SpMV (no counterpart in the reference) -------------------------------------
+ * y = alpha*A*x + beta*y straight from caller-owned device CSR arrays (rowptr m+1, col nnz, val nnz
+ * FP64; x n, y m), with no context, no matrix object and no device allocation. For callers that
+ * must not call cudaMalloc: a host application that owns and pre-sizes all device memory, or code
+ * between stream operations where cudaMalloc's implicit device synchronisation is not allowed.
+ * Work is split evenly over rows plus nonzeros; the only scratch, one partial sum per CTA for rows
+ * split between CTAs, is a 48 KB array built into the library (held on every GPU that loads it).
+ * Limit: m + nnz <= 2^28, else HHP_ERR_ARG. Runs on `stream` (a cudaStream_t; NULL = default
+ * stream) of the current device. The first call on a device looks up the scratch array's address
+ * there: make it before any stream capture. Calls share that array, so calls that overlap on one
+ * GPU race and give wrong results; serialise them. Rows split between CTAs are summed in another
+ * order than hhp_spmv_dev, so results agree to rounding, not bit for bit. */
+hhp_status hhp_spmv_csr_noalloc(int m, int n, int nnz, const int *rowptr_dev, const int *col_dev,
+                                const double *val_dev, double alpha, const double *x_dev, double beta,
+                                double *y_dev, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
