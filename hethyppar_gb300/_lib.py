@@ -47,6 +47,7 @@ class SolveInfo(ctypes.Structure):
         ("err_vs_target", ctypes.c_double),
         ("t_solve_s", ctypes.c_double),
         ("status", ctypes.c_int),
+        ("fp64_fallback", ctypes.c_int),
     ]
 
 

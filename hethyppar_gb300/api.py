@@ -185,6 +185,7 @@ class SolveResult:
     err_vs_target: float
     t_solve_s: float
     status: int
+    fp64_fallback: bool = False  # mixed: finished in FP64 after the FP32 recurrences failed
     history: List[float] = field(default_factory=list)
 
     @property
@@ -238,7 +239,7 @@ def bicgstab(ctx: Context, A: Matrix, b, x=None, x_target=None, *, rtol: float =
         st = lib().hhp_bicgstab(ctx.handle, A.handle, _ptr(bv), _ptr(out), _ptr(xt), ctypes.byref(o),
                                 ctypes.byref(info))
     res = SolveResult(info.iters, info.outer_iters, bool(info.half_step), info.rel_res_true, info.rel_res_recursive,
-                      info.err_vs_target, info.t_solve_s, st, hist)
+                      info.err_vs_target, info.t_solve_s, st, bool(info.fp64_fallback), hist)
     if raise_on_error and st not in (0, 6):  # MAXIT is reported in the result, not raised
         raise HHPError(st, "bicgstab")
     return out, res
@@ -262,7 +263,7 @@ def bicgstab_backward(ctx: Context, A: Matrix, x, dldx, *, rtol: float = 1e-12, 
         st = lib().hhp_bicgstab_backward(ctx.handle, A.handle, _ptr(xv), _ptr(gv), _ptr(dldb), _ptr(dlda),
                                          ctypes.byref(o), ctypes.byref(info))
     res = SolveResult(info.iters, info.outer_iters, bool(info.half_step), info.rel_res_true, info.rel_res_recursive,
-                      info.err_vs_target, info.t_solve_s, st)
+                      info.err_vs_target, info.t_solve_s, st, bool(info.fp64_fallback))
     if st not in (0, 6):
         raise HHPError(st, "bicgstab_backward")
     return dldb, dlda, res

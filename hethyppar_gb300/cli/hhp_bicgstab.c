@@ -213,7 +213,7 @@ int main(int argc, char **argv) {
     printf("iterations_to_tol : %d\n", (st == HHP_OK && !a.fixed) ? info.iters : -1);
     if (XT) printf("err_vs_target : %E\n", info.err_vs_target);
     printf("outer_iters : %d\n", info.outer_iters);
-    printf("precision : %s\n", a.mixed ? "mixed" : "fp64");
+    printf("precision : %s\n", a.mixed ? (info.fp64_fallback ? "mixed (finished in fp64)" : "mixed") : "fp64");
     printf("status : %s\n", hhp_status_str(st));
     printf("everything_total : %lf\n", now_s() - t_begin);
     printf("\n----------------------------------------------------------------------\n");

@@ -48,6 +48,9 @@ const Tuning &tuning() {
         d.ctas_per_sm = env_int("HHP_SPMV_CPS", d.ctas_per_sm);
         d.vec_blocks_per_sm = env_int("HHP_VEC_BLOCKS_PER_SM", d.vec_blocks_per_sm);
         d.unroll_iters = env_int("HHP_UNROLL_ITERS", d.unroll_iters);
+        d.spmv_unroll = env_int("HHP_SPMV_UNROLL", d.spmv_unroll);
+        d.rpl64 = env_int("HHP_SPMV_RPL64", d.rpl64);
+        d.rpl32 = env_int("HHP_SPMV_RPL32", d.rpl32);
         return d;
     }();
     return t;
@@ -426,7 +429,7 @@ static hhp_solve_opts default_opts() {
     o.rtol = 1e-10;
     o.maxit = 2000;
     o.precision = HHP_PREC_FP64;
-    o.inner_rtol = 1e-5;
+    o.inner_rtol = 0.1;
     o.max_outer = 50;
     return o;
 }

@@ -4,6 +4,8 @@
 #pragma once
 
 #include <cuda_runtime.h>
+
+#include <utility>
 #include <stdint.h>
 
 namespace hhp {
@@ -100,141 +102,184 @@ __device__ __forceinline__ float warp_sum(float v) {
     return v;
 }
 
-// Block-wide sum of NC values per thread; result valid in thread 0 of the block. Every thread
-// parks its values in shared memory and warp 0 alone adds them (lane l: threads l, l+32, ... in
-// order, then a butterfly), so the FP64 work is ~blockDim adds rather than a butterfly in every
-// warp. Fixed order: the result does not depend on scheduling. scratch: blockDim.x * NC doubles.
+// Two warp sums for the price of one butterfly: after the exchange at distance 16 lanes 0-15
+// carry partial sums of `a` and lanes 16-31 partial sums of `b`, and four more levels finish
+// both (5 FP64 adds instead of 10). On return lanes 0-15 hold sum(a) in both outputs and lanes
+// 16-31 hold sum(b): read a at lane 0 and b at lane 16. Fixed order: reproducible.
+__device__ __forceinline__ void warp_sum2(double &a, double &b, int lane) {
+    const bool hi = (lane & 16) != 0;
+    double keep = hi ? b : a;
+    const double give = hi ? a : b;
+    keep += __shfl_xor_sync(0xffffffffu, give, 16);
+#pragma unroll
+    for (int o = 8; o >= 1; o >>= 1) keep += __shfl_xor_sync(0xffffffffu, keep, o);
+    a = keep;
+    b = keep;
+}
+
+// NQ warp sums at once with a transposed butterfly: at each of the first levels a lane hands
+// half of the quantities it still carries to its partner and keeps the other half, so the FP64
+// adds per warp are 5 (NQ = 1), 5 (NQ = 2) or 6 (NQ = 4) instead of 5 * NQ. On return `r` holds,
+// in lanes [q * 32/NQ, (q+1) * 32/NQ), the warp's sum of quantity q. Fixed order: reproducible.
+template <int NQ>
+__device__ __forceinline__ double warp_reduce(const double (&v)[NQ], int lane);
+template <>
+__device__ __forceinline__ double warp_reduce<1>(const double (&v)[1], int) {
+    return warp_sum(v[0]);
+}
+template <>
+__device__ __forceinline__ double warp_reduce<2>(const double (&v)[2], int lane) {
+    double a = v[0], b = v[1];
+    warp_sum2(a, b, lane);
+    return a;
+}
+template <>
+__device__ __forceinline__ double warp_reduce<4>(const double (&v)[4], int lane) {
+    const bool h16 = (lane & 16) != 0, h8 = (lane & 8) != 0;
+    double k0 = h16 ? v[2] : v[0], k1 = h16 ? v[3] : v[1];
+    const double g0 = h16 ? v[0] : v[2], g1 = h16 ? v[1] : v[3];
+    k0 += __shfl_xor_sync(0xffffffffu, g0, 16);
+    k1 += __shfl_xor_sync(0xffffffffu, g1, 16);
+    double k = h8 ? k1 : k0;
+    const double g = h8 ? k0 : k1;
+    k += __shfl_xor_sync(0xffffffffu, g, 8);
+#pragma unroll
+    for (int o = 4; o >= 1; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+    return k;
+}
+
+// Shared-memory doubles a kernel provides to the block reductions below (block_sum stages
+// blockDim.x * NC values, up to 512 x 2).
+constexpr int kRedScratch = 1024 + 80;
+
+// Sums of NQ values per thread over the first `nwa` warps of the block (nwa <= 16), returned to
+// every thread. Each of those warps reduces with warp_reduce, warp 0 adds the per-warp results
+// (3-5 more FP64 adds). Fixed order: every block running the same code on the same data gets the
+// same bits. Must be called by all threads. scratch: >= 16 * NQ + NQ doubles.
+template <int NQ>
+__device__ __forceinline__ void group_allreduce(double (&v)[NQ], int nwa, double *scratch) {
+    constexpr int G = 32 / NQ;  // lanes per quantity after warp_reduce
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    if (w < nwa) {
+        const double r = warp_reduce<NQ>(v, lane);
+        if ((lane & (G - 1)) == 0) scratch[(lane / G) * 16 + w] = r;
+    }
+    __syncthreads();
+    if (w == 0) {
+        const int q = lane / G, i = lane & (G - 1);
+        double s = i < nwa ? scratch[q * 16 + i] : 0.0;
+        if (G < 16 && nwa > G) s += i + G < nwa ? scratch[q * 16 + i + G] : 0.0;
+        // combine the per-warp values held by the G lanes of each quantity (only as many
+        // levels as there are warps)
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1)
+            if (o < G && o < nwa) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (i == 0) scratch[16 * NQ + q] = s;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) v[q] = scratch[16 * NQ + q];
+    __syncthreads();
+}
+
+// Block-wide sum of NC values per thread (blockDim.x a power of two, 32..512), returned to every
+// thread. A dense tree in shared memory -- at each level the lower half of the live threads adds
+// the upper half's values, so every FP64 instruction has all its lanes busy -- down to one warp,
+// then one warp_reduce. About 15*NC + 5 FP64 warp instructions for 512 threads, against 16*5 for
+// a butterfly in every warp. Fixed order.
 template <int NC>
 __device__ __forceinline__ void block_sum(double (&v)[NC], double *scratch) {
     const int t = threadIdx.x, T = blockDim.x;
 #pragma unroll
     for (int c = 0; c < NC; ++c) scratch[c * T + t] = v[c];
     __syncthreads();
-    if (t < 32) {
-        double s[NC];
+    for (int h = T >> 1; h >= 32; h >>= 1) {
+        if (t < h) {
 #pragma unroll
-        for (int c = 0; c < NC; ++c) {
-            s[c] = 0.0;
-            for (int i = t; i < T; i += 32) s[c] += scratch[c * T + i];
-            s[c] = warp_sum(s[c]);
+            for (int c = 0; c < NC; ++c) scratch[c * T + t] += scratch[c * T + t + h];
         }
-        if (t == 0) {
-#pragma unroll
-            for (int c = 0; c < NC; ++c) v[c] = s[c];
-        }
+        __syncthreads();
     }
+    double r[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) r[c] = t < 32 ? scratch[c * T + t] : 0.0;
     __syncthreads();
+    group_allreduce<NC>(r, 1, scratch);
+#pragma unroll
+    for (int c = 0; c < NC; ++c) v[c] = r[c];
 }
 
-// Shared-memory doubles a kernel provides to reduce_partials (records are staged in chunks).
-constexpr int kRedScratch = 2048;
+// One thread's running sums over records i = k, k + K, ... of part[i*NC + c] (i < n) followed
+// by extra[(i-n)*NC + c]; the first record is assigned, not added. ld.global.cg: the records were
+// written by an earlier kernel.
+template <int NC>
+__device__ __forceinline__ void thread_records(const double *__restrict__ part, int n, const double *__restrict__ extra,
+                                               int n_extra, double *s, int k, int K) {
+    const int tot = n + n_extra;
+    int i = k;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) s[c] = 0.0;
+    if (i < tot) {
+        const double *src = i < n ? part + i * NC : extra + (i - n) * NC;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) s[c] = __ldcg(src + c);
+    }
+    for (i += K; i < tot; i += K) {
+        const double *src = i < n ? part + i * NC : extra + (i - n) * NC;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) s[c] += __ldcg(src + c);
+    }
+}
+
+// Warps that reduce the partial records: one per scheduler, so the four FP64 pipes share the
+// adds and no warp's adds are spent on empty lanes of a mostly idle block.
+__device__ __forceinline__ int reducing_warps() { return min(static_cast<int>((blockDim.x + 31) >> 5), 4); }
 
 // Sum of per-block partials part[i*NC + c] for i in [0, n), plus extra[j*NC + c] for j in
-// [0, n_extra), computed identically by every calling block. Records are staged through shared
-// memory in chunks of kRedScratch/NC: all threads load a chunk at once (one memory round trip per
-// chunk), then warp 0 alone adds it (lane l: records l, l+32, ... in order, continuing its running
-// sums), and a final butterfly combines the lanes. Only warp 0 does FP64 adds, keeping the FP64
-// work per block near the record count (the FP64 pipe is GB300's scarcest unit). The order is
-// fixed, so every block gets the same bits. Must be called by all threads; the result is
-// returned to every thread. Loads use ld.global.cg (values written by earlier kernels).
+// [0, n_extra), computed identically by every calling block and returned to every thread.
+// The first four warps take records t, t + 128, ... in order and group_allreduce combines them
+// (GB300's FP64 pipe, ~64 cycles per warp instruction per scheduler, is the scarcest unit).
 template <int NC>
 __device__ __forceinline__ void reduce_partials(const double *__restrict__ part, int n,
                                                 const double *__restrict__ extra, int n_extra,
                                                 double (&out)[NC], double *scratch /* kRedScratch */) {
-    const int T = blockDim.x, t = threadIdx.x;
-    constexpr int kRec = kRedScratch / NC;
-    const int tot = n + n_extra;
-    double s[NC];
-#pragma unroll
-    for (int c = 0; c < NC; ++c) s[c] = 0.0;
-    for (int r0 = 0; r0 < tot; r0 += kRec) {
-        const int cnt = min(kRec, tot - r0);
-        for (int i = t; i < cnt * NC; i += T) {
-            const int g = r0 * NC + i;
-            scratch[i] = g < n * NC ? __ldcg(part + g) : __ldcg(extra + (g - n * NC));
-        }
-        __syncthreads();
-        if (t < 32) {
-            for (int i = t; i < cnt; i += 32) {
-#pragma unroll
-                for (int c = 0; c < NC; ++c) s[c] += scratch[i * NC + c];
-            }
-        }
-        __syncthreads();
-    }
-    if (t < 32) {
-#pragma unroll
-        for (int c = 0; c < NC; ++c) s[c] = warp_sum(s[c]);
-        if (t == 0) {
-#pragma unroll
-            for (int c = 0; c < NC; ++c) scratch[c] = s[c];
-        }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int c = 0; c < NC; ++c) out[c] = scratch[c];
-    __syncthreads();
+    const int nwa = reducing_warps(), K = nwa * 32, t = threadIdx.x;
+    if (t < K) thread_records<NC>(part, n, extra, n_extra, out, t, K);
+    group_allreduce<NC>(out, nwa, scratch);
 }
 
-// Two independent reductions (A = part_a + extra_a, B = part_b) staged together, so they cost
-// one memory round trip and one pass of warp 0 instead of two. Same order guarantees as
-// reduce_partials.
+// Two independent reductions (A = part_a + extra_a, B = part_b) in one pass: one memory round
+// trip and one group_allreduce over 2*NC quantities. Same order guarantees as reduce_partials.
 template <int NC>
 __device__ __forceinline__ void reduce_pair(const double *__restrict__ part_a, int na, const double *__restrict__ extra_a,
                                             int nea, const double *__restrict__ part_b, int nb, double (&out_a)[NC],
                                             double (&out_b)[NC], double *scratch /* kRedScratch */) {
-    const int T = blockDim.x, t = threadIdx.x;
-    constexpr int kRec = kRedScratch / NC;
-    const int ta = na + nea, tot = ta + nb;
-    double sa[NC], sb[NC];
-#pragma unroll
-    for (int c = 0; c < NC; ++c) sa[c] = sb[c] = 0.0;
-    for (int r0 = 0; r0 < tot; r0 += kRec) {
-        const int cnt = min(kRec, tot - r0);
-        for (int i = t; i < cnt * NC; i += T) {
-            const int g = r0 * NC + i;
-            double v;
-            if (g < na * NC) v = __ldcg(part_a + g);
-            else if (g < ta * NC) v = __ldcg(extra_a + (g - na * NC));
-            else v = __ldcg(part_b + (g - ta * NC));
-            scratch[i] = v;
-        }
-        __syncthreads();
-        if (t < 32) {
-            for (int i = t; i < cnt; i += 32) {
-                const bool in_a = r0 + i < ta;
-#pragma unroll
-                for (int c = 0; c < NC; ++c) {
-                    if (in_a) sa[c] += scratch[i * NC + c];
-                    else sb[c] += scratch[i * NC + c];
-                }
-            }
-        }
-        __syncthreads();
+    const int nwa = reducing_warps(), K = nwa * 32, t = threadIdx.x;
+    double v[2 * NC];
+    if (t < K) {
+        thread_records<NC>(part_a, na, extra_a, nea, v, t, K);
+        thread_records<NC>(part_b, nb, nullptr, 0, v + NC, t, K);
     }
-    if (t < 32) {
-#pragma unroll
-        for (int c = 0; c < NC; ++c) {
-            sa[c] = warp_sum(sa[c]);
-            sb[c] = warp_sum(sb[c]);
-        }
-        if (t == 0) {
-#pragma unroll
-            for (int c = 0; c < NC; ++c) {
-                scratch[c] = sa[c];
-                scratch[NC + c] = sb[c];
-            }
-        }
-    }
-    __syncthreads();
+    group_allreduce<2 * NC>(v, nwa, scratch);
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
-        out_a[c] = scratch[c];
-        out_b[c] = scratch[NC + c];
+        out_a[c] = v[c];
+        out_b[c] = v[NC + c];
     }
-    __syncthreads();
 }
 
 __device__ __forceinline__ bool finite_nonzero(double v) { return isfinite(v) && v != 0.0; }
+
+// kern<<<grid, block, smem, stream>>>(args...), returning the launch error.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_k(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                     Args &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
 
 }  // namespace hhp

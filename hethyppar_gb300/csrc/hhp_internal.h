@@ -52,7 +52,7 @@ void assign_units(const SellHost &P, int n_warps, std::vector<int> &warp_ptr, st
                   double *imbalance);
 
 struct PlanDev {
-    int rpl = 0, H = 0, n_slices = 0, n_long = 0, n_chunks = 0, ctas = 0, warps_per_cta = 0;
+    int rpl = 0, H = 0, n_slices = 0, n_long = 0, n_chunks = 0, ctas = 0, warps_per_cta = 0, unroll = 4;
     bool has_perm = false, sorted = false;
     long long total = 0;
     double padding = 1.0;
@@ -115,6 +115,7 @@ enum EpKind : int {
     EP_DOT1 = 1,    // y = A x; partial[0] += y.w1
     EP_DOT2 = 2,    // y = A x; partial[0] += y.w1, partial[1] += y.y
     EP_RESID = 3,   // y = w1 - A x (residual); partial[0] += y.y, partial[1] += w1.w1
+    EP_Y = 4,       // y = A x (EP_AXPBY with alpha 1, beta 0; chosen by the launcher)
 };
 
 hhp_status ensure_plan(hhp_mat *A, bool fp32);
@@ -157,8 +158,9 @@ inline int pad4(int n) { return (n + 3) & ~3; }
 
 // Kernel tuning knobs (environment overrides read once).
 struct Tuning {
-    int cap = 2048, long_thr = 256, window = 8192, wpc = 8, ctas_per_sm = 3, vec_blocks_per_sm = 2,
-        unroll_iters = 4;
+    // ctas_per_sm, spmv_unroll, rpl64: 0 = chosen per matrix at plan time
+    int cap = 2048, long_thr = 256, window = 8192, wpc = 8, ctas_per_sm = 0, vec_blocks_per_sm = 1,
+        unroll_iters = 4, spmv_unroll = 0, rpl64 = 0, rpl32 = 4;
 };
 const Tuning &tuning();
 

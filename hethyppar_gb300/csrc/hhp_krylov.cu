@@ -192,6 +192,16 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
     __shared__ double red[kRedScratch];
     __shared__ double bc[2];
     __shared__ int go;
+    constexpr int E = Unit<T>::E;
+    const int stride = gridDim.x * blockDim.x;
+    int u = blockIdx.x * blockDim.x + threadIdx.x;
+    // the first unit's operands are requested before the reductions: their latency overlaps them
+    T p[E], vv[E], r[E];
+    if (u < nu) {
+        ldu(p, P, u);
+        ldu(vv, V, u);
+        ldu(r, R, u);
+    }
     double v[2], w[2];
     reduce_pair<2>(part_xr, nparts, nullptr, 0, part_s, nparts, v, w, red);
     if (threadIdx.x == 0) {
@@ -234,15 +244,16 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
     __syncthreads();
     if (!go) return;
     const T tb = static_cast<T>(bc[0]), tw = static_cast<T>(bc[1]);
-    constexpr int E = Unit<T>::E;
-    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += gridDim.x * blockDim.x) {
-        T p[E], vv[E], r[E];
-        ldu(p, P, u);
-        ldu(vv, V, u);
-        ldu(r, R, u);
+    while (u < nu) {
 #pragma unroll
         for (int e = 0; e < E; ++e) p[e] = tfma(tb, tfma(tw, vv[e], p[e]), r[e]);
         stu(P, u, p);
+        u += stride;
+        if (u < nu) {
+            ldu(p, P, u);
+            ldu(vv, V, u);
+            ldu(r, R, u);
+        }
     }
 }
 
@@ -253,6 +264,14 @@ __global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const 
     __shared__ double red[kRedScratch];
     __shared__ double bc[1];
     __shared__ int go;
+    constexpr int E = Unit<T>::E;
+    const int stride = gridDim.x * blockDim.x;
+    int u = blockIdx.x * blockDim.x + threadIdx.x;
+    T r[E], vv[E];
+    if (u < nu) {
+        ldu(r, R, u);
+        ldu(vv, V, u);
+    }
     double v[2];
     reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
     if (threadIdx.x == 0) {
@@ -277,16 +296,18 @@ __global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const 
     __syncthreads();
     if (!go) return;
     const T ta = static_cast<T>(bc[0]);
-    constexpr int E = Unit<T>::E;
     double acc[1] = {0.0};
-    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += gridDim.x * blockDim.x) {
-        T r[E], vv[E], s[E];
-        ldu(r, R, u);
-        ldu(vv, V, u);
+    while (u < nu) {
+        T s[E];
 #pragma unroll
         for (int e = 0; e < E; ++e) s[e] = tfma(ta, vv[e], r[e]);
         acc[0] = dunit<E>(acc[0], s, s);
         stu(S, u, s);
+        u += stride;
+        if (u < nu) {
+            ldu(r, R, u);
+            ldu(vv, V, u);
+        }
     }
     block_sum<1>(acc, red);
     if (threadIdx.x == 0) {
@@ -304,6 +325,19 @@ __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P,
     __shared__ double red[kRedScratch];
     __shared__ double bc[2];
     __shared__ int go, hf;
+    constexpr int E = Unit<T>::E;
+    const int stride = gridDim.x * blockDim.x;
+    int u = blockIdx.x * blockDim.x + threadIdx.x;
+    // operands of the first unit requested before the reductions (t too: the rare half step,
+    // known only after them, does not need it)
+    T x[E], p[E], s[E], r0[E], t[E];
+    if (u < nu) {
+        ldu(x, X, u);
+        ldu(p, P, u);
+        ldu(s, S, u);
+        ldu(r0, R0, u);
+        ldu(t, Tv, u);
+    }
     double v[2], w[2];
     reduce_pair<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, part_s, nparts, v, w, red);
     if (threadIdx.x == 0) {
@@ -332,17 +366,10 @@ __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P,
     if (!go) return;
     const bool half = hf != 0;
     const T ta = static_cast<T>(bc[0]), tw = static_cast<T>(bc[1]), tnw = static_cast<T>(-bc[1]);
-    constexpr int E = Unit<T>::E;
     double acc[2] = {0.0, 0.0};
-    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += gridDim.x * blockDim.x) {
-        T x[E], p[E], s[E], r0[E], r[E];
-        ldu(x, X, u);
-        ldu(p, P, u);
-        ldu(s, S, u);
-        ldu(r0, R0, u);
+    while (u < nu) {
+        T r[E];
         if (!half) {
-            T t[E];
-            ldu(t, Tv, u);
 #pragma unroll
             for (int e = 0; e < E; ++e) {
                 x[e] = tfma(tw, s[e], tfma(ta, p[e], x[e]));
@@ -359,6 +386,14 @@ __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P,
         acc[1] = dunit<E>(acc[1], r, r);
         stu(X, u, x);
         stu(R, u, r);
+        u += stride;
+        if (u < nu) {
+            ldu(x, X, u);
+            ldu(p, P, u);
+            ldu(s, S, u);
+            ldu(r0, R0, u);
+            ldu(t, Tv, u);
+        }
     }
     block_sum<2>(acc, red);
     if (threadIdx.x == 0) {
@@ -418,13 +453,16 @@ __global__ void __launch_bounds__(512) k_mix_init(DevScal *sc, const double *Rd,
         part_s32[2 * blockIdx.x + 1] = 0.0;
     }
     if (b0t0()) {
-        sc->rr0 = bb;
-        sc->bb = bb;
-        sc->thr2 = sc->rtol2 * bb;
+        if (!sc->restart) {  // a restart after a breakdown keeps the counts and the threshold
+            sc->rr0 = bb;
+            sc->bb = bb;
+            sc->thr2 = sc->rtol2 * bb;
+            sc->iter = 0;
+            sc->updates = 0;
+            sc->hist_scale = 1.0;
+        }
         sc->thr2_rec = -1.0;
-        sc->iter = 0;
-        sc->iter_start = 0;
-        sc->hist_scale = 1.0;
+        sc->iter_start = sc->iter;
         sc->rho_prev = 1.0;
         sc->alpha = 1.0;
         sc->omega = 1.0;
@@ -432,11 +470,14 @@ __global__ void __launch_bounds__(512) k_mix_init(DevScal *sc, const double *Rd,
         sc->rr_max[0] = sc->rr_max[1] = rd2;
         sc->true_rr = rd2;
         sc->rr_last = rd2;
-        sc->updates = 0;
         sc->ru_flag = 0;
         sc->status = (rd2 <= sc->rtol2 * bb) ? ST_CONVERGED : (isfinite(rd2) ? ST_RUNNING : ST_BREAKDOWN);
     }
 }
+
+// Growth of the FP32 recursive ||r||^2 over the last true ||b - A x||^2 taken as divergence
+// (a factor 1e5 in the norm: BiCGStab's residual peaks stay far below it when it converges).
+constexpr double kDivergence2 = 1e10;
 
 // After K_XR: decide whether this iteration ends with an FP64 update; if so x += d, d = 0.
 __global__ void __launch_bounds__(512) k_ru_check(DevScal *sc, double *X, float *D32, int nu4,
@@ -451,8 +492,16 @@ __global__ void __launch_bounds__(512) k_ru_check(DevScal *sc, double *X, float 
             const double rr = v[1];
             const int it = sc->iter;
             const double mx = sc->rr_max[it & 1];
-            update = rr <= sc->thr2 || rr < sc->inner_rtol2 * mx || it >= sc->maxit || !isfinite(rr);
-            if (blockIdx.x == 0) sc->rr_max[(it + 1) & 1] = update ? mx : fmax(mx, rr);
+            // An FP32 recursive residual that has grown far above the true residual of the last
+            // update (or is not finite) means the FP32 recurrences have come apart: its increment
+            // is not folded into x, and the solve ends this pass as a breakdown (the host restarts
+            // it from x).
+            if (!isfinite(rr) || rr > kDivergence2 * sc->true_rr) {
+                if (blockIdx.x == 0) sc->status = ST_BREAKDOWN;
+            } else {
+                update = rr <= sc->thr2 || rr < sc->inner_rtol2 * mx || it >= sc->maxit;
+                if (blockIdx.x == 0) sc->rr_max[(it + 1) & 1] = update ? mx : fmax(mx, rr);
+            }
         }
         if (blockIdx.x == 0) sc->ru_flag = update;
         go = update;
@@ -511,17 +560,22 @@ __global__ void __launch_bounds__(512) k_ru_apply(DevScal *sc, const double *Rd,
 }
 
 // After the loop: fold any increment not yet absorbed by an update into x.
-__global__ void __launch_bounds__(512) k_mix_final(double *X, float *D32, int nu4) {
+__global__ void __launch_bounds__(512) k_mix_final(const DevScal *sc, double *X, float *D32, int nu4) {
+    // after a breakdown the increment since the last update may be garbage: x keeps its value
+    // as of that update (the increment is dropped)
+    const bool keep = sc->status != ST_BREAKDOWN;
     for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu4; u += gridDim.x * blockDim.x) {
         const float4 d = reinterpret_cast<const float4 *>(D32)[u];
         double2 a = reinterpret_cast<double2 *>(X)[2 * u];
         double2 b = reinterpret_cast<double2 *>(X)[2 * u + 1];
-        a.x += static_cast<double>(d.x);
-        a.y += static_cast<double>(d.y);
-        b.x += static_cast<double>(d.z);
-        b.y += static_cast<double>(d.w);
-        reinterpret_cast<double2 *>(X)[2 * u] = a;
-        reinterpret_cast<double2 *>(X)[2 * u + 1] = b;
+        if (keep) {
+            a.x += static_cast<double>(d.x);
+            a.y += static_cast<double>(d.y);
+            b.x += static_cast<double>(d.z);
+            b.y += static_cast<double>(d.w);
+            reinterpret_cast<double2 *>(X)[2 * u] = a;
+            reinterpret_cast<double2 *>(X)[2 * u + 1] = b;
+        }
         reinterpret_cast<float4 *>(D32)[u] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
 }
@@ -639,8 +693,8 @@ hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R,
     const PlanDev &pl = fp32 ? A->plan32 : A->plan64;
     hhp_status st = HHP_OK;
     for (int k = 0; k < s->unroll && st == HHP_OK; ++k) {
-        k_p<T><<<s->nblk, s->nthr, 0, s->s2>>>(sc, P, V, R, nu, part_xr, part_s, s->nblk, s->hist, s->hist_cap, cond,
-                                               k == 0 ? 1 : 0, A->ctx->dev_err, 1);
+        HHP_CUDA(launch_k(k_p<T>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, sc, P, V, R, nu, part_xr, part_s, s->nblk,
+                          s->hist, s->hist_cap, cond, k == 0 ? 1 : 0, A->ctx->dev_err, 1));
         if (fp32)
             st = launch_spmv32(A, s->s2, EP_DOT1, reinterpret_cast<const float *>(P), reinterpret_cast<float *>(V),
                                reinterpret_cast<const float *>(R0));
@@ -648,7 +702,7 @@ hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R,
             st = launch_spmv64(A, s->s2, EP_DOT1, reinterpret_cast<const double *>(P), reinterpret_cast<double *>(V),
                                reinterpret_cast<const double *>(R0), 1.0, 0.0);
         if (st != HHP_OK) break;
-        k_s<T><<<s->nblk, s->nthr, 0, s->s2>>>(sc, S, R, V, nu, parts_of(pl), part_s);
+        HHP_CUDA(launch_k(k_s<T>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, sc, S, R, V, nu, parts_of(pl), part_s));
         if (fp32)
             st = launch_spmv32(A, s->s2, EP_DOT2, reinterpret_cast<const float *>(S), reinterpret_cast<float *>(Tv),
                                reinterpret_cast<const float *>(S));
@@ -656,7 +710,8 @@ hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R,
             st = launch_spmv64(A, s->s2, EP_DOT2, reinterpret_cast<const double *>(S),
                                reinterpret_cast<double *>(Tv), reinterpret_cast<const double *>(S), 1.0, 0.0);
         if (st != HHP_OK) break;
-        k_xr<T><<<s->nblk, s->nthr, 0, s->s2>>>(sc, X, R, P, S, Tv, R0, nu, parts_of(pl), part_s, s->nblk, part_xr);
+        HHP_CUDA(launch_k(k_xr<T>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, sc, X, R, P, S, Tv, R0, nu, parts_of(pl),
+                          part_s, s->nblk, part_xr));
     }
     cudaGraph_t body_out = body;
     cudaError_t e = cudaStreamEndCapture(s->s2, &body_out);
@@ -676,20 +731,21 @@ hhp_status run_direct64(Solver *s) {
     const int nu = s->n_pad / 2;
     HHP_CUDA(cudaMemcpyAsync(s->sc, s->h_sc, kCtlBytes, cudaMemcpyHostToDevice, st));
     HHP_TRY(launch_spmv64(A, st, EP_RESID, s->X, s->R, s->B, 1.0, 0.0));
-    k_init<double><<<s->nblk, s->nthr, 0, st>>>(s->sc, s->R, s->R0, s->P, s->V, nu, parts_of(A->plan64), s->part_xr,
-                                                 s->part_s);
+    HHP_CUDA(launch_k(k_init<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->R, s->R0, s->P, s->V, nu,
+                      parts_of(A->plan64), s->part_xr, s->part_s));
     A->ctx->kernel_launches += 1;
     const PlanDev &pl = A->plan64;
     for (;;) {
         for (int k = 0; k < s->unroll; ++k) {
-            k_p<double><<<s->nblk, s->nthr, 0, st>>>(s->sc, s->P, s->V, s->R, nu, s->part_xr, s->part_s, s->nblk,
-                                                      s->hist, s->hist_cap, cudaGraphConditionalHandle(), k == 0,
-                                                      A->ctx->dev_err, 0);
+            HHP_CUDA(launch_k(k_p<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->P, s->V, s->R, nu,
+                              s->part_xr, s->part_s, s->nblk, s->hist, s->hist_cap, cudaGraphConditionalHandle(),
+                              k == 0, A->ctx->dev_err, 0));
             HHP_TRY(launch_spmv64(A, st, EP_DOT1, s->P, s->V, s->R0, 1.0, 0.0));
-            k_s<double><<<s->nblk, s->nthr, 0, st>>>(s->sc, s->S, s->R, s->V, nu, parts_of(pl), s->part_s);
+            HHP_CUDA(launch_k(k_s<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->S, s->R, s->V, nu,
+                              parts_of(pl), s->part_s));
             HHP_TRY(launch_spmv64(A, st, EP_DOT2, s->S, s->T, s->S, 1.0, 0.0));
-            k_xr<double><<<s->nblk, s->nthr, 0, st>>>(s->sc, s->X, s->R, s->P, s->S, s->T, s->R0, nu, parts_of(pl),
-                                                       s->part_s, s->nblk, s->part_xr);
+            HHP_CUDA(launch_k(k_xr<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->X, s->R, s->P, s->S, s->T,
+                              s->R0, nu, parts_of(pl), s->part_s, s->nblk, s->part_xr));
             A->ctx->kernel_launches += 3;
         }
         HHP_CUDA(cudaMemcpyAsync(s->h_sc, s->sc, sizeof(DevScal), cudaMemcpyDeviceToHost, st));
@@ -697,7 +753,7 @@ hhp_status run_direct64(Solver *s) {
         if (s->h_sc->status != ST_RUNNING) break;
     }
     HHP_TRY(launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0));
-    k_finish<<<1, 32, 0, st>>>(s->sc, parts_of(A->plan64));
+    HHP_CUDA(launch_k(k_finish, dim3(1), dim3(32), 0, st, s->sc, parts_of(A->plan64)));
     A->ctx->kernel_launches += 1;
     HHP_CUDA(cudaGetLastError());
     return HHP_OK;
@@ -718,15 +774,15 @@ hhp_status build_g64(Solver *s) {
         }
         rc = launch_spmv64(A, st, EP_RESID, s->X, s->R, s->B, 1.0, 0.0);
         if (rc != HHP_OK) break;
-        k_init<double><<<s->nblk, s->nthr, 0, st>>>(s->sc, s->R, s->R0, s->P, s->V, nu, parts_of(A->plan64),
-                                                     s->part_xr, s->part_s);
+        HHP_CUDA(launch_k(k_init<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->R, s->R0, s->P, s->V, nu,
+                          parts_of(A->plan64), s->part_xr, s->part_s));
         cudaGraphConditionalHandle cond;
         rc = capture_loop<double>(s, st, s->sc, s->X, s->R, s->R0, s->P, s->V, s->S, s->T, s->part_xr, s->part_s,
                                   false, &cond);
         if (rc != HHP_OK) break;
         rc = launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0);
         if (rc != HHP_OK) break;
-        k_finish<<<1, 32, 0, st>>>(s->sc, parts_of(A->plan64));
+        HHP_CUDA(launch_k(k_finish, dim3(1), dim3(32), 0, st, s->sc, parts_of(A->plan64)));
     } while (0);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(st, &g);
@@ -762,8 +818,8 @@ hhp_status build_gmix(Solver *s) {
         }
         rc = launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0);
         if (rc != HHP_OK) break;
-        k_mix_init<<<s->nblk, s->nthr, 0, st>>>(s->sc32, s->Y, s->R32, s->R0_32, s->D32, s->P32, s->V32, nu4,
-                                                 parts_of(A->plan64), s->part_xr32, s->part_s32);
+        HHP_CUDA(launch_k(k_mix_init, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc32, s->Y, s->R32, s->R0_32, s->D32,
+                          s->P32, s->V32, nu4, parts_of(A->plan64), s->part_xr32, s->part_s32));
         cudaStreamCaptureStatus cs;
         cudaGraph_t g = nullptr;
         const cudaGraphNode_t *deps = nullptr;
@@ -801,23 +857,23 @@ hhp_status build_gmix(Solver *s) {
         }
         const int nu = s->n_pad / 4;
         for (int k = 0; k < s->unroll && rc == HHP_OK; ++k) {
-            k_p<float><<<s->nblk, s->nthr, 0, s->s2>>>(s->sc32, s->P32, s->V32, s->R32, nu, s->part_xr32,
-                                                       s->part_s32, s->nblk, s->hist, s->hist_cap, cond, k == 0,
-                                                       A->ctx->dev_err, 1);
+            HHP_CUDA(launch_k(k_p<float>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, s->sc32, s->P32, s->V32, s->R32, nu,
+                              s->part_xr32, s->part_s32, s->nblk, s->hist, s->hist_cap, cond, k == 0, A->ctx->dev_err,
+                              1));
             rc = launch_spmv32(A, s->s2, EP_DOT1, s->P32, s->V32, s->R0_32);
             if (rc != HHP_OK) break;
-            k_s<float><<<s->nblk, s->nthr, 0, s->s2>>>(s->sc32, s->S32, s->R32, s->V32, nu, parts_of(A->plan32),
-                                                       s->part_s32);
+            HHP_CUDA(launch_k(k_s<float>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, s->sc32, s->S32, s->R32, s->V32, nu,
+                              parts_of(A->plan32), s->part_s32));
             rc = launch_spmv32(A, s->s2, EP_DOT2, s->S32, s->T32, s->S32);
             if (rc != HHP_OK) break;
-            k_xr<float><<<s->nblk, s->nthr, 0, s->s2>>>(s->sc32, s->D32, s->R32, s->P32, s->S32, s->T32, s->R0_32,
-                                                        nu, parts_of(A->plan32), s->part_s32, s->nblk,
-                                                        s->part_xr32);
-            k_ru_check<<<s->nblk, s->nthr, 0, s->s2>>>(s->sc32, s->X, s->D32, nu4, s->part_xr32, s->nblk);
+            HHP_CUDA(launch_k(k_xr<float>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, s->sc32, s->D32, s->R32, s->P32,
+                              s->S32, s->T32, s->R0_32, nu, parts_of(A->plan32), s->part_s32, s->nblk, s->part_xr32));
+            HHP_CUDA(launch_k(k_ru_check, dim3(s->nblk), dim3(s->nthr), 0, s->s2, s->sc32, s->X, s->D32, nu4,
+                              s->part_xr32, s->nblk));
             rc = launch_spmv64(A, s->s2, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0, &s->sc32->ru_flag);
             if (rc != HHP_OK) break;
-            k_ru_apply<<<s->nblk, s->nthr, 0, s->s2>>>(s->sc32, s->Y, s->R32, s->R0_32, nu4, parts_of(A->plan64),
-                                                       s->part_xr32);
+            HHP_CUDA(launch_k(k_ru_apply, dim3(s->nblk), dim3(s->nthr), 0, s->s2, s->sc32, s->Y, s->R32, s->R0_32,
+                              nu4, parts_of(A->plan64), s->part_xr32));
         }
         cudaGraph_t body_out = body;
         cudaError_t e2 = cudaStreamEndCapture(s->s2, &body_out);
@@ -826,10 +882,10 @@ hhp_status build_gmix(Solver *s) {
             rc = HHP_ERR_CUDA;
             break;
         }
-        k_mix_final<<<s->nblk, s->nthr, 0, st>>>(s->X, s->D32, nu4);
+        HHP_CUDA(launch_k(k_mix_final, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc32, s->X, s->D32, nu4));
         rc = launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0);
         if (rc != HHP_OK) break;
-        k_finish<<<1, 32, 0, st>>>(s->sc32, parts_of(A->plan64));
+        HHP_CUDA(launch_k(k_finish, dim3(1), dim3(32), 0, st, s->sc32, parts_of(A->plan64)));
     } while (0);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(st, &g);
@@ -902,18 +958,20 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
 
     DevScal &h = *s->h_sc;
     h.rtol2 = o->rtol * o->rtol;
-    const double irt = o->inner_rtol > 0.0 ? o->inner_rtol : 1e-5;
-    h.inner_rtol2 = irt * irt;
+    h.inner_rtol2 = 0.0;  // FP64 form: no inner tolerance
     h.maxit = o->maxit;
     h.fixed = (o->fixed_iters && !mixed) ? 1 : 0;
-    int total_iters = 0, outer = 0, half = 0;
+    int total_iters = 0, outer = 0, half = 0, fallback = 0;
     hhp_status result = HHP_OK;
     const int max_outer = o->max_outer > 0 ? o->max_outer : 50;
     double rel_true = NAN, rel_rec = NAN;
 
-    if (!mixed) {
+    // FP64 passes from the current X: residual replacement after rounding drift and restarts
+    // after a breakdown, each pass a fresh residual and shadow residual of X.
+    auto fp64_passes = [&](int it_before) -> hhp_status {
         const bool use_graph = env_int("HHP_SOLVE_GRAPH", 1) != 0;
         if (use_graph && !s->g64) HHP_TRY(build_g64(s));
+        h.maxit = o->maxit - it_before;
         int dev_status = ST_RUNNING;
         for (int pass = 0; pass < max_outer; ++pass) {
             h.restart = pass > 0 ? 1 : 0;
@@ -929,12 +987,16 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
             if (use_graph) ctx->kernel_launches += s->g64_kernels_pro + s->g64_kernels_epi + 5LL * s->unroll * h.bodies;
             dev_status = h.status;
             // Residual replacement: the recursive residual met the threshold but the true one
-            // did not (rounding drift); restart from the current iterate with the original r0.
+            // did not (rounding drift); restart from the current iterate, whose true residual
+            // becomes the new r and shadow residual.
             const bool conv = dev_status == ST_CONVERGED || dev_status == ST_CONVERGED_HALF;
             if (conv && !h.fixed && h.true_rr > h.thr2 && h.iter < h.maxit) continue;
+            // Breakdown (rho or omega vanished) after some progress: restart from the current
+            // iterate with a fresh shadow residual.
+            if (dev_status == ST_BREAKDOWN && !h.fixed && h.iter > h.iter_start && h.iter < h.maxit) continue;
             break;
         }
-        total_iters = h.iter;
+        total_iters = it_before + h.iter;
         half = dev_status == ST_CONVERGED_HALF;
         rel_true = sqrt(h.true_rr / h.bb);
         rel_rec = sqrt(h.rr_last / h.rr0);
@@ -942,6 +1004,11 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
         else if (dev_status == ST_CONVERGED || dev_status == ST_CONVERGED_HALF)
             result = (h.true_rr <= h.thr2 || h.thr2 < 0) ? HHP_OK : HHP_ERR_MAXIT;
         else result = status_of(dev_status);
+        return HHP_OK;
+    };
+
+    if (!mixed) {
+        HHP_TRY(fp64_passes(0));
     } else {
         if (!s->gmix) HHP_TRY(build_gmix(s));
         DevScal &h32 = *s->h_sc32;
@@ -950,12 +1017,20 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
         h32.inner_rtol2 = delta * delta;
         h32.maxit = o->maxit;
         h32.fixed = 0;
-        h32.restart = 0;
         h32.first_outer = 1;
-        HHP_CUDA(cudaGraphLaunch(s->gmix, st));
-        HHP_CUDA(cudaMemcpyAsync(s->h_sc32, s->sc32, sizeof(DevScal), cudaMemcpyDeviceToHost, st));
-        HHP_CUDA(cudaStreamSynchronize(st));
-        ctx->kernel_launches += s->gmix_kernels_pro + s->gmix_kernels_epi + 8LL * s->unroll * h32.bodies;
+        for (int pass = 0; pass < 2; ++pass) {
+            h32.restart = pass > 0 ? 1 : 0;
+            HHP_CUDA(cudaGraphLaunch(s->gmix, st));
+            HHP_CUDA(cudaMemcpyAsync(s->h_sc32, s->sc32, sizeof(DevScal), cudaMemcpyDeviceToHost, st));
+            HHP_CUDA(cudaStreamSynchronize(st));
+            ctx->kernel_launches += s->gmix_kernels_pro + s->gmix_kernels_epi + 8LL * s->unroll * h32.bodies;
+            // an inner breakdown or divergence after some progress restarts the FP32 recurrences
+            // once from the last FP64 iterate (its true residual becomes the new shadow
+            // residual); a second one hands the solve to FP64 below
+            if (pass == 0 && h32.status == ST_BREAKDOWN && h32.iter > h32.iter_start && h32.iter < h32.maxit)
+                continue;
+            break;
+        }
         total_iters = h32.iter;
         outer = h32.updates;
         half = 0;
@@ -963,6 +1038,12 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
         rel_true = sqrt(h32.true_rr / h32.bb);
         if (result == HHP_OK && !(h32.true_rr <= h32.thr2)) result = HHP_ERR_MAXIT;
         rel_rec = sqrt(h32.rr_last / h32.rr0);
+        // The FP32 recurrences came apart twice on this matrix: finish in FP64 from the last
+        // FP64 iterate, which the mixed passes left intact.
+        if (result == HHP_ERR_BREAKDOWN && total_iters < o->maxit) {
+            fallback = 1;
+            HHP_TRY(fp64_passes(total_iters));
+        }
     }
     HHP_CUDA(cudaEventRecord(ctx->ev1, st));
     HHP_CUDA(cudaMemcpyAsync(x_io, s->X, sizeof(double) * static_cast<size_t>(A->n),
@@ -997,6 +1078,7 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
         info->err_vs_target = err;
         info->t_solve_s = ms * 1e-3;
         info->status = result;
+        info->fp64_fallback = fallback;
     }
     if (o->cb && o->print_every > 0 && total_iters > 0) {
         const int nh = std::min(total_iters, s->hist_cap);

@@ -27,6 +27,7 @@
 //    the store of y; one partial per CTA, summed in a fixed order by the consumer.
 #include <algorithm>
 #include <mutex>
+#include <type_traits>
 
 #include "hhp_device.cuh"
 #include "hhp_internal.h"
@@ -35,21 +36,31 @@ namespace hhp {
 
 namespace {
 
-constexpr int kUnroll = 4;
+constexpr int kChunkUnroll = 4;
 
-template <typename VT>
+// A lane's words of one slice step: the values (V) and column indices (I) of its R rows, each
+// read with one load (8 or 16 bytes; 32 lanes make one contiguous request).
+template <typename VT, int R>
 struct Vec;
 template <>
-struct Vec<double> {
-    using V = double2;
-    using I = int2;
-    static constexpr int R = 2;
+struct Vec<double, 1> {
+    using V = double;
+    using I = int;
 };
 template <>
-struct Vec<float> {
+struct Vec<double, 2> {
+    using V = double2;
+    using I = int2;
+};
+template <>
+struct Vec<float, 2> {
+    using V = float2;
+    using I = int2;
+};
+template <>
+struct Vec<float, 4> {
     using V = float4;
     using I = int4;
-    static constexpr int R = 4;
 };
 
 template <typename VT>
@@ -93,7 +104,9 @@ __device__ __forceinline__ T comp(const V &v, int t) {
 // caller folds them into FP64 once per slice for FP32 data).
 template <typename VT, int EP, typename DT>
 __device__ __forceinline__ void row_epilogue(const SellArgs<VT> &a, int r, VT acc, DT &d0, DT &d1) {
-    if (EP == EP_AXPBY) {
+    if (EP == EP_Y) {
+        a.y[r] = acc;
+    } else if (EP == EP_AXPBY) {
         VT out = acc;
         if (a.scale) out = static_cast<VT>(a.alpha) * out;  // integer flags: no FP64 compares per row
         if (a.accum) out = vfma(static_cast<VT>(a.beta), a.y[r], out);
@@ -114,61 +127,74 @@ __device__ __forceinline__ void row_epilogue(const SellArgs<VT> &a, int r, VT ac
     }
 }
 
-template <typename VT, int EP>
+template <typename VT, int R, int U, int EP>
 __device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, int lane, double &d0, double &d1) {
-    using VV = typename Vec<VT>::V;
-    using IV = typename Vec<VT>::I;
-    constexpr int R = Vec<VT>::R;
+    using VV = typename Vec<VT, R>::V;
+    using IV = typename Vec<VT, R>::I;
     constexpr int H = 32 * R;
     const long long base = a.slice_ptr[s];
+    // the slice's longest row: every lane walks this many steps (uniform across the warp)
+    const int wmax = static_cast<int>((a.slice_ptr[s + 1] - base) / H);
     const int q0 = s * H + lane * R;
     const IV lv = *reinterpret_cast<const IV *>(a.pos_len + q0);
     int len[R];
 #pragma unroll
     for (int t = 0; t < R; ++t) len[t] = comp<IV, int>(lv, t);
-    int maxlen = len[0];
-#pragma unroll
-    for (int t = 1; t < R; ++t) maxlen = max(maxlen, len[t]);
     const VV *vp = reinterpret_cast<const VV *>(a.sval + base) + lane;
     const IV *cp = reinterpret_cast<const IV *>(a.scol + base) + lane;
     VT acc[R];
 #pragma unroll
     for (int t = 0; t < R; ++t) acc[t] = VT(0);
-    // Software pipeline over groups of kUnroll steps: the values and indices of group g+1 are
-    // requested before the gathers and multiply-adds of group g, so the HBM latency of the
+    // Software pipeline over full groups of U steps: the values and indices of group g+1
+    // are requested before the gathers and multiply-adds of group g, so the HBM latency of the
     // streams overlaps the L1/L2 latency of the gathers (warps issue in order: a load placed
-    // after a stalled FMA would wait for it).
-    VV v[kUnroll];
-    IV c[kUnroll];
+    // after a stalled FMA would wait for it). The last wmax % U steps run one at a time
+    // after the loop: a multiply-add predicated off still occupies GB300's FP64 pipe for a full
+    // warp slot, so no group is ever padded with dead steps.
+    VV v[U];
+    IV c[U];
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) {
-        v[u] = u < maxlen ? __ldg(vp + static_cast<size_t>(u) * 32) : VV();
-        c[u] = u < maxlen ? __ldg(cp + static_cast<size_t>(u) * 32) : IV();
+    for (int u = 0; u < U; ++u) {
+        v[u] = u < wmax ? __ldg(vp + static_cast<size_t>(u) * 32) : VV();
+        c[u] = u < wmax ? __ldg(cp + static_cast<size_t>(u) * 32) : IV();
     }
-    for (int j = 0; j < maxlen; j += kUnroll) {
-        VV vn[kUnroll];
-        IV cn[kUnroll];
+    int j = 0;
+    for (; j + U <= wmax; j += U) {
+        VV vn[U];
+        IV cn[U];
 #pragma unroll
-        for (int u = 0; u < kUnroll; ++u) {
-            const int jn = j + kUnroll + u;
-            vn[u] = jn < maxlen ? __ldg(vp + static_cast<size_t>(jn) * 32) : VV();
-            cn[u] = jn < maxlen ? __ldg(cp + static_cast<size_t>(jn) * 32) : IV();
+        for (int u = 0; u < U; ++u) {
+            const int jn = j + U + u;
+            vn[u] = jn < wmax ? __ldg(vp + static_cast<size_t>(jn) * 32) : VV();
+            cn[u] = jn < wmax ? __ldg(cp + static_cast<size_t>(jn) * 32) : IV();
         }
-        VT xv[kUnroll][R];
+        VT xv[U][R];
 #pragma unroll
-        for (int u = 0; u < kUnroll; ++u)
+        for (int u = 0; u < U; ++u)
 #pragma unroll
             for (int t = 0; t < R; ++t) xv[u][t] = (j + u < len[t]) ? __ldg(a.x + comp<IV, int>(c[u], t)) : VT(0);
 #pragma unroll
-        for (int u = 0; u < kUnroll; ++u)
+        for (int u = 0; u < U; ++u)
 #pragma unroll
             for (int t = 0; t < R; ++t)
                 if (j + u < len[t]) acc[t] = vfma(comp<VV, VT>(v[u], t), xv[u][t], acc[t]);
 #pragma unroll
-        for (int u = 0; u < kUnroll; ++u) {
+        for (int u = 0; u < U; ++u) {
             v[u] = vn[u];
             c[u] = cn[u];
         }
+    }
+    // tail steps (their values and indices were requested by the last prefetch: L1 hits)
+#pragma unroll 1
+    for (; j < wmax; ++j) {
+        const VV vt = __ldg(vp + static_cast<size_t>(j) * 32);
+        const IV ct = __ldg(cp + static_cast<size_t>(j) * 32);
+        VT xt[R];
+#pragma unroll
+        for (int t = 0; t < R; ++t) xt[t] = (j < len[t]) ? __ldg(a.x + comp<IV, int>(ct, t)) : VT(0);
+#pragma unroll
+        for (int t = 0; t < R; ++t)
+            if (j < len[t]) acc[t] = vfma(comp<VV, VT>(vt, t), xt[t], acc[t]);
     }
     VT e0 = VT(0), e1 = VT(0);
 #pragma unroll
@@ -177,7 +203,7 @@ __device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, int lane,
         const int r = a.has_perm ? a.pos_row[p] : p;
         if (r >= 0 && r < a.m) row_epilogue<VT, EP>(a, r, acc[t], e0, e1);
     }
-    if (EP != EP_AXPBY) {
+    if (EP != EP_AXPBY && EP != EP_Y) {
         d0 += static_cast<double>(e0);
         d1 += static_cast<double>(e1);
     }
@@ -187,19 +213,19 @@ template <typename VT, int EP>
 __device__ __forceinline__ void do_chunk(const SellArgs<VT> &a, int c, int lane) {
     const int4 d = __ldg(&a.chunks[c]);
     VT acc = VT(0);
-    for (int k = d.z + lane; k < d.w; k += 32 * kUnroll) {
-        VT v[kUnroll], xv[kUnroll];
-        int cc[kUnroll];
+    for (int k = d.z + lane; k < d.w; k += 32 * kChunkUnroll) {
+        VT v[kChunkUnroll], xv[kChunkUnroll];
+        int cc[kChunkUnroll];
 #pragma unroll
-        for (int u = 0; u < kUnroll; ++u) {
+        for (int u = 0; u < kChunkUnroll; ++u) {
             const int kk = k + 32 * u;
             v[u] = kk < d.w ? __ldg(a.csr_val + kk) : VT(0);
             cc[u] = kk < d.w ? __ldg(a.csr_col + kk) : 0;
         }
 #pragma unroll
-        for (int u = 0; u < kUnroll; ++u) xv[u] = (k + 32 * u < d.w) ? __ldg(a.x + cc[u]) : VT(0);
+        for (int u = 0; u < kChunkUnroll; ++u) xv[u] = (k + 32 * u < d.w) ? __ldg(a.x + cc[u]) : VT(0);
 #pragma unroll
-        for (int u = 0; u < kUnroll; ++u)
+        for (int u = 0; u < kChunkUnroll; ++u)
             if (k + 32 * u < d.w) acc = vfma(v[u], xv[u], acc);
     }
     acc = warp_sum(acc);
@@ -217,7 +243,7 @@ __device__ __forceinline__ void do_chunk(const SellArgs<VT> &a, int c, int lane)
             a.long_cnt[l] = 0u;  // ready for the next launch
             double e0 = 0.0, e1 = 0.0;
             row_epilogue<VT, EP, double>(a, d.x, static_cast<VT>(tot), e0, e1);
-            if (EP != EP_AXPBY) {
+            if (EP != EP_AXPBY && EP != EP_Y) {
                 a.long_dot[2 * l] = e0;
                 a.long_dot[2 * l + 1] = e1;
             }
@@ -225,12 +251,18 @@ __device__ __forceinline__ void do_chunk(const SellArgs<VT> &a, int c, int lane)
     }
 }
 
-template <typename VT, int EP>
-__global__ void __launch_bounds__(256, 3) k_spmv(const SellArgs<VT> a) {
+// Resident CTAs of 256 threads that the register need of R*U words in flight per lane allows.
+template <int R, int U>
+struct MinCtas {
+    static constexpr int value = R * U >= 8 ? 3 : (R * U >= 4 ? 5 : 6);
+};
+
+template <typename VT, int R, int U, int EP>
+__global__ void __launch_bounds__(256, MinCtas<R, U>::value) k_spmv(const SellArgs<VT> a) {
     // After a recorded device error every later launch returns at once (uniform across the grid).
     if (*reinterpret_cast<volatile const int *>(a.err) != DEV_OK) return;
     if (a.gate && *a.gate == 0) return;
-    __shared__ double red[2 * 256];
+    __shared__ double red[16];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int gw = blockIdx.x * nw + warp;
     double d0 = 0.0, d1 = 0.0;
@@ -238,42 +270,53 @@ __global__ void __launch_bounds__(256, 3) k_spmv(const SellArgs<VT> a) {
     const int ub = a.warp_ptr[gw], ue = a.warp_ptr[gw + 1];
     for (int i = ub; i < ue; ++i) {
         const int u = __ldg(a.warp_units + i);
-        if (u < a.n_slices) do_slice<VT, EP>(a, u, lane, d0, d1);
+        if (u < a.n_slices) do_slice<VT, R, U, EP>(a, u, lane, d0, d1);
         else do_chunk<VT, EP>(a, u - a.n_slices, lane);
     }
-    if (EP != EP_AXPBY) {
-        // per-CTA partial: lanes park their sums in shared memory, warp 0 adds them in thread
-        // order (fixed, and only one warp spends FP64 adds on it)
-        const int T = blockDim.x, t = threadIdx.x;
-        red[t] = d0;
-        red[T + t] = d1;
+    if (EP != EP_AXPBY && EP != EP_Y) {
+        // per-CTA partial: each warp folds its lanes' (d0, d1) with a transposed butterfly
+        // (5 FP64 adds for both sums), warp 0 adds the warps' results; fixed order throughout
+        warp_sum2(d0, d1, lane);
+        if (lane == 0) red[warp] = d0;
+        if (lane == 16) red[8 + warp] = d1;
         __syncthreads();
-        if (t < 32) {
-            double s0 = 0.0, s1 = 0.0;
-            for (int i = t; i < T; i += 32) {
-                s0 += red[i];
-                s1 += red[T + i];
-            }
-            s0 = warp_sum(s0);
-            s1 = warp_sum(s1);
-            if (t == 0) {
-                a.cta_part[2 * blockIdx.x] = s0;
-                a.cta_part[2 * blockIdx.x + 1] = s1;
-            }
+        if (warp == 0) {
+            // lanes 0-7 take the warps' d0 sums, lanes 8-15 their d1 sums (nw <= 8 warps)
+            double s = (lane < 16 && (lane & 7) < nw) ? red[lane] : 0.0;
+#pragma unroll
+            for (int o = 4; o >= 1; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) a.cta_part[2 * blockIdx.x] = s;
+            if (lane == 8) a.cta_part[2 * blockIdx.x + 1] = s;
         }
     }
 }
 
-template <typename VT>
-cudaError_t launch_ep(EpKind ep, const PlanDev &p, const SellArgs<VT> &a, cudaStream_t s) {
+template <typename VT, int R, int U>
+cudaError_t launch_ru(EpKind ep, const PlanDev &p, const SellArgs<VT> &a, cudaStream_t s) {
     const dim3 grid(p.ctas), block(p.warps_per_cta * 32);
     switch (ep) {
-        case EP_DOT1: k_spmv<VT, EP_DOT1><<<grid, block, 0, s>>>(a); break;
-        case EP_DOT2: k_spmv<VT, EP_DOT2><<<grid, block, 0, s>>>(a); break;
-        case EP_RESID: k_spmv<VT, EP_RESID><<<grid, block, 0, s>>>(a); break;
-        default: k_spmv<VT, EP_AXPBY><<<grid, block, 0, s>>>(a); break;
+        case EP_DOT1: return launch_k(k_spmv<VT, R, U, EP_DOT1>, grid, block, 0, s, a);
+        case EP_DOT2: return launch_k(k_spmv<VT, R, U, EP_DOT2>, grid, block, 0, s, a);
+        case EP_RESID: return launch_k(k_spmv<VT, R, U, EP_RESID>, grid, block, 0, s, a);
+        default:
+            // y = A x needs no epilogue arithmetic: a separate instantiation keeps the FP64 pipe
+            // free of predicated-off scale and accumulate instructions
+            if (!a.scale && !a.accum) return launch_k(k_spmv<VT, R, U, EP_Y>, grid, block, 0, s, a);
+            return launch_k(k_spmv<VT, R, U, EP_AXPBY>, grid, block, 0, s, a);
     }
-    return cudaGetLastError();
+}
+
+// Rows per lane come from the plan, the unroll from the tuning (2 or 4 steps in flight per lane).
+template <typename VT>
+cudaError_t launch_ep(EpKind ep, const PlanDev &p, const SellArgs<VT> &a, cudaStream_t s) {
+    const bool u2 = p.unroll == 2;
+    if constexpr (std::is_same<VT, double>::value) {
+        if (p.rpl == 1) return u2 ? launch_ru<VT, 1, 2>(ep, p, a, s) : launch_ru<VT, 1, 4>(ep, p, a, s);
+        return u2 ? launch_ru<VT, 2, 2>(ep, p, a, s) : launch_ru<VT, 2, 4>(ep, p, a, s);
+    } else {
+        if (p.rpl == 2) return u2 ? launch_ru<VT, 2, 2>(ep, p, a, s) : launch_ru<VT, 2, 4>(ep, p, a, s);
+        return u2 ? launch_ru<VT, 4, 2>(ep, p, a, s) : launch_ru<VT, 4, 4>(ep, p, a, s);
+    }
 }
 
 // Device re-layout: position p of the slices <- row pos_row[p] of the CSR (values cast to VT).
@@ -320,12 +363,34 @@ template <typename VT>
 hhp_status build_plan_dev(hhp_mat *A, PlanDev &p) {
     const Tuning &t = tuning();
     hhp_ctx *ctx = A->ctx;
-    constexpr int R = Vec<VT>::R;
+    // Layout and launch shape, measured on GB300 over the banded, power-law and stencil workloads
+    // (environment knobs override each choice). FP32: 4 rows per lane (16-byte words), 4 steps in
+    // flight, 3 CTAs per SM. FP64: short regular rows (stencils: no long rows, no length sorting
+    // needed, under 10 nonzeros per row) take 2 rows per lane, 2 steps, 5 CTAs; length-sorted
+    // matrices (power-law rows) 1 row per lane, 4 steps, 5 CTAs, so more warps share the
+    // scattered gathers; others (banded) 2 rows per lane, 4 steps, 3 CTAs.
     SellHost h;
-    build_plan(A->m, A->rowptr_host.data(), R, std::max(t.long_thr, 1), std::max(t.cap, 32), std::max(t.window, 1),
-               h);
+    int R, U, cps;
+    if (std::is_same<VT, double>::value) {
+        build_plan(A->m, A->rowptr_host.data(), 2, std::max(t.long_thr, 1), std::max(t.cap, 32),
+                   std::max(t.window, 1), h);
+        const bool regular = h.long_rows.empty() && !h.sorted && A->nnz < 10LL * std::max(A->m, 1);
+        R = t.rpl64 == 1 || t.rpl64 == 2 ? t.rpl64 : (h.sorted && !regular ? 1 : 2);
+        U = t.spmv_unroll == 2 || t.spmv_unroll == 4 ? t.spmv_unroll : (regular ? 2 : 4);
+        cps = t.ctas_per_sm > 0 ? t.ctas_per_sm : (regular || R == 1 ? 5 : 3);
+        if (R != 2)
+            build_plan(A->m, A->rowptr_host.data(), R, std::max(t.long_thr, 1), std::max(t.cap, 32),
+                       std::max(t.window, 1), h);
+    } else {
+        R = t.rpl32 == 2 ? 2 : 4;
+        U = t.spmv_unroll == 2 || t.spmv_unroll == 4 ? t.spmv_unroll : 4;
+        cps = t.ctas_per_sm > 0 ? t.ctas_per_sm : 3;
+        build_plan(A->m, A->rowptr_host.data(), R, std::max(t.long_thr, 1), std::max(t.cap, 32),
+                   std::max(t.window, 1), h);
+    }
     p.release();
     p.rpl = R;
+    p.unroll = U;
     p.H = h.H;
     p.n_slices = h.n_slices;
     p.n_long = static_cast<int>(h.long_rows.size());
@@ -335,7 +400,7 @@ hhp_status build_plan_dev(hhp_mat *A, PlanDev &p) {
     p.total = h.total;
     p.padding = h.padding;
     p.warps_per_cta = std::min(std::max(t.wpc, 1), 8);
-    p.ctas = ctx->num_sms * std::min(std::max(t.ctas_per_sm, 1), 8);
+    p.ctas = ctx->num_sms * std::min(std::max(cps, 1), 8);
     std::vector<int> wptr, wunits;
     assign_units(h, p.ctas * p.warps_per_cta, wptr, wunits, &p.imbalance);
     HHP_TRY(upload(&p.warp_ptr, wptr));

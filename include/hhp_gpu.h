@@ -72,6 +72,8 @@ typedef struct {
     double err_vs_target;      /* max_i |x_i - x_target_i| (NaN when no target was given)        */
     double t_solve_s;          /* device time of the solve (CUDA events on the context stream)   */
     hhp_status status;
+    int fp64_fallback;         /* mixed: 1 if the FP32 recurrences kept breaking down or diverging
+                                  and the solve was finished in FP64 from the last FP64 iterate  */
 } hhp_solve_info;
 
 /* ---- errors -------------------------------------------------------------------------------- */
