@@ -155,8 +155,9 @@ def run_reference_arm(args, rk):
 
 
 def traffic_from_profile():
-    """DRAM bytes per SpMV launch from the committed ncu summary (scaled to the full workload)."""
-    p = os.path.join(ROOT, "profiles", "spmv_fp64_banded450k_ncu.md")
+    """DRAM bytes (read + write) of one C2 SpMV launch, from the committed ncu summary of the same
+    kernel on the same workload (captured at full size: one launch holds ~0.2 GB)."""
+    p = os.path.join(ROOT, "profiles", "k_spmv_fp64_banded450k.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
