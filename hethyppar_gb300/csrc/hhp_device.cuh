@@ -1,6 +1,6 @@
-// hhp_device.cuh -- device-side building blocks for the sm_103a kernels: 1-D TMA bulk copies
-// (cp.async.bulk) completing on shared-memory mbarriers, bounded mbarrier waits, and warp/block
-// reductions with a fixed summation order (so every reduction is bit-reproducible run to run).
+// hhp_device.cuh -- device-side building blocks for the sm_103a kernels: status codes, warp and
+// block reductions with a fixed summation order (so every reduction is bit-reproducible run to
+// run), and the host-side kernel launcher.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -10,10 +10,13 @@
 
 namespace hhp {
 
-// Device error codes written to the context's error word (first writer wins).
+// Device error codes for the context's error word. No kernel of this build waits on another
+// (the long-row combine is a last-arriver atomic count, every other ordering is a kernel
+// boundary), so nothing sets it today; SpMV launches and the solve loop check it, so a future
+// bounded wait that gives up stops every later launch and the solve returns HHP_ERR_TIMEOUT.
 enum : int {
     DEV_OK = 0,
-    DEV_ERR_TIMEOUT = 1,   // an mbarrier wait exceeded its time limit
+    DEV_ERR_TIMEOUT = 1,
 };
 
 // Solver status values kept in device memory.
@@ -26,70 +29,6 @@ enum : int {
     ST_MAXIT = 5,          // iteration cap reached
     ST_DEVICE_ERROR = 6,   // a kernel recorded a device error (e.g. a wait timeout)
 };
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ uint64_t global_timer_ns() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-// Makes mbarrier initialisation visible to the async (TMA) proxy.
-__device__ __forceinline__ void fence_mbar_init() {
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-// Orders this thread's earlier generic-proxy shared-memory accesses before later async-proxy
-// writes (a TMA copy into a buffer the warp has just read).
-__device__ __forceinline__ void fence_proxy_async_smem() {
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Waits for the mbarrier phase with the given parity to complete, for at most `limit_ns`.
-// Returns false on timeout (the caller records the error and stops issuing work).
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint64_t limit_ns) {
-    if (mbar_try_wait(bar, parity)) return true;
-    const uint64_t t0 = global_timer_ns();
-    while (true) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if (global_timer_ns() - t0 > limit_ns) return false;
-    }
-}
-
-// 1-D bulk copy global -> shared (TMA engine), completion counted on `bar` in bytes.
-// Both addresses 16-byte aligned, bytes a multiple of 16.
-__device__ __forceinline__ void bulk_g2s(void *dst_smem, const void *src_gmem, uint32_t bytes, uint64_t *bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_u32(dst_smem)),
-        "l"(src_gmem), "r"(bytes), "r"(smem_u32(bar))
-        : "memory");
-}
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
