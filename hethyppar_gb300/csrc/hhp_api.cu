@@ -51,6 +51,7 @@ const Tuning &tuning() {
         d.spmv_unroll = env_int("HHP_SPMV_UNROLL", d.spmv_unroll);
         d.rpl64 = env_int("HHP_SPMV_RPL64", d.rpl64);
         d.rpl32 = env_int("HHP_SPMV_RPL32", d.rpl32);
+        d.stream_hint = env_int("HHP_SPMV_HINT", d.stream_hint);
         return d;
     }();
     return t;

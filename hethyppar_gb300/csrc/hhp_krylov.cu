@@ -43,7 +43,7 @@ struct DevScal {
     // state
     double rho_prev, rho_cur, alpha, omega, beta;
     double rr0, thr2, bb, rr_last, true_rr;
-    double rd2, hist_scale;
+    double rd2;
     double thr2_rec;      // threshold for the recursive-residual tests (-1: none, mixed form)
     double rr_max[2];     // mixed form: largest recursive ||r||^2 since the last FP64 update,
                           // double-buffered by iteration parity (read one, write the other)
@@ -166,7 +166,6 @@ __global__ void __launch_bounds__(512) k_init(DevScal *sc, const T *R, T *R0, T 
             sc->thr2_rec = sc->thr2;
             sc->iter = 0;
             sc->bb = bb;
-            sc->hist_scale = 1.0;
         }
         sc->iter_start = sc->iter;
         sc->bodies = 0;
@@ -209,14 +208,16 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
         const bool lead = blockIdx.x == 0;
         const int st = sc->status;
         int term = ST_RUNNING;
+        if (lead && first_in_body) sc->bodies += 1;  // bodies executed (kernel-launch accounting)
         if (st != ST_RUNNING) {
             if (lead && use_cond) cudaGraphSetConditional(cond, 0);
             term = st;
         } else {
-            if (lead && first_in_body) sc->bodies += 1;
             const int iter = sc->iter, it0 = sc->iter_start;
             const double thr2 = sc->thr2_rec;
-            if (lead && iter > it0 && iter - 1 < hist_cap) hist[iter - 1] = sc->hist_scale * sqrt(rr / sc->rr0);
+            // raw ||r||^2: the host forms sqrt(rr / rr0), keeping FP64 sqrt and division off the
+            // loop's critical path
+            if (lead && iter > it0 && iter - 1 < hist_cap) hist[iter - 1] = rr;
             if (*reinterpret_cast<volatile const int *>(dev_err) != DEV_OK) term = ST_DEVICE_ERROR;
             else if (thr2 >= 0.0 && iter > it0 && ss <= thr2) term = ST_CONVERGED_HALF;
             else if (thr2 >= 0.0 && rr <= thr2) term = ST_CONVERGED;
@@ -459,7 +460,6 @@ __global__ void __launch_bounds__(512) k_mix_init(DevScal *sc, const double *Rd,
             sc->thr2 = sc->rtol2 * bb;
             sc->iter = 0;
             sc->updates = 0;
-            sc->hist_scale = 1.0;
         }
         sc->thr2_rec = -1.0;
         sc->iter_start = sc->iter;
@@ -663,19 +663,24 @@ hhp_status ensure_fp32_inner(hhp_mat *A, Solver *s) {
     return HHP_OK;
 }
 
-// Adds a WHILE conditional node to the graph being captured on `stream`, captures `unroll`
-// iterations of the loop body into it on s->s2, and makes later work on `stream` depend on it.
-template <typename T>
-hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R, T *R0, T *P, T *V, T *S, T *Tv,
-                        double *part_xr, double *part_s, bool fp32, cudaGraphConditionalHandle *cond_out) {
-    hhp_mat *A = s->A;
+// A conditional handle in the graph being captured on `stream`; its value starts at 1 at every
+// graph launch and K_P clears it to end the loop.
+hhp_status make_cond(cudaStream_t stream, cudaGraphConditionalHandle *cond) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    HHP_CUDA(cudaStreamGetCaptureInfo(stream, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+    HHP_CUDA(cudaGraphConditionalHandleCreate(cond, g, 1, cudaGraphCondAssignDefault));
+    return HHP_OK;
+}
+
+// Adds a WHILE node on `cond` after the work captured so far on `stream`, makes later work on
+// `stream` depend on it, and starts capturing its body on s->s2 (ended by end_loop_body).
+hhp_status begin_loop_body(Solver *s, cudaStream_t stream, cudaGraphConditionalHandle cond) {
     cudaStreamCaptureStatus cs;
     cudaGraph_t g = nullptr;
     const cudaGraphNode_t *deps = nullptr;
     size_t nd = 0;
     HHP_CUDA(cudaStreamGetCaptureInfo(stream, &cs, nullptr, &g, &deps, nullptr, &nd));
-    cudaGraphConditionalHandle cond;
-    HHP_CUDA(cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault));
     cudaGraphNodeParams cp = {};
     memset(&cp, 0, sizeof(cp));
     cp.type = cudaGraphNodeTypeConditional;
@@ -686,15 +691,42 @@ hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R,
     HHP_CUDA(cudaGraphAddNode(&cn, g, deps, nullptr, nd, &cp));
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     HHP_CUDA(cudaStreamUpdateCaptureDependencies(stream, &cn, nullptr, 1, cudaStreamSetCaptureDependencies));
-
     HHP_CUDA(cudaStreamBeginCaptureToGraph(s->s2, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    return HHP_OK;
+}
+
+hhp_status end_loop_body(Solver *s, hhp_status rc) {
+    cudaGraph_t body_out = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s->s2, &body_out);
+    if (rc != HHP_OK) return rc;
+    HHP_CUDA(e);
+    HHP_CUDA(cudaGetLastError());
+    return HHP_OK;
+}
+
+// The FP64 (or FP32-inner) iteration loop as graph nodes on `stream`: the first K_P (stop tests
+// on the initial residual) before a WHILE node whose body holds `unroll` iterations, each
+// [SpMV + r0.v, K_S, SpMV + t.s/t.t, K_XR, (mixed: update check, gated FP64 residual, residual
+// replacement), K_P]. K_P ends the body, so the body that meets the stop test ends at the test:
+// no kernel after it runs for nothing.
+template <typename T>
+hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R, T *R0, T *P, T *V, T *S, T *Tv,
+                        double *part_xr, double *part_s, bool fp32) {
+    hhp_mat *A = s->A;
     constexpr int E = Unit<T>::E;
-    const int nu = s->n_pad / E;
+    const int nu = s->n_pad / E, nu4 = s->n_pad / 4;
     const PlanDev &pl = fp32 ? A->plan32 : A->plan64;
     hhp_status st = HHP_OK;
+    auto kp = [&](cudaStream_t q, cudaGraphConditionalHandle c, int first_in_body) -> hhp_status {
+        HHP_CUDA(launch_k(k_p<T>, dim3(s->nblk), dim3(s->nthr), 0, q, sc, P, V, R, nu, part_xr, part_s, s->nblk,
+                          s->hist, s->hist_cap, c, first_in_body, A->ctx->dev_err, 1));
+        return HHP_OK;
+    };
+    cudaGraphConditionalHandle cond;
+    HHP_TRY(make_cond(stream, &cond));
+    HHP_TRY(kp(stream, cond, 0));  // stop tests on the initial residual, before the node
+    HHP_TRY(begin_loop_body(s, stream, cond));
     for (int k = 0; k < s->unroll && st == HHP_OK; ++k) {
-        HHP_CUDA(launch_k(k_p<T>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, sc, P, V, R, nu, part_xr, part_s, s->nblk,
-                          s->hist, s->hist_cap, cond, k == 0 ? 1 : 0, A->ctx->dev_err, 1));
         if (fp32)
             st = launch_spmv32(A, s->s2, EP_DOT1, reinterpret_cast<const float *>(P), reinterpret_cast<float *>(V),
                                reinterpret_cast<const float *>(R0));
@@ -702,7 +734,11 @@ hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R,
             st = launch_spmv64(A, s->s2, EP_DOT1, reinterpret_cast<const double *>(P), reinterpret_cast<double *>(V),
                                reinterpret_cast<const double *>(R0), 1.0, 0.0);
         if (st != HHP_OK) break;
-        HHP_CUDA(launch_k(k_s<T>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, sc, S, R, V, nu, parts_of(pl), part_s));
+        if (launch_k(k_s<T>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, sc, S, R, V, nu, parts_of(pl), part_s) !=
+            cudaSuccess) {
+            st = HHP_ERR_CUDA;
+            break;
+        }
         if (fp32)
             st = launch_spmv32(A, s->s2, EP_DOT2, reinterpret_cast<const float *>(S), reinterpret_cast<float *>(Tv),
                                reinterpret_cast<const float *>(S));
@@ -710,16 +746,29 @@ hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R,
             st = launch_spmv64(A, s->s2, EP_DOT2, reinterpret_cast<const double *>(S),
                                reinterpret_cast<double *>(Tv), reinterpret_cast<const double *>(S), 1.0, 0.0);
         if (st != HHP_OK) break;
-        HHP_CUDA(launch_k(k_xr<T>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, sc, X, R, P, S, Tv, R0, nu, parts_of(pl),
-                          part_s, s->nblk, part_xr));
+        if (launch_k(k_xr<T>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, sc, X, R, P, S, Tv, R0, nu, parts_of(pl),
+                     part_s, s->nblk, part_xr) != cudaSuccess) {
+            st = HHP_ERR_CUDA;
+            break;
+        }
+        if (fp32) {
+            // reliable update: decide, gated FP64 residual, gated residual replacement
+            if (launch_k(k_ru_check, dim3(s->nblk), dim3(s->nthr), 0, s->s2, s->sc32, s->X, s->D32, nu4,
+                         s->part_xr32, s->nblk) != cudaSuccess) {
+                st = HHP_ERR_CUDA;
+                break;
+            }
+            st = launch_spmv64(A, s->s2, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0, &s->sc32->ru_flag);
+            if (st != HHP_OK) break;
+            if (launch_k(k_ru_apply, dim3(s->nblk), dim3(s->nthr), 0, s->s2, s->sc32, s->Y, s->R32, s->R0_32, nu4,
+                         parts_of(A->plan64), s->part_xr32) != cudaSuccess) {
+                st = HHP_ERR_CUDA;
+                break;
+            }
+        }
+        st = kp(s->s2, cond, k == 0 ? 1 : 0);
     }
-    cudaGraph_t body_out = body;
-    cudaError_t e = cudaStreamEndCapture(s->s2, &body_out);
-    if (st != HHP_OK) return st;
-    HHP_CUDA(e);
-    HHP_CUDA(cudaGetLastError());
-    *cond_out = cond;
-    return HHP_OK;
+    return end_loop_body(s, st);
 }
 
 // The FP64 loop launched kernel by kernel (no graph), for profilers that cannot see inside
@@ -776,9 +825,8 @@ hhp_status build_g64(Solver *s) {
         if (rc != HHP_OK) break;
         HHP_CUDA(launch_k(k_init<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->R, s->R0, s->P, s->V, nu,
                           parts_of(A->plan64), s->part_xr, s->part_s));
-        cudaGraphConditionalHandle cond;
         rc = capture_loop<double>(s, st, s->sc, s->X, s->R, s->R0, s->P, s->V, s->S, s->T, s->part_xr, s->part_s,
-                                  false, &cond);
+                                  false);
         if (rc != HHP_OK) break;
         rc = launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0);
         if (rc != HHP_OK) break;
@@ -794,15 +842,16 @@ hhp_status build_g64(Solver *s) {
     cudaError_t ie = cudaGraphInstantiate(&s->g64, g, 0);
     cudaGraphDestroy(g);
     HHP_CUDA(ie);
-    s->g64_kernels_pro = 2;
+    s->g64_kernels_pro = 3;
     s->g64_kernels_epi = 2;
     // launch_spmv64 counted its captured launches; graph launches are counted when executed.
     A->ctx->kernel_launches -= 2 + 2 * s->unroll;
     return HHP_OK;
 }
 
-// Mixed-form graph: FP64 residual, init, WHILE{ unroll x [FP32 iteration, update check, gated
-// FP64 residual, gated residual replacement] }, fold d into x, FP64 true residual, finish.
+// Mixed-form graph: FP64 residual, init, first stop test, WHILE{ unroll x [FP32 iteration,
+// update check, gated FP64 residual, gated residual replacement, stop test] }, fold d into x,
+// FP64 true residual, finish.
 hhp_status build_gmix(Solver *s) {
     hhp_mat *A = s->A;
     cudaStream_t st = A->ctx->stream;
@@ -820,68 +869,9 @@ hhp_status build_gmix(Solver *s) {
         if (rc != HHP_OK) break;
         HHP_CUDA(launch_k(k_mix_init, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc32, s->Y, s->R32, s->R0_32, s->D32,
                           s->P32, s->V32, nu4, parts_of(A->plan64), s->part_xr32, s->part_s32));
-        cudaStreamCaptureStatus cs;
-        cudaGraph_t g = nullptr;
-        const cudaGraphNode_t *deps = nullptr;
-        size_t nd = 0;
-        if (cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd) != cudaSuccess) {
-            rc = HHP_ERR_CUDA;
-            break;
-        }
-        cudaGraphConditionalHandle cond;
-        if (cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) {
-            rc = HHP_ERR_CUDA;
-            break;
-        }
-        cudaGraphNodeParams cp = {};
-        memset(&cp, 0, sizeof(cp));
-        cp.type = cudaGraphNodeTypeConditional;
-        cp.conditional.handle = cond;
-        cp.conditional.type = cudaGraphCondTypeWhile;
-        cp.conditional.size = 1;
-        cudaGraphNode_t cn;
-        if (cudaGraphAddNode(&cn, g, deps, nullptr, nd, &cp) != cudaSuccess) {
-            rc = HHP_ERR_CUDA;
-            break;
-        }
-        cudaGraph_t body = cp.conditional.phGraph_out[0];
-        if (cudaStreamUpdateCaptureDependencies(st, &cn, nullptr, 1, cudaStreamSetCaptureDependencies) !=
-            cudaSuccess) {
-            rc = HHP_ERR_CUDA;
-            break;
-        }
-        if (cudaStreamBeginCaptureToGraph(s->s2, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) !=
-            cudaSuccess) {
-            rc = HHP_ERR_CUDA;
-            break;
-        }
-        const int nu = s->n_pad / 4;
-        for (int k = 0; k < s->unroll && rc == HHP_OK; ++k) {
-            HHP_CUDA(launch_k(k_p<float>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, s->sc32, s->P32, s->V32, s->R32, nu,
-                              s->part_xr32, s->part_s32, s->nblk, s->hist, s->hist_cap, cond, k == 0, A->ctx->dev_err,
-                              1));
-            rc = launch_spmv32(A, s->s2, EP_DOT1, s->P32, s->V32, s->R0_32);
-            if (rc != HHP_OK) break;
-            HHP_CUDA(launch_k(k_s<float>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, s->sc32, s->S32, s->R32, s->V32, nu,
-                              parts_of(A->plan32), s->part_s32));
-            rc = launch_spmv32(A, s->s2, EP_DOT2, s->S32, s->T32, s->S32);
-            if (rc != HHP_OK) break;
-            HHP_CUDA(launch_k(k_xr<float>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, s->sc32, s->D32, s->R32, s->P32,
-                              s->S32, s->T32, s->R0_32, nu, parts_of(A->plan32), s->part_s32, s->nblk, s->part_xr32));
-            HHP_CUDA(launch_k(k_ru_check, dim3(s->nblk), dim3(s->nthr), 0, s->s2, s->sc32, s->X, s->D32, nu4,
-                              s->part_xr32, s->nblk));
-            rc = launch_spmv64(A, s->s2, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0, &s->sc32->ru_flag);
-            if (rc != HHP_OK) break;
-            HHP_CUDA(launch_k(k_ru_apply, dim3(s->nblk), dim3(s->nthr), 0, s->s2, s->sc32, s->Y, s->R32, s->R0_32,
-                              nu4, parts_of(A->plan64), s->part_xr32));
-        }
-        cudaGraph_t body_out = body;
-        cudaError_t e2 = cudaStreamEndCapture(s->s2, &body_out);
+        rc = capture_loop<float>(s, st, s->sc32, s->D32, s->R32, s->R0_32, s->P32, s->V32, s->S32, s->T32,
+                                 s->part_xr32, s->part_s32, true);
         if (rc != HHP_OK) break;
-        if (e2 != cudaSuccess) {
-            rc = HHP_ERR_CUDA;
-            break;
-        }
         HHP_CUDA(launch_k(k_mix_final, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc32, s->X, s->D32, nu4));
         rc = launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0);
         if (rc != HHP_OK) break;
@@ -899,7 +889,7 @@ hhp_status build_gmix(Solver *s) {
     cudaError_t ie = cudaGraphInstantiate(&s->gmix, g, 0);
     cudaGraphDestroy(g);
     HHP_CUDA(ie);
-    s->gmix_kernels_pro = 2;
+    s->gmix_kernels_pro = 3;
     s->gmix_kernels_epi = 3;
     // launch_spmv* counted their captured launches; graph launches are counted when executed.
     A->ctx->kernel_launches -= 2 + 3 * s->unroll;
@@ -961,7 +951,8 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
     h.inner_rtol2 = 0.0;  // FP64 form: no inner tolerance
     h.maxit = o->maxit;
     h.fixed = (o->fixed_iters && !mixed) ? 1 : 0;
-    int total_iters = 0, outer = 0, half = 0, fallback = 0;
+    int total_iters = 0, outer = 0, half = 0, fallback = 0, hist_offset = 0;
+    double hist_rr0 = 1.0;
     hhp_status result = HHP_OK;
     const int max_outer = o->max_outer > 0 ? o->max_outer : 50;
     double rel_true = NAN, rel_rec = NAN;
@@ -997,6 +988,8 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
             break;
         }
         total_iters = it_before + h.iter;
+        hist_offset = it_before;
+        hist_rr0 = h.rr0;
         half = dev_status == ST_CONVERGED_HALF;
         rel_true = sqrt(h.true_rr / h.bb);
         rel_rec = sqrt(h.rr_last / h.rr0);
@@ -1032,6 +1025,7 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
             break;
         }
         total_iters = h32.iter;
+        hist_rr0 = h32.rr0;
         outer = h32.updates;
         half = 0;
         result = status_of(h32.status);
@@ -1080,12 +1074,17 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
         info->status = result;
         info->fp64_fallback = fallback;
     }
-    if (o->cb && o->print_every > 0 && total_iters > 0) {
-        const int nh = std::min(total_iters, s->hist_cap);
+    // History: the device stored ||r_k||^2 per iteration; the callback gets ||r_k|| / ||r_0||. After
+    // an FP64 fallback the buffer holds the FP64 part only (iterations after hist_offset).
+    if (o->cb && o->print_every > 0 && total_iters > hist_offset) {
+        const int nh = std::min(total_iters - hist_offset, s->hist_cap);
         std::vector<double> hh(static_cast<size_t>(nh));
         HHP_CUDA(cudaMemcpy(hh.data(), s->hist, sizeof(double) * static_cast<size_t>(nh), cudaMemcpyDeviceToHost));
-        for (int i = 0; i < nh; ++i)
-            if ((i + 1) % o->print_every == 0 || i + 1 == nh) o->cb(i + 1, hh[static_cast<size_t>(i)], o->user);
+        for (int i = 0; i < nh; ++i) {
+            const int it = hist_offset + i + 1;
+            if (it % o->print_every == 0 || i + 1 == nh)
+                o->cb(it, std::sqrt(hh[static_cast<size_t>(i)] / hist_rr0), o->user);
+        }
     }
     return result;
 }

@@ -26,6 +26,7 @@
 //  * Epilogues fuse the BiCGStab dot products (r0.v, t.s, t.t) and the residual r = b - A x into
 //    the store of y; one partial per CTA, summed in a fixed order by the consumer.
 #include <algorithm>
+#include <cstring>
 #include <mutex>
 #include <type_traits>
 
@@ -62,6 +63,54 @@ struct Vec<float, 4> {
     using V = float4;
     using I = int4;
 };
+
+// Loads of the matrix streams (slice values and indices, chunk CSR ranges) with a cache policy:
+//   HINT 0: the read-only path (ld.global.nc), default caching;
+//   HINT 1: not allocated in L1 (leaves L1 to the x gathers), L2 evict-first (the stream does
+//           not push the solver's vectors out of L2);
+//   HINT 2: not allocated in L1, L2 evict-last (the matrix tends to stay in L2 across launches);
+//   HINT 3: not allocated in L1, default L2 policy.
+template <int HINT>
+__device__ __forceinline__ uint64_t stream_policy() {
+    uint64_t pol = 0;
+    if (HINT == 1) asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    if (HINT == 2) asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+template <int HINT, typename T>
+__device__ __forceinline__ T ld_stream(const T *p, uint64_t pol) {
+    static_assert(sizeof(T) == 4 || sizeof(T) == 8 || sizeof(T) == 16, "4, 8 or 16 bytes");
+    if (HINT == 0) return __ldg(p);
+    T out;
+    if (sizeof(T) == 4) {
+        uint32_t r;
+        if (HINT == 3) asm volatile("ld.global.nc.L1::no_allocate.b32 %0, [%1];" : "=r"(r) : "l"(p));
+        else asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(r) : "l"(p), "l"(pol));
+        memcpy(&out, &r, 4);
+    } else if (sizeof(T) == 8) {
+        uint32_t r[2];
+        if (HINT == 3)
+            asm volatile("ld.global.nc.L1::no_allocate.v2.b32 {%0, %1}, [%2];" : "=r"(r[0]), "=r"(r[1]) : "l"(p));
+        else
+            asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.b32 {%0, %1}, [%2], %3;"
+                         : "=r"(r[0]), "=r"(r[1])
+                         : "l"(p), "l"(pol));
+        memcpy(&out, r, 8);
+    } else {
+        uint32_t r[4];
+        if (HINT == 3)
+            asm volatile("ld.global.nc.L1::no_allocate.v4.b32 {%0, %1, %2, %3}, [%4];"
+                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                         : "l"(p));
+        else
+            asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.b32 {%0, %1, %2, %3}, [%4], %5;"
+                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                         : "l"(p), "l"(pol));
+        memcpy(&out, r, 16);
+    }
+    return out;
+}
 
 template <typename VT>
 struct SellArgs {
@@ -127,8 +176,9 @@ __device__ __forceinline__ void row_epilogue(const SellArgs<VT> &a, int r, VT ac
     }
 }
 
-template <typename VT, int R, int U, int EP>
-__device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, int lane, double &d0, double &d1) {
+template <typename VT, int R, int U, int EP, int HINT>
+__device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, int lane, double &d0, double &d1,
+                                         uint64_t pol) {
     using VV = typename Vec<VT, R>::V;
     using IV = typename Vec<VT, R>::I;
     constexpr int H = 32 * R;
@@ -155,8 +205,8 @@ __device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, int lane,
     IV c[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-        v[u] = u < wmax ? __ldg(vp + static_cast<size_t>(u) * 32) : VV();
-        c[u] = u < wmax ? __ldg(cp + static_cast<size_t>(u) * 32) : IV();
+        v[u] = u < wmax ? ld_stream<HINT>(vp + static_cast<size_t>(u) * 32, pol) : VV();
+        c[u] = u < wmax ? ld_stream<HINT>(cp + static_cast<size_t>(u) * 32, pol) : IV();
     }
     int j = 0;
     for (; j + U <= wmax; j += U) {
@@ -165,8 +215,8 @@ __device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, int lane,
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const int jn = j + U + u;
-            vn[u] = jn < wmax ? __ldg(vp + static_cast<size_t>(jn) * 32) : VV();
-            cn[u] = jn < wmax ? __ldg(cp + static_cast<size_t>(jn) * 32) : IV();
+            vn[u] = jn < wmax ? ld_stream<HINT>(vp + static_cast<size_t>(jn) * 32, pol) : VV();
+            cn[u] = jn < wmax ? ld_stream<HINT>(cp + static_cast<size_t>(jn) * 32, pol) : IV();
         }
         VT xv[U][R];
 #pragma unroll
@@ -187,8 +237,8 @@ __device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, int lane,
     // tail steps (their values and indices were requested by the last prefetch: L1 hits)
 #pragma unroll 1
     for (; j < wmax; ++j) {
-        const VV vt = __ldg(vp + static_cast<size_t>(j) * 32);
-        const IV ct = __ldg(cp + static_cast<size_t>(j) * 32);
+        const VV vt = ld_stream<HINT>(vp + static_cast<size_t>(j) * 32, pol);
+        const IV ct = ld_stream<HINT>(cp + static_cast<size_t>(j) * 32, pol);
         VT xt[R];
 #pragma unroll
         for (int t = 0; t < R; ++t) xt[t] = (j < len[t]) ? __ldg(a.x + comp<IV, int>(ct, t)) : VT(0);
@@ -209,8 +259,8 @@ __device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, int lane,
     }
 }
 
-template <typename VT, int EP>
-__device__ __forceinline__ void do_chunk(const SellArgs<VT> &a, int c, int lane) {
+template <typename VT, int EP, int HINT>
+__device__ __forceinline__ void do_chunk(const SellArgs<VT> &a, int c, int lane, uint64_t pol) {
     const int4 d = __ldg(&a.chunks[c]);
     VT acc = VT(0);
     for (int k = d.z + lane; k < d.w; k += 32 * kChunkUnroll) {
@@ -219,8 +269,8 @@ __device__ __forceinline__ void do_chunk(const SellArgs<VT> &a, int c, int lane)
 #pragma unroll
         for (int u = 0; u < kChunkUnroll; ++u) {
             const int kk = k + 32 * u;
-            v[u] = kk < d.w ? __ldg(a.csr_val + kk) : VT(0);
-            cc[u] = kk < d.w ? __ldg(a.csr_col + kk) : 0;
+            v[u] = kk < d.w ? ld_stream<HINT>(a.csr_val + kk, pol) : VT(0);
+            cc[u] = kk < d.w ? ld_stream<HINT>(a.csr_col + kk, pol) : 0;
         }
 #pragma unroll
         for (int u = 0; u < kChunkUnroll; ++u) xv[u] = (k + 32 * u < d.w) ? __ldg(a.x + cc[u]) : VT(0);
@@ -257,7 +307,7 @@ struct MinCtas {
     static constexpr int value = R * U >= 8 ? 3 : (R * U >= 4 ? 5 : 6);
 };
 
-template <typename VT, int R, int U, int EP>
+template <typename VT, int R, int U, int EP, int HINT>
 __global__ void __launch_bounds__(256, MinCtas<R, U>::value) k_spmv(const SellArgs<VT> a) {
     // After a recorded device error every later launch returns at once (uniform across the grid).
     if (*reinterpret_cast<volatile const int *>(a.err) != DEV_OK) return;
@@ -268,10 +318,11 @@ __global__ void __launch_bounds__(256, MinCtas<R, U>::value) k_spmv(const SellAr
     double d0 = 0.0, d1 = 0.0;
     // this warp's units, balanced at plan time (fixed order: reductions are reproducible)
     const int ub = a.warp_ptr[gw], ue = a.warp_ptr[gw + 1];
+    const uint64_t pol = stream_policy<HINT>();
     for (int i = ub; i < ue; ++i) {
         const int u = __ldg(a.warp_units + i);
-        if (u < a.n_slices) do_slice<VT, R, U, EP>(a, u, lane, d0, d1);
-        else do_chunk<VT, EP>(a, u - a.n_slices, lane);
+        if (u < a.n_slices) do_slice<VT, R, U, EP, HINT>(a, u, lane, d0, d1, pol);
+        else do_chunk<VT, EP, HINT>(a, u - a.n_slices, lane, pol);
     }
     if (EP != EP_AXPBY && EP != EP_Y) {
         // per-CTA partial: each warp folds its lanes' (d0, d1) with a transposed butterfly
@@ -291,18 +342,31 @@ __global__ void __launch_bounds__(256, MinCtas<R, U>::value) k_spmv(const SellAr
     }
 }
 
-template <typename VT, int R, int U>
-cudaError_t launch_ru(EpKind ep, const PlanDev &p, const SellArgs<VT> &a, cudaStream_t s) {
+template <typename VT, int R, int U, int HINT>
+cudaError_t launch_ruh(EpKind ep, const PlanDev &p, const SellArgs<VT> &a, cudaStream_t s) {
     const dim3 grid(p.ctas), block(p.warps_per_cta * 32);
     switch (ep) {
-        case EP_DOT1: return launch_k(k_spmv<VT, R, U, EP_DOT1>, grid, block, 0, s, a);
-        case EP_DOT2: return launch_k(k_spmv<VT, R, U, EP_DOT2>, grid, block, 0, s, a);
-        case EP_RESID: return launch_k(k_spmv<VT, R, U, EP_RESID>, grid, block, 0, s, a);
+        case EP_DOT1: return launch_k(k_spmv<VT, R, U, EP_DOT1, HINT>, grid, block, 0, s, a);
+        case EP_DOT2: return launch_k(k_spmv<VT, R, U, EP_DOT2, HINT>, grid, block, 0, s, a);
+        case EP_RESID: return launch_k(k_spmv<VT, R, U, EP_RESID, HINT>, grid, block, 0, s, a);
         default:
             // y = A x needs no epilogue arithmetic: a separate instantiation keeps the FP64 pipe
             // free of predicated-off scale and accumulate instructions
-            if (!a.scale && !a.accum) return launch_k(k_spmv<VT, R, U, EP_Y>, grid, block, 0, s, a);
-            return launch_k(k_spmv<VT, R, U, EP_AXPBY>, grid, block, 0, s, a);
+            if (!a.scale && !a.accum) return launch_k(k_spmv<VT, R, U, EP_Y, HINT>, grid, block, 0, s, a);
+            return launch_k(k_spmv<VT, R, U, EP_AXPBY, HINT>, grid, block, 0, s, a);
+    }
+}
+
+// Stream loads: FP64 matrices skip L1 (measured faster in the FP64 solves: L1 stays with the x
+// gathers), FP32 ones keep the default (their solves measured slower without L1 allocation).
+template <typename VT, int R, int U>
+cudaError_t launch_ru(EpKind ep, const PlanDev &p, const SellArgs<VT> &a, cudaStream_t s) {
+    const int h = tuning().stream_hint;
+    switch (h >= 0 ? h : (std::is_same<VT, double>::value ? 3 : 0)) {
+        case 1: return launch_ruh<VT, R, U, 1>(ep, p, a, s);
+        case 2: return launch_ruh<VT, R, U, 2>(ep, p, a, s);
+        case 3: return launch_ruh<VT, R, U, 3>(ep, p, a, s);
+        default: return launch_ruh<VT, R, U, 0>(ep, p, a, s);
     }
 }
 
