@@ -272,6 +272,29 @@ def run_ours(args, rk):
     e1.record(stream)
     e1.synchronize()
     warm_ms = e0.elapsed_time(e1) / 50
+    # library comparator: cuSPARSE's CSR SpMV (torch.mv on a sparse CSR tensor) on the same
+    # matrix and vector, same flush and timing
+    cus_ms = []
+    try:
+        At = torch.sparse_csr_tensor(torch.as_tensor(s.rowptr, device="cuda", dtype=torch.int32),
+                                     torch.as_tensor(s.col, device="cuda", dtype=torch.int32),
+                                     torch.as_tensor(s.val, device="cuda"), size=(s.m, s.n))
+        with torch.cuda.stream(stream):
+            for _ in range(5):
+                torch.mv(At, xs)
+            for _ in range(30):
+                torch.cuda.synchronize()
+                flush_l2(sync=False)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                yc = torch.mv(At, xs)
+                e1.record(stream)
+                e1.synchronize()
+                cus_ms.append(e0.elapsed_time(e1))
+        cus_err = float((yc - ys).abs().max().item())
+        del At
+    except Exception as e:  # reported, not fatal
+        cus_err = str(e)
     hbm, peak_kind = peaks()
     bsp = spmv_bytes(s.m, s.n, s.nnz)
     t_sp = statistics.mean(spmv_ms) * 1e-3  # mean: the event clock ticks in ~2 us steps
@@ -294,6 +317,10 @@ def run_ours(args, rk):
            "rel_res_true": res.rel_res_true, "err_vs_target": res.err_vs_target,
            "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": 2 * 8 * s.n, "d2h_bytes_per_step": 8 * s.n},
            "roofline": roof,
+           "spmv_cusparse": ({"us_l2_flushed": statistics.mean(cus_ms) * 1e3,
+                              "gbs_l2_flushed": bsp / (statistics.mean(cus_ms) * 1e-3) / 1e9,
+                              "max_abs_diff_vs_ours": cus_err, "via": "torch.mv on a sparse CSR tensor (cuSPARSE SpMV)"}
+                             if cus_ms else {"error": cus_err}),
            "spmv": {"gbs_l2_flushed": achieved, "frac_of_hbm": achieved / hbm, "us_l2_flushed": t_sp * 1e6,
                     "gbs_effective_warm_l2": bsp / (warm_ms * 1e-3) / 1e9, "us_warm": warm_ms * 1e3},
            "clocks": clk, "gpu_launches": int(launches)}

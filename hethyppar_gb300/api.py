@@ -269,6 +269,14 @@ def bicgstab_backward(ctx: Context, A: Matrix, x, dldx, *, rtol: float = 1e-12, 
     return dldb, dlda, res
 
 
+def csr_file_write(path: str, rowptr, col, val, n: Optional[int] = None):
+    """Binary CSR file (hhp_csr_file_write): read back by mtx_read / Matrix.from_mtx / the CLI's -m."""
+    rp, cl, vl = _host(rowptr, np.int32), _host(col, np.int32), _host(val, np.float64)
+    m = rp.size - 1
+    check(lib().hhp_csr_file_write(path.encode(), m, m if n is None else int(n), int(rp[-1]), _ptr(rp), _ptr(cl),
+                                   _ptr(vl)), "hhp_csr_file_write")
+
+
 def vector_read(path: str, size: int) -> np.ndarray:
     out = np.empty(size, np.float64)
     check(lib().hhp_vector_read(path.encode(), size, _ptr(out)), "hhp_vector_read")

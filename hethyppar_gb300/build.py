@@ -23,7 +23,7 @@ ORACLE_DIR = os.path.join(ROOT, "oracle")
 REFERENCE_DIR = "/root/reference"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE]
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-pthread", "-I" + INCLUDE]
 
 
 def _nvcc() -> str:
@@ -86,7 +86,7 @@ def build_lib(verbose: bool = False) -> str:
                     print(out)
     objs = [os.path.join(OBJ_DIR, os.path.basename(s) + ".o") for s in srcs]
     if _stale(LIB, objs):
-        _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
+        _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-lpthread"])
         _stamp(LIB)
     return LIB
 

@@ -29,10 +29,10 @@
 
 #include "hhp_gpu.h"
 
-enum { OPT_RTOL = 1000, OPT_FIXED, OPT_PREC, OPT_XT, OPT_PERM, OPT_PRINT, OPT_OUTFMT, OPT_DEVICE };
+enum { OPT_RTOL = 1000, OPT_FIXED, OPT_PREC, OPT_XT, OPT_PERM, OPT_PRINT, OPT_OUTFMT, OPT_DEVICE, OPT_WCSR };
 
 struct arguments {
-    char *input_matrix, *input_x, *input_y, *output_x, *x_target, *perm;
+    char *input_matrix, *input_x, *input_y, *output_x, *x_target, *perm, *write_csr;
     int n_iters, fixed, mixed, print_every, exact, device;
     double rtol;
 };
@@ -51,6 +51,7 @@ static struct argp_option options[] = {
     {"print-every", OPT_PRINT, "K", 0, "Print the residual every K iterations", 0},
     {"out-format", OPT_OUTFMT, "compat|exact", 0, "Number format of the output X file", 0},
     {"device", OPT_DEVICE, "ID", 0, "CUDA device (default 0)", 0},
+    {"write-csr", OPT_WCSR, "FILE", 0, "Also store the matrix as a binary CSR file (later runs: -m FILE)", 0},
     {0}};
 
 static error_t parse_opt(int key, char *arg, struct argp_state *state) {
@@ -78,6 +79,7 @@ static error_t parse_opt(int key, char *arg, struct argp_state *state) {
             else argp_error(state, "unknown output format '%s'", arg);
             break;
         case OPT_DEVICE: a->device = (int)strtol(arg, &end, 10); break;
+        case OPT_WCSR: a->write_csr = arg; break;
         case ARGP_KEY_ARG: return 0;
         default: return ARGP_ERR_UNKNOWN;
     }
@@ -152,6 +154,13 @@ int main(int argc, char **argv) {
     int m = 0, n = 0, nnz = 0;
     CHECK(hhp_mat_shape(A, &m, &n, &nnz));
     printf("Matrix name : %s\n", a.input_matrix);
+    if (a.write_csr) {  /* the matrix as read (before any --perm), for binary re-reads with -m */
+        int *rp = malloc(sizeof(int) * ((size_t)m + 1)), *cl = malloc(sizeof(int) * (size_t)(nnz > 0 ? nnz : 1));
+        double *vl = malloc(sizeof(double) * (size_t)(nnz > 0 ? nnz : 1));
+        CHECK(hhp_mat_get_csr(A, rp, cl, vl));
+        CHECK(hhp_csr_file_write(a.write_csr, m, n, nnz, rp, cl, vl));
+        free(rp); free(cl); free(vl);
+    }
     if (m != n) FAIL("the matrix is %d x %d; BiCGStab needs a square matrix", m, n);
     double *X = malloc(sizeof(double) * (size_t)n), *B = malloc(sizeof(double) * (size_t)m);
     double *XT = NULL;

@@ -9,7 +9,14 @@
 //   '%' comment lines, then "M N nz", then nz triplets "i j v", 1-based;
 //   rows in order, entries of a row in file order, duplicates kept (SpMV sums them).
 // Unlike the reference (fscanf, unchecked), short files and out-of-range indices are errors.
-// Parsing reads the whole file and converts with std::from_chars.
+// Parsing reads the whole file and converts with std::from_chars; large files are parsed by one
+// thread per core on line-aligned chunks, joined in file order (so the CSR is identical to the
+// serial parse), and any irregularity (a malformed entry, a count mismatch) re-parses serially
+// for the exact error message.
+//
+// Binary CSR files ("HHPCSR01" magic, then int64 m, n, nnz, then rowptr[m+1] and col[nnz] as
+// int32 and val[nnz] as FP64, little-endian) skip text parsing altogether: hhp_csr_file_write
+// stores a matrix once, and every reader that takes a Matrix Market path accepts them.
 #include <algorithm>
 #include <cctype>
 #include <charconv>
@@ -17,7 +24,13 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
+
+#include <fcntl.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
 
 #include "hhp_internal.h"
 
@@ -40,6 +53,42 @@ bool read_file(const char *path, std::string &buf) {
     std::fclose(f);
     return got == static_cast<size_t>(sz);
 }
+
+// A read-only view of a whole file: mapped from the page cache (no copy, no zero-fill of a
+// fresh buffer), or read into memory where mapping is not possible.
+struct FileView {
+    const char *data = nullptr;
+    size_t size = 0;
+    void *map = nullptr;
+    std::string copy;
+    FileView() = default;
+    FileView(const FileView &) = delete;
+    FileView &operator=(const FileView &) = delete;
+    ~FileView() {
+        if (map) munmap(map, size);
+    }
+    bool open(const char *path) {
+        const int fd = ::open(path, O_RDONLY);
+        if (fd >= 0) {
+            struct stat st;
+            if (fstat(fd, &st) == 0 && st.st_size > 0) {
+                void *m = mmap(nullptr, static_cast<size_t>(st.st_size), PROT_READ, MAP_PRIVATE, fd, 0);
+                if (m != MAP_FAILED) {
+                    map = m;
+                    data = static_cast<const char *>(m);
+                    size = static_cast<size_t>(st.st_size);
+                    ::close(fd);
+                    return true;
+                }
+            }
+            ::close(fd);
+        }
+        if (!read_file(path, copy)) return false;
+        data = copy.data();
+        size = copy.size();
+        return true;
+    }
+};
 
 struct Cursor {
     const char *p, *e;
@@ -66,15 +115,197 @@ std::string lower(std::string s) {
 
 }  // namespace
 
-// Parses a Matrix Market file into host CSR arrays.
+namespace {
+
+constexpr char kCsrMagic[8] = {'H', 'H', 'P', 'C', 'S', 'R', '0', '1'};
+
+// One thread's entries of a line-aligned chunk, in file order.
+struct EntryChunk {
+    std::vector<int> ri, ci;
+    std::vector<double> vv;
+    bool ok = true;        // every triplet in the chunk parsed and in range
+    bool sorted = true;    // rows non-decreasing inside the chunk
+};
+
+void parse_chunk(const char *p, const char *e, long long M, long long N, EntryChunk &out) {
+    const size_t guess = static_cast<size_t>(e - p) / 24 + 16;
+    out.ri.reserve(guess);
+    out.ci.reserve(guess);
+    out.vv.reserve(guess);
+    Cursor c{p, e};
+    int last = -1;
+    for (;;) {
+        c.skip_ws();
+        if (c.p >= c.e) return;
+        long long i = 0, j = 0;
+        double v = 0.0;
+        if (!c.num(i) || !c.num(j) || !c.num(v) || i < 1 || i > M || j < 1 || j > N) {
+            out.ok = false;
+            return;
+        }
+        const int r = static_cast<int>(i - 1);
+        if (r < last) out.sorted = false;
+        last = r;
+        out.ri.push_back(r);
+        out.ci.push_back(static_cast<int>(j - 1));
+        out.vv.push_back(v);
+    }
+}
+
+// Parallel parse of the entry section [p, e) into CSR; false if the serial path must run (a
+// malformed or out-of-range entry, or a count other than nnz).
+bool parse_entries_parallel(const char *p, const char *e, long long M, long long N, int nnz, int m,
+                            std::vector<int> &rowptr, std::vector<int> &col, std::vector<double> &val) {
+    const size_t bytes = static_cast<size_t>(e - p);
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int T = static_cast<int>(std::min<size_t>(std::min(hw, 64u), bytes / (4u << 20)));
+    if (T < 2) return false;
+    std::vector<const char *> cut(static_cast<size_t>(T) + 1);
+    cut[0] = p;
+    cut[static_cast<size_t>(T)] = e;
+    for (int t = 1; t < T; ++t) {
+        const char *q = p + bytes * static_cast<size_t>(t) / static_cast<size_t>(T);
+        const char *nl = static_cast<const char *>(std::memchr(q, '\n', static_cast<size_t>(e - q)));
+        cut[static_cast<size_t>(t)] = nl ? nl + 1 : e;
+    }
+    std::vector<EntryChunk> ch(static_cast<size_t>(T));
+    std::vector<std::thread> th;
+    for (int t = 0; t < T; ++t)
+        th.emplace_back(parse_chunk, std::max(cut[static_cast<size_t>(t)], cut[0]),
+                        std::max(cut[static_cast<size_t>(t) + 1], cut[static_cast<size_t>(t)]), M, N,
+                        std::ref(ch[static_cast<size_t>(t)]));
+    for (auto &x : th) x.join();
+    long long total = 0;
+    bool sorted = true;
+    int prev_last = -1;
+    for (const auto &c : ch) {
+        if (!c.ok) return false;
+        total += static_cast<long long>(c.ri.size());
+        if (!c.sorted || (!c.ri.empty() && c.ri.front() < prev_last)) sorted = false;
+        if (!c.ri.empty()) prev_last = c.ri.back();
+    }
+    if (total != nnz) return false;
+    rowptr.assign(static_cast<size_t>(m) + 1, 0);
+    col.resize(static_cast<size_t>(nnz));
+    val.resize(static_cast<size_t>(nnz));
+    if (sorted) {
+        // row counts: each chunk's rows form a range that meets its neighbours' only at the ends,
+        // so the chunks count their own rows in parallel and only boundary rows are merged
+        std::vector<std::thread> cnt;
+        std::vector<std::vector<int>> edge(static_cast<size_t>(T));  // {first row, its count, last row, its count}
+        for (int t = 0; t < T; ++t)
+            cnt.emplace_back([&, t] {
+                const EntryChunk &c = ch[static_cast<size_t>(t)];
+                if (c.ri.empty()) return;
+                const int first = c.ri.front(), last = c.ri.back();
+                int nf = 0, nl = 0;
+                for (int r : c.ri) {
+                    if (r == first) ++nf;
+                    else if (r == last) ++nl;
+                    else rowptr[static_cast<size_t>(r) + 1]++;  // interior rows belong to this chunk alone
+                }
+                edge[static_cast<size_t>(t)] = {first, nf, last, nl};
+            });
+        for (auto &x : cnt) x.join();
+        for (const auto &eg : edge) {
+            if (eg.empty()) continue;
+            rowptr[static_cast<size_t>(eg[0]) + 1] += eg[1];
+            if (eg[2] != eg[0]) rowptr[static_cast<size_t>(eg[2]) + 1] += eg[3];
+        }
+        for (int r = 0; r < m; ++r) rowptr[static_cast<size_t>(r) + 1] += rowptr[static_cast<size_t>(r)];
+        // rows in file order already: the CSR is the chunks' concatenation
+        std::vector<size_t> off(static_cast<size_t>(T) + 1, 0);
+        for (int t = 0; t < T; ++t) off[static_cast<size_t>(t) + 1] = off[static_cast<size_t>(t)] + ch[static_cast<size_t>(t)].ri.size();
+        std::vector<std::thread> cp;
+        for (int t = 0; t < T; ++t)
+            cp.emplace_back([&, t] {
+                const EntryChunk &c = ch[static_cast<size_t>(t)];
+                if (c.ci.empty()) return;
+                std::memcpy(col.data() + off[static_cast<size_t>(t)], c.ci.data(), sizeof(int) * c.ci.size());
+                std::memcpy(val.data() + off[static_cast<size_t>(t)], c.vv.data(), sizeof(double) * c.vv.size());
+            });
+        for (auto &x : cp) x.join();
+    } else {
+        // stable counting sort by row, chunks in file order: entries of a row keep file order
+        for (const auto &c : ch)
+            for (int r : c.ri) rowptr[static_cast<size_t>(r) + 1]++;
+        for (int r = 0; r < m; ++r) rowptr[static_cast<size_t>(r) + 1] += rowptr[static_cast<size_t>(r)];
+        std::vector<int> fill(rowptr.begin(), rowptr.end() - 1);
+        for (const auto &c : ch)
+            for (size_t k = 0; k < c.ri.size(); ++k) {
+                const int d = fill[static_cast<size_t>(c.ri[k])]++;
+                col[static_cast<size_t>(d)] = c.ci[k];
+                val[static_cast<size_t>(d)] = c.vv[k];
+            }
+    }
+    return true;
+}
+
+// Binary CSR file (see the file comment); false if `buf` does not start with the magic.
+bool is_csr_file(const FileView &buf) {
+    return buf.size >= sizeof(kCsrMagic) && std::memcmp(buf.data, kCsrMagic, sizeof(kCsrMagic)) == 0;
+}
+
+hhp_status parse_csr_file(const char *path, const FileView &buf, int &m, int &n, int &nnz,
+                          std::vector<int> &rowptr, std::vector<int> &col, std::vector<double> &val) {
+    long long h[3];
+    if (buf.size < sizeof(kCsrMagic) + sizeof(h)) {
+        set_error("'%s': truncated binary CSR header", path);
+        return HHP_ERR_FORMAT;
+    }
+    std::memcpy(h, buf.data + sizeof(kCsrMagic), sizeof(h));
+    if (h[0] < 0 || h[1] < 0 || h[2] < 0 || h[0] > 2147483646LL || h[1] > 2147483646LL || h[2] > 2147483646LL) {
+        set_error("'%s': binary CSR sizes out of range", path);
+        return HHP_ERR_FORMAT;
+    }
+    const size_t need = sizeof(kCsrMagic) + sizeof(h) + sizeof(int) * static_cast<size_t>(h[0] + 1) +
+                        (sizeof(int) + sizeof(double)) * static_cast<size_t>(h[2]);
+    if (buf.size != need) {
+        set_error("'%s': binary CSR file has %zu bytes, expected %zu", path, buf.size, need);
+        return HHP_ERR_FORMAT;
+    }
+    m = static_cast<int>(h[0]);
+    n = static_cast<int>(h[1]);
+    nnz = static_cast<int>(h[2]);
+    const char *q = buf.data + sizeof(kCsrMagic) + sizeof(h);
+    rowptr.resize(static_cast<size_t>(m) + 1);
+    col.resize(static_cast<size_t>(nnz));
+    val.resize(static_cast<size_t>(nnz));
+    std::memcpy(rowptr.data(), q, sizeof(int) * rowptr.size());
+    q += sizeof(int) * rowptr.size();
+    if (nnz) std::memcpy(col.data(), q, sizeof(int) * col.size());
+    q += sizeof(int) * col.size();
+    if (nnz) std::memcpy(val.data(), q, sizeof(double) * val.size());
+    // the same validity rules as a Matrix Market file: monotone row pointers, columns in range
+    if (rowptr[0] != 0 || rowptr[static_cast<size_t>(m)] != nnz) {
+        set_error("'%s': binary CSR row pointers do not span 0..nnz", path);
+        return HHP_ERR_FORMAT;
+    }
+    for (int r = 0; r < m; ++r)
+        if (rowptr[static_cast<size_t>(r) + 1] < rowptr[static_cast<size_t>(r)]) {
+            set_error("'%s': binary CSR row pointers decrease at row %d", path, r);
+            return HHP_ERR_FORMAT;
+        }
+    for (int k = 0; k < nnz; ++k)
+        if (col[static_cast<size_t>(k)] < 0 || col[static_cast<size_t>(k)] >= n) {
+            set_error("'%s': binary CSR column index %d out of range at entry %d", path, col[static_cast<size_t>(k)], k);
+            return HHP_ERR_FORMAT;
+        }
+    return HHP_OK;
+}
+
+}  // namespace
+
+// Parses a Matrix Market (or binary CSR) file into host CSR arrays.
 hhp_status read_mtx(const char *path, int &m, int &n, int &nnz, std::vector<int> &rowptr, std::vector<int> &col,
                     std::vector<double> &val) {
-    std::string buf;
-    if (!path || !read_file(path, buf)) {
+    FileView buf;
+    if (!path || !buf.open(path)) {
         set_error("cannot read matrix file '%s'", path ? path : "(null)");
         return HHP_ERR_IO;
     }
-    const char *p = buf.data(), *e = buf.data() + buf.size();
+    if (is_csr_file(buf)) return parse_csr_file(path, buf, m, n, nnz, rowptr, col, val);
+    const char *p = buf.data, *e = buf.data + buf.size;
     const char *eol = static_cast<const char *>(std::memchr(p, '\n', static_cast<size_t>(e - p)));
     std::string first(p, eol ? eol : e);
     char t[5][64];
@@ -112,6 +343,7 @@ hhp_status read_mtx(const char *path, int &m, int &n, int &nnz, std::vector<int>
     m = static_cast<int>(M);
     n = static_cast<int>(N);
     nnz = static_cast<int>(NZ);
+    if (parse_entries_parallel(c.p, c.e, M, N, nnz, m, rowptr, col, val)) return HHP_OK;
     std::vector<int> ri(static_cast<size_t>(nnz)), ci(static_cast<size_t>(nnz));
     std::vector<double> vv(static_cast<size_t>(nnz));
     rowptr.assign(static_cast<size_t>(m) + 1, 0);
@@ -223,3 +455,33 @@ extern "C" hhp_status hhp_mtx_read(const char *path, int *m, int *n, int *nnz, i
 }
 
 extern "C" void hhp_free(void *p) { std::free(p); }
+
+extern "C" hhp_status hhp_csr_file_write(const char *path, int m, int n, int nnz, const int *rowptr, const int *col,
+                                         const double *val) {
+    if (!path || m < 0 || n < 0 || nnz < 0 || !rowptr || (nnz > 0 && (!col || !val))) {
+        hhp::set_error("hhp_csr_file_write: invalid arguments");
+        return HHP_ERR_ARG;
+    }
+    if (rowptr[0] != 0 || rowptr[m] != nnz) {
+        hhp::set_error("hhp_csr_file_write: rowptr[0] must be 0 and rowptr[m] must equal nnz");
+        return HHP_ERR_ARG;
+    }
+    FILE *f = std::fopen(path, "wb");
+    if (!f) {
+        hhp::set_error("cannot write '%s'", path);
+        return HHP_ERR_IO;
+    }
+    const long long h[3] = {m, n, nnz};
+    bool ok = std::fwrite(hhp::kCsrMagic, 1, sizeof(hhp::kCsrMagic), f) == sizeof(hhp::kCsrMagic) &&
+              std::fwrite(h, sizeof(h), 1, f) == 1 &&
+              std::fwrite(rowptr, sizeof(int), static_cast<size_t>(m) + 1, f) == static_cast<size_t>(m) + 1;
+    if (ok && nnz > 0)
+        ok = std::fwrite(col, sizeof(int), static_cast<size_t>(nnz), f) == static_cast<size_t>(nnz) &&
+             std::fwrite(val, sizeof(double), static_cast<size_t>(nnz), f) == static_cast<size_t>(nnz);
+    if (std::fclose(f) != 0) ok = false;
+    if (!ok) {
+        hhp::set_error("write to '%s' failed", path);
+        return HHP_ERR_IO;
+    }
+    return HHP_OK;
+}

@@ -103,7 +103,9 @@ hhp_status hhp_mat_from_csr(hhp_ctx *ctx, int m, int n, int nnz, const int *rowp
 hhp_status hhp_mat_from_csr_dev(hhp_ctx *ctx, int m, int n, int nnz, const int *rowptr_dev, const int *col_dev,
                                 const double *val_dev, hhp_mat **out);
 /* Matrix Market coordinate real/integer general file (readMatrixMarketFromFile,
- * src/util/hhp_wrap_bora.c:13-104): rows in order, entries of a row in file order. */
+ * src/util/hhp_wrap_bora.c:13-104): rows in order, entries of a row in file order. Large files
+ * are parsed by all host cores (same result as a serial parse). A binary CSR file written by
+ * hhp_csr_file_write is accepted at the same path argument and loaded without text parsing. */
 hhp_status hhp_mat_from_mtx(hhp_ctx *ctx, const char *path, hhp_mat **out);
 void hhp_mat_destroy(hhp_mat *mat);
 hhp_status hhp_mat_shape(const hhp_mat *mat, int *m, int *n, int *nnz);
@@ -155,6 +157,11 @@ hhp_status hhp_vector_write(const char *path, int size, const double *v, int exa
  * are allocated with malloc (m+1, nnz, nnz); release each with hhp_free. */
 hhp_status hhp_mtx_read(const char *path, int *m, int *n, int *nnz, int **rowptr, int **col, double **val);
 void hhp_free(void *p);
+/* Binary CSR file for fast re-reads (the reference re-parses text on every run,
+ * src/util/hhp_wrap_bora.c:13-104): "HHPCSR01", int64 m, n, nnz, int32 rowptr[m+1], int32
+ * col[nnz], FP64 val[nnz], little-endian. Read back by hhp_mtx_read / hhp_mat_from_mtx. */
+hhp_status hhp_csr_file_write(const char *path, int m, int n, int nnz, const int *rowptr, const int *col,
+                              const double *val);
 
 /* ---- host-side helpers exposed for testing the work plan without a GPU ---------------------- */
 /* The SpMV work plan of a host CSR (rows_per_lane 2 = the FP64 kernel's slices of 64 rows, 4 =

@@ -24,10 +24,6 @@ def _files(td, g):
         np.savetxt(paths[key], g[key], fmt="%.17g")
     paths["A"] = os.path.join(td, "A.mtx")
     open(paths["A"], "w").write(str(g["mtx_text"]))
-    if "perm" in g:
-        parts = np.zeros(g["rowptr"].size - 1, np.int64)
-        # rebuild a two-part vector consistent with the stored permutation order
-        paths["part"] = os.path.join(td, "part.txt")
     return paths
 
 
@@ -75,6 +71,20 @@ def test_cli_partition_permutation():
         out = os.path.join(td, "X.txt")
         kv, _ = _run(["-m", p["A"], "-x", p["x0"], "-y", p["b"], "-o", out, "--perm", part, "--out-format", "exact"])
         assert np.max(np.abs(np.loadtxt(out) - np.arange(1, 17))) < 1e-8
+
+
+def test_cli_binary_csr_rerun_matches_text_run():
+    g = load_golden("sample320")
+    with tempfile.TemporaryDirectory() as td:
+        p = _files(td, g)
+        csr = os.path.join(td, "A.csr")
+        out1, out2 = os.path.join(td, "X1.txt"), os.path.join(td, "X2.txt")
+        kv1, _ = _run(["-m", p["A"], "-x", p["x0"], "-y", p["b"], "-o", out1, "-n", "200", "--out-format", "exact",
+                       "--write-csr", csr])
+        assert os.path.getsize(csr) == 8 + 24 + 4 * (320 + 1) + 12 * int(g["rowptr"][-1])
+        kv2, _ = _run(["-m", csr, "-x", p["x0"], "-y", p["b"], "-o", out2, "-n", "200", "--out-format", "exact"])
+        assert kv1["n_iters"] == kv2["n_iters"] and kv1["relative_residual"] == kv2["relative_residual"]
+        assert open(out1).read() == open(out2).read()
 
 
 def _d(a):

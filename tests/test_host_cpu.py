@@ -94,6 +94,99 @@ def test_integer_field_and_blank_comment_lines():
     assert shape == (2, 2) and rp.tolist() == [0, 1, 2] and col.tolist() == [1, 0] and val.tolist() == [-4.0, 3.0]
 
 
+def _big_mtx(td, rows, cols, vals, m, n, name="big.mtx"):
+    """A Matrix Market file large enough (> 8 MB) for the parallel parse."""
+    path = os.path.join(td, name)
+    with open(path, "w") as f:
+        f.write("%%MatrixMarket matrix coordinate real general\n%% big\n")
+        f.write(f"{m} {n} {rows.size}\n")
+        np.savetxt(f, np.column_stack([rows + 1, cols + 1, vals]), fmt="%d %d %.17g")
+    assert os.path.getsize(path) > 9 << 20
+    return path
+
+
+def _expected_csr(rows, cols, vals, m):
+    """CSR with rows ordered and the entries of each row in file order (duplicates kept)."""
+    order = np.argsort(rows, kind="stable")
+    rp = np.zeros(m + 1, np.int64)
+    np.add.at(rp, rows + 1, 1)
+    return np.cumsum(rp).astype(np.int32), cols[order].astype(np.int32), vals[order]
+
+
+@pytest.mark.parametrize("sorted_rows", [True, False])
+def test_parallel_reader_equals_file_order_csr(sorted_rows):
+    rng = np.random.default_rng(11)
+    m, n, nz = 60_000, 50_000, 420_000
+    rows = np.sort(rng.integers(0, m, nz)) if sorted_rows else rng.integers(0, m, nz)
+    cols = rng.integers(0, n, nz)
+    cols[5:9] = cols[4]  # duplicates of one entry in a row
+    rows[5:9] = rows[4]
+    vals = rng.standard_normal(nz)
+    with tempfile.TemporaryDirectory() as td:
+        path = _big_mtx(td, rows, cols, vals, m, n)
+        rp, col, val, shape = hhp.mtx_read(path)
+        erp, ecol, eval_ = _expected_csr(rows, cols, vals, m)
+        assert shape == (m, n)
+        assert np.array_equal(rp, erp) and np.array_equal(col, ecol) and np.array_equal(val, eval_)
+        # the binary CSR file reads back to the same arrays through the same entry point
+        bpath = os.path.join(td, "big.csr")
+        hhp.csr_file_write(bpath, rp, col, val, n)
+        brp, bcol, bval, bshape = hhp.mtx_read(bpath)
+        assert bshape == (m, n) and np.array_equal(brp, rp) and np.array_equal(bcol, col) and np.array_equal(bval, val)
+
+
+def test_parallel_reader_errors_match_serial():
+    rng = np.random.default_rng(12)
+    m, n, nz = 60_000, 60_000, 420_000
+    rows, cols, vals = np.sort(rng.integers(0, m, nz)), rng.integers(0, n, nz), rng.standard_normal(nz)
+    with tempfile.TemporaryDirectory() as td:
+        path = _big_mtx(td, rows, cols, vals, m, n)
+        text = open(path).read().split("\n")
+        bad = list(text)
+        bad[3 + 300_000] = "1 x 2.0"  # entry 300001 malformed
+        p1 = os.path.join(td, "bad.mtx")
+        open(p1, "w").write("\n".join(bad))
+        with pytest.raises(hhp.HHPError) as e:
+            hhp.mtx_read(p1)
+        assert e.value.status == 8 and "entry 300001" in str(e.value)
+        short = text[:3 + 200_000]  # 200000 of 420000 entries
+        p2 = os.path.join(td, "short.mtx")
+        open(p2, "w").write("\n".join(short) + "\n")
+        with pytest.raises(hhp.HHPError) as e:
+            hhp.mtx_read(p2)
+        assert e.value.status == 8 and "entry 200001" in str(e.value)
+        big_row = list(text)
+        big_row[3 + 123_456] = f"{m + 1} 1 1.0"
+        p3 = os.path.join(td, "range.mtx")
+        open(p3, "w").write("\n".join(big_row))
+        with pytest.raises(hhp.HHPError) as e:
+            hhp.mtx_read(p3)
+        assert e.value.status == 8 and "outside" in str(e.value)
+
+
+def test_binary_csr_file_rejects_corruption():
+    rp = np.array([0, 2, 3], np.int32)
+    col = np.array([0, 1, 1], np.int32)
+    val = np.array([1.0, 2.0, 3.0])
+    with tempfile.TemporaryDirectory() as td:
+        p = os.path.join(td, "a.csr")
+        hhp.csr_file_write(p, rp, col, val, 2)
+        raw = open(p, "rb").read()
+        open(p, "wb").write(raw[:-8])  # truncated
+        with pytest.raises(hhp.HHPError) as e:
+            hhp.mtx_read(p)
+        assert e.value.status == 8
+        cut = bytearray(raw)
+        cut[32 + 12 + 4] = 9  # column index 9 in a 2-column matrix
+        open(p, "wb").write(bytes(cut))
+        with pytest.raises(hhp.HHPError) as e:
+            hhp.mtx_read(p)
+        assert e.value.status == 8
+    with pytest.raises(hhp.HHPError) as e:
+        hhp.csr_file_write(os.path.join("/nonexistent", "a.csr"), rp, col, val, 2)
+    assert e.value.status == 2
+
+
 def test_vector_files_roundtrip_and_short_file():
     v = np.array([1.0, -2.5, 1.0 / 3.0, 1e-300, 12345.678901234567])
     with tempfile.TemporaryDirectory() as td:
@@ -119,13 +212,14 @@ def _check_plan(rp, rpl, cap):
     covered = np.zeros(m, np.int64)
     placed = rows[rows >= 0]
     np.add.at(covered, placed, 1)
-    assert np.all(lens[placed] <= hhp.plan_stats(rp, rpl, cap)["padding"] * 0 + lens.max())
+    assert np.all(lens[placed] <= 256)  # slices hold rows up to the long-row threshold
     # long rows: chunks cover [rp[r], rp[r+1]) contiguously, in order, each at most cap entries
     long_rows = sorted(set(chunks[:, 0].tolist())) if chunks.size else []
     for r in long_rows:
         ch = chunks[chunks[:, 0] == r]
         assert ch[0, 2] == rp[r] and ch[-1, 3] == rp[r + 1]
         assert np.all(ch[1:, 2] == ch[:-1, 3]) and np.all(ch[:, 3] - ch[:, 2] <= cap) and np.all(ch[:, 3] > ch[:, 2])
+        assert lens[r] > 256  # only rows past the threshold are cut into chunks
         covered[r] += 1
     assert np.all(covered == 1), np.nonzero(covered != 1)[0][:10]
     if chunks.size:
