@@ -33,6 +33,7 @@ class SolveOpts(ctypes.Structure):
         ("print_every", ctypes.c_int),
         ("cb", ITER_CB),
         ("user", ctypes.c_void_p),
+        ("precond", ctypes.c_int),
     ]
 
 

@@ -193,8 +193,12 @@ class SolveResult:
         return self.status == 0
 
 
-def _opts(rtol, maxit, precision, inner_rtol, max_outer, fixed_iters, print_every, cb) -> SolveOpts:
+PRECONDS = {"none": 0, "jacobi": 1}
+
+
+def _opts(rtol, maxit, precision, inner_rtol, max_outer, fixed_iters, print_every, cb, precond="none") -> SolveOpts:
     o = SolveOpts()
+    o.precond = PRECONDS[precond] if isinstance(precond, str) else int(precond)
     o.rtol = rtol
     o.maxit = maxit
     o.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
@@ -210,7 +214,7 @@ def _opts(rtol, maxit, precision, inner_rtol, max_outer, fixed_iters, print_ever
 def bicgstab(ctx: Context, A: Matrix, b, x=None, x_target=None, *, rtol: float = 1e-10, maxit: int = 2000,
              precision: str = "fp64", inner_rtol: float = 0.1, max_outer: int = 50, fixed_iters: bool = False,
              record_history: bool = False, callback: Optional[Callable[[int, float], None]] = None,
-             print_every: int = 1, raise_on_error: bool = True):
+             print_every: int = 1, raise_on_error: bool = True, precond: str = "none"):
     """Solves A x = b. Host numpy arrays use hhp_bicgstab (copies in/out); CUDA tensors use
     hhp_bicgstab_dev. x is the initial guess (zeros if None) and is overwritten for tensors.
     Returns (x, SolveResult)."""
@@ -223,7 +227,8 @@ def bicgstab(ctx: Context, A: Matrix, b, x=None, x_target=None, *, rtol: float =
 
     want_cb = record_history or callback is not None
     cfun = ITER_CB(_cb) if want_cb else None
-    o = _opts(rtol, maxit, precision, inner_rtol, max_outer, fixed_iters, print_every if want_cb else 0, cfun)
+    o = _opts(rtol, maxit, precision, inner_rtol, max_outer, fixed_iters, print_every if want_cb else 0, cfun,
+              precond)
     info = SolveInfo()
     if _is_dev(b):
         import torch

@@ -29,11 +29,11 @@
 
 #include "hhp_gpu.h"
 
-enum { OPT_RTOL = 1000, OPT_FIXED, OPT_PREC, OPT_XT, OPT_PERM, OPT_PRINT, OPT_OUTFMT, OPT_DEVICE, OPT_WCSR };
+enum { OPT_RTOL = 1000, OPT_FIXED, OPT_PREC, OPT_XT, OPT_PERM, OPT_PRINT, OPT_OUTFMT, OPT_DEVICE, OPT_WCSR, OPT_PRECOND };
 
 struct arguments {
     char *input_matrix, *input_x, *input_y, *output_x, *x_target, *perm, *write_csr;
-    int n_iters, fixed, mixed, print_every, exact, device;
+    int n_iters, fixed, mixed, print_every, exact, device, jacobi;
     double rtol;
 };
 
@@ -52,6 +52,7 @@ static struct argp_option options[] = {
     {"out-format", OPT_OUTFMT, "compat|exact", 0, "Number format of the output X file", 0},
     {"device", OPT_DEVICE, "ID", 0, "CUDA device (default 0)", 0},
     {"write-csr", OPT_WCSR, "FILE", 0, "Also store the matrix as a binary CSR file (later runs: -m FILE)", 0},
+    {"precond", OPT_PRECOND, "none|jacobi", 0, "Preconditioner (default none, as the reference)", 0},
     {0}};
 
 static error_t parse_opt(int key, char *arg, struct argp_state *state) {
@@ -80,6 +81,11 @@ static error_t parse_opt(int key, char *arg, struct argp_state *state) {
             break;
         case OPT_DEVICE: a->device = (int)strtol(arg, &end, 10); break;
         case OPT_WCSR: a->write_csr = arg; break;
+        case OPT_PRECOND:
+            if (strcmp(arg, "jacobi") == 0) a->jacobi = 1;
+            else if (strcmp(arg, "none") == 0) a->jacobi = 0;
+            else argp_error(state, "unknown preconditioner '%s'", arg);
+            break;
         case ARGP_KEY_ARG: return 0;
         default: return ARGP_ERR_UNKNOWN;
     }
@@ -200,6 +206,7 @@ int main(int argc, char **argv) {
     o.maxit = a.n_iters;
     o.precision = a.mixed ? HHP_PREC_MIXED : HHP_PREC_FP64;
     o.inner_rtol = 0.1;
+    o.precond = a.jacobi ? HHP_PRECOND_JACOBI : HHP_PRECOND_NONE;
     o.fixed_iters = a.fixed;
     o.print_every = a.print_every;
     o.cb = a.print_every > 0 ? print_iter : NULL;

@@ -319,6 +319,7 @@ void hhp_mat_destroy(hhp_mat *A) {
     if (!A) return;
     if (A->ctx && A->ctx->stream) cudaStreamSynchronize(A->ctx->stream);
     if (A->t) hhp_mat_destroy(A->t);
+    release_jacobi(A);
     solver_release(A->solver);
     A->plan64.release();
     A->plan32.release();
@@ -348,6 +349,7 @@ static hhp_status set_values(hhp_mat *A, const double *v, cudaMemcpyKind kind) {
         HHP_CUDA(cudaMemcpyAsync(A->val, v, sizeof(double) * static_cast<size_t>(A->nnz), kind, A->ctx->stream));
     if (A->val32 || A->t || A->plan64.built() || A->plan32.built()) HHP_TRY(mat_refresh_derived(A));
     HHP_CUDA(cudaStreamSynchronize(A->ctx->stream));
+    release_jacobi(A);  // rebuilt from the new values on the next preconditioned solve
     return HHP_OK;
 }
 
@@ -444,8 +446,10 @@ static hhp_status check_solve(hhp_ctx *ctx, hhp_mat *A, const void *b, const voi
         set_error("bicgstab: the matrix must be square and non-empty (got %d x %d)", A->m, A->n);
         return HHP_ERR_ARG;
     }
-    if (o && (o->maxit < 0 || !(o->rtol >= 0.0) || (o->precision != HHP_PREC_FP64 && o->precision != HHP_PREC_MIXED))) {
-        set_error("bicgstab: invalid options (maxit %d, rtol %g, precision %d)", o->maxit, o->rtol, o->precision);
+    if (o && (o->maxit < 0 || !(o->rtol >= 0.0) || (o->precision != HHP_PREC_FP64 && o->precision != HHP_PREC_MIXED) ||
+              (o->precond != HHP_PRECOND_NONE && o->precond != HHP_PRECOND_JACOBI))) {
+        set_error("bicgstab: invalid options (maxit %d, rtol %g, precision %d, precond %d)", o->maxit, o->rtol,
+                  o->precision, o->precond);
         return HHP_ERR_ARG;
     }
     return HHP_OK;
@@ -455,6 +459,7 @@ hhp_status hhp_bicgstab(hhp_ctx *ctx, hhp_mat *A, const double *b, double *x, co
                         const hhp_solve_opts *opts, hhp_solve_info *info) {
     HHP_TRY(check_solve(ctx, A, b, x, opts));
     const hhp_solve_opts o = opts ? *opts : default_opts();
+    if (o.precond == HHP_PRECOND_JACOBI) return solve_jacobi(A, b, x, xt, &o, info, true);
     return solve_any(A, b, x, xt, &o, info, true);
 }
 
@@ -462,6 +467,7 @@ hhp_status hhp_bicgstab_dev(hhp_ctx *ctx, hhp_mat *A, const double *b, double *x
                             const hhp_solve_opts *opts, hhp_solve_info *info) {
     HHP_TRY(check_solve(ctx, A, b, x, opts));
     const hhp_solve_opts o = opts ? *opts : default_opts();
+    if (o.precond == HHP_PRECOND_JACOBI) return solve_jacobi(A, b, x, xt, &o, info, false);
     return solve_any(A, b, x, xt, &o, info, false);
 }
 

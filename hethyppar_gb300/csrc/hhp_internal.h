@@ -104,6 +104,10 @@ struct hhp_mat {
     int *t_map = nullptr;             // t_map[p] = index in A of A^T's entry p
     int *rowidx = nullptr;            // row of each stored entry (built with the transpose)
     hhp::Solver *solver = nullptr;    // FP64/mixed workspace for A (A^T's lives in t->solver)
+    // Jacobi preconditioning (lazily built): A with column j scaled by 1/a_jj, and 1/diag(A)
+    hhp_mat *jac = nullptr;
+    double *dinv = nullptr;
+    std::vector<double> dinv_host;
 };
 
 namespace hhp {
@@ -138,6 +142,11 @@ inline hhp_status solve_dev(hhp_mat *A, const double *b, double *x, const double
     return solve_any(A, b, x, xt, o, info, false);
 }
 void solver_release(Solver *s);
+// Jacobi (right) preconditioning: builds A->jac / A->dinv; solves through A->jac (hhp_precond.cu).
+hhp_status ensure_jacobi(hhp_mat *A);
+void release_jacobi(hhp_mat *A);
+hhp_status solve_jacobi(hhp_mat *A, const double *b, double *x, const double *xt, const hhp_solve_opts *o,
+                        hhp_solve_info *info, bool host);
 // Adjoint: lambda = A^-T g; dlda[k] = -lambda[row(k)] * x[col(k)].
 hhp_status backward_dev(hhp_mat *A, const double *x_dev, const double *g_dev, double *dldb_dev, double *dlda_dev,
                         const hhp_solve_opts *o, hhp_solve_info *info);

@@ -46,6 +46,12 @@ typedef void (*hhp_iter_cb)(int iter, double rel_res, void *user);
 
 typedef enum { HHP_PREC_FP64 = 0, HHP_PREC_MIXED = 1 } hhp_precision;
 
+/* Preconditioner. JACOBI: right preconditioning with M = diag(A) (the diagonal form of the ILU path
+ * left commented out in gpu_BiCGStab, src/entry/bicgstab_gpu.c:185-201, 238-254): BiCGStab runs on
+ * A M^-1 (a column-scaled copy of A built once per matrix) and x = M^-1 y; the stop test and the
+ * reported residual are those of A x = b. Needs a nonzero diagonal (HHP_ERR_ARG otherwise). */
+typedef enum { HHP_PRECOND_NONE = 0, HHP_PRECOND_JACOBI = 1 } hhp_precond;
+
 typedef struct {
     double rtol;        /* stop when ||b - A x|| <= rtol * ||b|| (the relative residual the reference
                            prints, bicgstab_cpu.c:251-255; equal to gpu_BiCGStab's threshold
@@ -61,6 +67,7 @@ typedef struct {
     int print_every;    /* callback stride; 0 = no callback                                       */
     hhp_iter_cb cb;
     void *user;
+    int precond;        /* hhp_precond (forward solves; the adjoint runs unpreconditioned)        */
 } hhp_solve_opts;
 
 typedef struct {
