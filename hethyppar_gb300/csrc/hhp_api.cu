@@ -51,7 +51,7 @@ const Tuning &tuning() {
         d.spmv_unroll = env_int("HHP_SPMV_UNROLL", d.spmv_unroll);
         d.rpl64 = env_int("HHP_SPMV_RPL64", d.rpl64);
         d.rpl32 = env_int("HHP_SPMV_RPL32", d.rpl32);
-        d.stream_hint = env_int("HHP_SPMV_HINT", d.stream_hint);
+        d.d16 = env_int("HHP_SPMV_D16", d.d16);
         return d;
     }();
     return t;

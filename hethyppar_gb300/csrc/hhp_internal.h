@@ -53,7 +53,7 @@ void assign_units(const SellHost &P, int n_warps, std::vector<int> &warp_ptr, st
 
 struct PlanDev {
     int rpl = 0, H = 0, n_slices = 0, n_long = 0, n_chunks = 0, ctas = 0, warps_per_cta = 0, unroll = 4;
-    bool has_perm = false, sorted = false;
+    bool has_perm = false, sorted = false, d16 = false;  // d16: 16-bit column offsets (scol16)
     long long total = 0;
     double padding = 1.0;
     long long *slice_ptr = nullptr;   // n_slices + 1
@@ -63,7 +63,8 @@ struct PlanDev {
     int *warp_units = nullptr;        // unit ids (slice s < n_slices, else chunk n_slices + c)
     double imbalance = 1.0;           // max warp cost / mean warp cost
     void *sval = nullptr;             // total values (double or float), padding zero
-    int *scol = nullptr;              // total column indices
+    int *scol = nullptr;              // total column indices (when !d16)
+    short *scol16 = nullptr;          // total offsets col - row (when d16)
     int4 *chunks = nullptr;
     int *long_first = nullptr, *chunk_long = nullptr;
     double *chunk_part = nullptr;     // n_chunks
@@ -167,9 +168,9 @@ inline int pad4(int n) { return (n + 3) & ~3; }
 
 // Kernel tuning knobs (environment overrides read once).
 struct Tuning {
-    // ctas_per_sm, spmv_unroll, rpl64: 0 = chosen per matrix at plan time; stream_hint -1: by type
+    // ctas_per_sm, spmv_unroll, rpl64: 0 = chosen per matrix at plan time; d16 0: never 16-bit offsets
     int cap = 2048, long_thr = 256, window = 8192, wpc = 8, ctas_per_sm = 0, vec_blocks_per_sm = 1,
-        unroll_iters = 2, spmv_unroll = 0, rpl64 = 0, rpl32 = 4, stream_hint = -1;
+        unroll_iters = 2, spmv_unroll = 0, rpl64 = 0, rpl32 = 4, d16 = 1;
 };
 const Tuning &tuning();
 

@@ -39,74 +39,62 @@ namespace {
 
 constexpr int kChunkUnroll = 4;
 
-// A lane's words of one slice step: the values (V) and column indices (I) of its R rows, each
-// read with one load (8 or 16 bytes; 32 lanes make one contiguous request).
+// A lane's words of one slice step: the values (V) and column indices (I: int32 columns; I16:
+// 16-bit offsets col - row) of its R rows, each read with one load (32 lanes make one contiguous
+// request).
 template <typename VT, int R>
 struct Vec;
 template <>
 struct Vec<double, 1> {
     using V = double;
     using I = int;
+    using I16 = short;
 };
 template <>
 struct Vec<double, 2> {
     using V = double2;
     using I = int2;
+    using I16 = short2;
 };
 template <>
 struct Vec<float, 2> {
     using V = float2;
     using I = int2;
+    using I16 = short2;
 };
 template <>
 struct Vec<float, 4> {
     using V = float4;
     using I = int4;
+    using I16 = short4;
 };
 
-// Loads of the matrix streams (slice values and indices, chunk CSR ranges) with a cache policy:
-//   HINT 0: the read-only path (ld.global.nc), default caching;
-//   HINT 1: not allocated in L1 (leaves L1 to the x gathers), L2 evict-first (the stream does
-//           not push the solver's vectors out of L2);
-//   HINT 2: not allocated in L1, L2 evict-last (the matrix tends to stay in L2 across launches);
-//   HINT 3: not allocated in L1, default L2 policy.
-template <int HINT>
-__device__ __forceinline__ uint64_t stream_policy() {
-    uint64_t pol = 0;
-    if (HINT == 1) asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
-    if (HINT == 2) asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
-    return pol;
-}
-
-template <int HINT, typename T>
-__device__ __forceinline__ T ld_stream(const T *p, uint64_t pol) {
-    static_assert(sizeof(T) == 4 || sizeof(T) == 8 || sizeof(T) == 16, "4, 8 or 16 bytes");
-    if (HINT == 0) return __ldg(p);
+// Loads of the matrix streams (slice values and indices, chunk CSR ranges). FP64 matrices are not
+// allocated in L1 (ld.global.nc.L1::no_allocate: L1 stays with the x gathers; measured faster in
+// the FP64 solves); FP32 ones take the default read-only path (their solves measured slower
+// without L1 allocation).
+template <typename VT, typename T>
+__device__ __forceinline__ T ld_stream(const T *p) {
+    static_assert(sizeof(T) == 2 || sizeof(T) == 4 || sizeof(T) == 8 || sizeof(T) == 16, "2 to 16 bytes");
+    if (!std::is_same<VT, double>::value) return __ldg(p);
     T out;
-    if (sizeof(T) == 4) {
+    if (sizeof(T) == 2) {
+        unsigned short r;
+        asm volatile("ld.global.nc.L1::no_allocate.b16 %0, [%1];" : "=h"(r) : "l"(p));
+        memcpy(&out, &r, 2);
+    } else if (sizeof(T) == 4) {
         uint32_t r;
-        if (HINT == 3) asm volatile("ld.global.nc.L1::no_allocate.b32 %0, [%1];" : "=r"(r) : "l"(p));
-        else asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(r) : "l"(p), "l"(pol));
+        asm volatile("ld.global.nc.L1::no_allocate.b32 %0, [%1];" : "=r"(r) : "l"(p));
         memcpy(&out, &r, 4);
     } else if (sizeof(T) == 8) {
         uint32_t r[2];
-        if (HINT == 3)
-            asm volatile("ld.global.nc.L1::no_allocate.v2.b32 {%0, %1}, [%2];" : "=r"(r[0]), "=r"(r[1]) : "l"(p));
-        else
-            asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.b32 {%0, %1}, [%2], %3;"
-                         : "=r"(r[0]), "=r"(r[1])
-                         : "l"(p), "l"(pol));
+        asm volatile("ld.global.nc.L1::no_allocate.v2.b32 {%0, %1}, [%2];" : "=r"(r[0]), "=r"(r[1]) : "l"(p));
         memcpy(&out, r, 8);
     } else {
         uint32_t r[4];
-        if (HINT == 3)
-            asm volatile("ld.global.nc.L1::no_allocate.v4.b32 {%0, %1, %2, %3}, [%4];"
-                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                         : "l"(p));
-        else
-            asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.b32 {%0, %1, %2, %3}, [%4], %5;"
-                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                         : "l"(p), "l"(pol));
+        asm volatile("ld.global.nc.L1::no_allocate.v4.b32 {%0, %1, %2, %3}, [%4];"
+                     : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                     : "l"(p));
         memcpy(&out, r, 16);
     }
     return out;
@@ -120,7 +108,8 @@ struct SellArgs {
     const int *warp_ptr;
     const int *warp_units;
     const VT *sval;
-    const int *scol;
+    const int *scol;       // int32 columns, or
+    const short *scol16;   // 16-bit offsets col - row (plans whose every |col - row| < 2^15)
     const VT *csr_val;  // CSR values (FP64, or the FP32 copy) for long-row chunks
     const int *csr_col;
     const int4 *chunks;
@@ -176,22 +165,36 @@ __device__ __forceinline__ void row_epilogue(const SellArgs<VT> &a, int r, VT ac
     }
 }
 
-template <typename VT, int R, int U, int EP, int HINT>
-__device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, int lane, double &d0, double &d1,
-                                         uint64_t pol) {
+template <typename VT, int R, int U, int EP, bool D16>
+__device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, int lane, double &d0, double &d1) {
     using VV = typename Vec<VT, R>::V;
     using IV = typename Vec<VT, R>::I;
+    using CW = typename std::conditional<D16, typename Vec<VT, R>::I16, IV>::type;  // index word
+    using CT = typename std::conditional<D16, short, int>::type;
     constexpr int H = 32 * R;
     const long long base = a.slice_ptr[s];
     // the slice's longest row: every lane walks this many steps (uniform across the warp)
     const int wmax = static_cast<int>((a.slice_ptr[s + 1] - base) / H);
     const int q0 = s * H + lane * R;
     const IV lv = *reinterpret_cast<const IV *>(a.pos_len + q0);
-    int len[R];
+    int len[R], row[R];
 #pragma unroll
     for (int t = 0; t < R; ++t) len[t] = comp<IV, int>(lv, t);
+    if (a.has_perm) {
+        const IV rv = *reinterpret_cast<const IV *>(a.pos_row + q0);
+#pragma unroll
+        for (int t = 0; t < R; ++t) row[t] = comp<IV, int>(rv, t);
+    } else {
+#pragma unroll
+        for (int t = 0; t < R; ++t) row[t] = q0 + t;
+    }
+    // column of row t's entry in an index word: stored, or the row plus a 16-bit offset
+    auto colof = [&](const CW &w, int t) -> int {
+        return D16 ? row[t] + static_cast<int>(comp<CW, CT>(w, t)) : static_cast<int>(comp<CW, CT>(w, t));
+    };
     const VV *vp = reinterpret_cast<const VV *>(a.sval + base) + lane;
-    const IV *cp = reinterpret_cast<const IV *>(a.scol + base) + lane;
+    const CW *cp = D16 ? reinterpret_cast<const CW *>(a.scol16 + base) + lane
+                       : reinterpret_cast<const CW *>(a.scol + base) + lane;
     VT acc[R];
 #pragma unroll
     for (int t = 0; t < R; ++t) acc[t] = VT(0);
@@ -202,27 +205,27 @@ __device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, int lane,
     // after the loop: a multiply-add predicated off still occupies GB300's FP64 pipe for a full
     // warp slot, so no group is ever padded with dead steps.
     VV v[U];
-    IV c[U];
+    CW c[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-        v[u] = u < wmax ? ld_stream<HINT>(vp + static_cast<size_t>(u) * 32, pol) : VV();
-        c[u] = u < wmax ? ld_stream<HINT>(cp + static_cast<size_t>(u) * 32, pol) : IV();
+        v[u] = u < wmax ? ld_stream<VT>(vp + static_cast<size_t>(u) * 32) : VV();
+        c[u] = u < wmax ? ld_stream<VT>(cp + static_cast<size_t>(u) * 32) : CW();
     }
     int j = 0;
     for (; j + U <= wmax; j += U) {
         VV vn[U];
-        IV cn[U];
+        CW cn[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const int jn = j + U + u;
-            vn[u] = jn < wmax ? ld_stream<HINT>(vp + static_cast<size_t>(jn) * 32, pol) : VV();
-            cn[u] = jn < wmax ? ld_stream<HINT>(cp + static_cast<size_t>(jn) * 32, pol) : IV();
+            vn[u] = jn < wmax ? ld_stream<VT>(vp + static_cast<size_t>(jn) * 32) : VV();
+            cn[u] = jn < wmax ? ld_stream<VT>(cp + static_cast<size_t>(jn) * 32) : CW();
         }
         VT xv[U][R];
 #pragma unroll
         for (int u = 0; u < U; ++u)
 #pragma unroll
-            for (int t = 0; t < R; ++t) xv[u][t] = (j + u < len[t]) ? __ldg(a.x + comp<IV, int>(c[u], t)) : VT(0);
+            for (int t = 0; t < R; ++t) xv[u][t] = (j + u < len[t]) ? __ldg(a.x + colof(c[u], t)) : VT(0);
 #pragma unroll
         for (int u = 0; u < U; ++u)
 #pragma unroll
@@ -234,14 +237,14 @@ __device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, int lane,
             c[u] = cn[u];
         }
     }
-    // tail steps (their values and indices were requested by the last prefetch: L1 hits)
+    // tail steps, one at a time (their words were requested by the last prefetch)
 #pragma unroll 1
     for (; j < wmax; ++j) {
-        const VV vt = ld_stream<HINT>(vp + static_cast<size_t>(j) * 32, pol);
-        const IV ct = ld_stream<HINT>(cp + static_cast<size_t>(j) * 32, pol);
+        const VV vt = ld_stream<VT>(vp + static_cast<size_t>(j) * 32);
+        const CW ct = ld_stream<VT>(cp + static_cast<size_t>(j) * 32);
         VT xt[R];
 #pragma unroll
-        for (int t = 0; t < R; ++t) xt[t] = (j < len[t]) ? __ldg(a.x + comp<IV, int>(ct, t)) : VT(0);
+        for (int t = 0; t < R; ++t) xt[t] = (j < len[t]) ? __ldg(a.x + colof(ct, t)) : VT(0);
 #pragma unroll
         for (int t = 0; t < R; ++t)
             if (j < len[t]) acc[t] = vfma(comp<VV, VT>(vt, t), xt[t], acc[t]);
@@ -249,8 +252,7 @@ __device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, int lane,
     VT e0 = VT(0), e1 = VT(0);
 #pragma unroll
     for (int t = 0; t < R; ++t) {
-        const int p = q0 + t;
-        const int r = a.has_perm ? a.pos_row[p] : p;
+        const int r = row[t];
         if (r >= 0 && r < a.m) row_epilogue<VT, EP>(a, r, acc[t], e0, e1);
     }
     if (EP != EP_AXPBY && EP != EP_Y) {
@@ -259,8 +261,8 @@ __device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, int lane,
     }
 }
 
-template <typename VT, int EP, int HINT>
-__device__ __forceinline__ void do_chunk(const SellArgs<VT> &a, int c, int lane, uint64_t pol) {
+template <typename VT, int EP>
+__device__ __forceinline__ void do_chunk(const SellArgs<VT> &a, int c, int lane) {
     const int4 d = __ldg(&a.chunks[c]);
     VT acc = VT(0);
     for (int k = d.z + lane; k < d.w; k += 32 * kChunkUnroll) {
@@ -269,8 +271,8 @@ __device__ __forceinline__ void do_chunk(const SellArgs<VT> &a, int c, int lane,
 #pragma unroll
         for (int u = 0; u < kChunkUnroll; ++u) {
             const int kk = k + 32 * u;
-            v[u] = kk < d.w ? ld_stream<HINT>(a.csr_val + kk, pol) : VT(0);
-            cc[u] = kk < d.w ? ld_stream<HINT>(a.csr_col + kk, pol) : 0;
+            v[u] = kk < d.w ? ld_stream<VT>(a.csr_val + kk) : VT(0);
+            cc[u] = kk < d.w ? ld_stream<VT>(a.csr_col + kk) : 0;
         }
 #pragma unroll
         for (int u = 0; u < kChunkUnroll; ++u) xv[u] = (k + 32 * u < d.w) ? __ldg(a.x + cc[u]) : VT(0);
@@ -307,7 +309,7 @@ struct MinCtas {
     static constexpr int value = R * U >= 8 ? 3 : (R * U >= 4 ? 5 : 6);
 };
 
-template <typename VT, int R, int U, int EP, int HINT>
+template <typename VT, int R, int U, int EP, bool D16>
 __global__ void __launch_bounds__(256, MinCtas<R, U>::value) k_spmv(const SellArgs<VT> a) {
     // After a recorded device error every later launch returns at once (uniform across the grid).
     if (*reinterpret_cast<volatile const int *>(a.err) != DEV_OK) return;
@@ -318,11 +320,10 @@ __global__ void __launch_bounds__(256, MinCtas<R, U>::value) k_spmv(const SellAr
     double d0 = 0.0, d1 = 0.0;
     // this warp's units, balanced at plan time (fixed order: reductions are reproducible)
     const int ub = a.warp_ptr[gw], ue = a.warp_ptr[gw + 1];
-    const uint64_t pol = stream_policy<HINT>();
     for (int i = ub; i < ue; ++i) {
         const int u = __ldg(a.warp_units + i);
-        if (u < a.n_slices) do_slice<VT, R, U, EP, HINT>(a, u, lane, d0, d1, pol);
-        else do_chunk<VT, EP, HINT>(a, u - a.n_slices, lane, pol);
+        if (u < a.n_slices) do_slice<VT, R, U, EP, D16>(a, u, lane, d0, d1);
+        else do_chunk<VT, EP>(a, u - a.n_slices, lane);
     }
     if (EP != EP_AXPBY && EP != EP_Y) {
         // per-CTA partial: each warp folds its lanes' (d0, d1) with a transposed butterfly
@@ -342,32 +343,24 @@ __global__ void __launch_bounds__(256, MinCtas<R, U>::value) k_spmv(const SellAr
     }
 }
 
-template <typename VT, int R, int U, int HINT>
-cudaError_t launch_ruh(EpKind ep, const PlanDev &p, const SellArgs<VT> &a, cudaStream_t s) {
+template <typename VT, int R, int U, bool D16>
+cudaError_t launch_rud(EpKind ep, const PlanDev &p, const SellArgs<VT> &a, cudaStream_t s) {
     const dim3 grid(p.ctas), block(p.warps_per_cta * 32);
     switch (ep) {
-        case EP_DOT1: return launch_k(k_spmv<VT, R, U, EP_DOT1, HINT>, grid, block, 0, s, a);
-        case EP_DOT2: return launch_k(k_spmv<VT, R, U, EP_DOT2, HINT>, grid, block, 0, s, a);
-        case EP_RESID: return launch_k(k_spmv<VT, R, U, EP_RESID, HINT>, grid, block, 0, s, a);
+        case EP_DOT1: return launch_k(k_spmv<VT, R, U, EP_DOT1, D16>, grid, block, 0, s, a);
+        case EP_DOT2: return launch_k(k_spmv<VT, R, U, EP_DOT2, D16>, grid, block, 0, s, a);
+        case EP_RESID: return launch_k(k_spmv<VT, R, U, EP_RESID, D16>, grid, block, 0, s, a);
         default:
             // y = A x needs no epilogue arithmetic: a separate instantiation keeps the FP64 pipe
             // free of predicated-off scale and accumulate instructions
-            if (!a.scale && !a.accum) return launch_k(k_spmv<VT, R, U, EP_Y, HINT>, grid, block, 0, s, a);
-            return launch_k(k_spmv<VT, R, U, EP_AXPBY, HINT>, grid, block, 0, s, a);
+            if (!a.scale && !a.accum) return launch_k(k_spmv<VT, R, U, EP_Y, D16>, grid, block, 0, s, a);
+            return launch_k(k_spmv<VT, R, U, EP_AXPBY, D16>, grid, block, 0, s, a);
     }
 }
 
-// Stream loads: FP64 matrices skip L1 (measured faster in the FP64 solves: L1 stays with the x
-// gathers), FP32 ones keep the default (their solves measured slower without L1 allocation).
 template <typename VT, int R, int U>
 cudaError_t launch_ru(EpKind ep, const PlanDev &p, const SellArgs<VT> &a, cudaStream_t s) {
-    const int h = tuning().stream_hint;
-    switch (h >= 0 ? h : (std::is_same<VT, double>::value ? 3 : 0)) {
-        case 1: return launch_ruh<VT, R, U, 1>(ep, p, a, s);
-        case 2: return launch_ruh<VT, R, U, 2>(ep, p, a, s);
-        case 3: return launch_ruh<VT, R, U, 3>(ep, p, a, s);
-        default: return launch_ruh<VT, R, U, 0>(ep, p, a, s);
-    }
+    return p.d16 ? launch_rud<VT, R, U, true>(ep, p, a, s) : launch_rud<VT, R, U, false>(ep, p, a, s);
 }
 
 // Rows per lane come from the plan, the unroll from the tuning (2 or 4 steps in flight per lane).
@@ -387,7 +380,8 @@ cudaError_t launch_ep(EpKind ep, const PlanDev &p, const SellArgs<VT> &a, cudaSt
 template <typename VT>
 __global__ void k_sell_fill(const int *__restrict__ rowptr, const int *__restrict__ col, const double *__restrict__ val,
                             const int *__restrict__ pos_row, const int *__restrict__ pos_len,
-                            const long long *__restrict__ slice_ptr, int H, long long npos, VT *sval, int *scol) {
+                            const long long *__restrict__ slice_ptr, int H, long long npos, VT *sval, int *scol,
+                            short *scol16) {
     for (long long p = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; p < npos;
          p += static_cast<long long>(gridDim.x) * blockDim.x) {
         const int r = pos_row[p], len = pos_len[p];
@@ -396,8 +390,26 @@ __global__ void k_sell_fill(const int *__restrict__ rowptr, const int *__restric
         const long long dst = slice_ptr[s] + q;
         const int src = rowptr[r];
         for (int j = 0; j < len; ++j) {
-            sval[dst + static_cast<long long>(j) * H] = static_cast<VT>(val[src + j]);
-            if (scol) scol[dst + static_cast<long long>(j) * H] = col[src + j];
+            const long long d = dst + static_cast<long long>(j) * H;
+            sval[d] = static_cast<VT>(val[src + j]);
+            if (scol) scol[d] = col[src + j];
+            if (scol16) scol16[d] = static_cast<short>(col[src + j] - r);
+        }
+    }
+}
+
+// bad[0] = 1 if some entry of a row with at most long_thr entries has |col - row| >= 2^15.
+__global__ void k_offsets_fit(const int *__restrict__ rowptr, const int *__restrict__ col, int m, int long_thr,
+                              int *bad) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
+        const int b = rowptr[r], e = rowptr[r + 1];
+        if (e - b > long_thr) continue;  // long rows are read from the CSR
+        for (int k = b; k < e; ++k) {
+            const int d = col[k] - r;
+            if (d > 32767 || d < -32767) {
+                *bad = 1;
+                break;
+            }
         }
     }
 }
@@ -418,7 +430,7 @@ hhp_status fill_values(hhp_mat *A, PlanDev &p, bool with_cols) {
     const int grid = static_cast<int>(std::min<long long>((npos + 255) / 256, 8LL * A->ctx->num_sms));
     k_sell_fill<VT><<<grid, 256, 0, A->ctx->stream>>>(A->rowptr, A->col, A->val, p.pos_row, p.pos_len, p.slice_ptr,
                                                       p.H, npos, static_cast<VT *>(p.sval),
-                                                      with_cols ? p.scol : nullptr);
+                                                      with_cols ? p.scol : nullptr, with_cols ? p.scol16 : nullptr);
     HHP_CUDA(cudaGetLastError());
     return HHP_OK;
 }
@@ -478,8 +490,29 @@ hhp_status build_plan_dev(hhp_mat *A, PlanDev &p) {
     const size_t tot = static_cast<size_t>(std::max<long long>(h.total, 1));
     HHP_CUDA(cudaMalloc(&p.sval, tot * sizeof(VT)));
     HHP_CUDA(cudaMemset(p.sval, 0, tot * sizeof(VT)));
-    HHP_CUDA(cudaMalloc(&p.scol, tot * sizeof(int)));
-    HHP_CUDA(cudaMemset(p.scol, 0, tot * sizeof(int)));
+    // Index words: 16-bit offsets col - row when every slice row's entries lie within 2^15 of
+    // the diagonal (stencils: 2 bytes per nonzero instead of 4), else int32 columns.
+    p.d16 = false;
+    if (t.d16 && A->m > 0 && A->nnz > 0) {
+        int *bad = nullptr, hbad = 0;
+        HHP_CUDA(cudaMalloc(&bad, sizeof(int)));
+        cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream);
+        const int g = static_cast<int>(std::min<long long>((A->m + 255) / 256, 8LL * ctx->num_sms));
+        k_offsets_fit<<<g, 256, 0, ctx->stream>>>(A->rowptr, A->col, A->m, std::max(t.long_thr, 1), bad);
+        const cudaError_t e1 = cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+        const cudaError_t e2 = cudaStreamSynchronize(ctx->stream);
+        cudaFree(bad);
+        HHP_CUDA(e1);
+        HHP_CUDA(e2);
+        p.d16 = hbad == 0;
+    }
+    if (p.d16) {
+        HHP_CUDA(cudaMalloc(&p.scol16, tot * sizeof(short)));
+        HHP_CUDA(cudaMemset(p.scol16, 0, tot * sizeof(short)));
+    } else {
+        HHP_CUDA(cudaMalloc(&p.scol, tot * sizeof(int)));
+        HHP_CUDA(cudaMemset(p.scol, 0, tot * sizeof(int)));
+    }
     HHP_CUDA(cudaMalloc(&p.chunk_part, sizeof(double) * std::max(1, p.n_chunks)));
     HHP_CUDA(cudaMalloc(&p.long_cnt, sizeof(unsigned) * std::max(1, p.n_long)));
     HHP_CUDA(cudaMemset(p.long_cnt, 0, sizeof(unsigned) * std::max(1, p.n_long)));
@@ -503,6 +536,7 @@ SellArgs<VT> make_args(hhp_mat *A, const PlanDev &p, const VT *csr_val, const VT
     a.warp_units = p.warp_units;
     a.sval = static_cast<const VT *>(p.sval);
     a.scol = p.scol;
+    a.scol16 = p.scol16;
     a.csr_val = csr_val;
     a.csr_col = A->col;
     a.chunks = p.chunks;
@@ -538,6 +572,7 @@ void PlanDev::release() {
     cudaFree(warp_units);
     cudaFree(sval);
     cudaFree(scol);
+    cudaFree(scol16);
     cudaFree(chunks);
     cudaFree(long_first);
     cudaFree(chunk_long);
