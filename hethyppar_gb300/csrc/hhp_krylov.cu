@@ -66,7 +66,7 @@ struct Solver {
     DevScal *h_sc = nullptr, *h_sc32 = nullptr;        // pinned host mirrors
     double *hist = nullptr;
     int hist_cap = 0;
-    cudaStream_t s2 = nullptr;
+    cudaStream_t s2 = nullptr, s3 = nullptr;  // capture streams: loop body, IF body
     cudaGraphExec_t g64 = nullptr, gmix = nullptr;
     int g64_kernels_pro = 0, g64_kernels_epi = 0, gmix_kernels_pro = 0, gmix_kernels_epi = 0, unroll = 4;
 };
@@ -178,6 +178,21 @@ __global__ void __launch_bounds__(512) k_init(DevScal *sc, const T *R, T *R0, T 
     }
 }
 
+// K_P's stop tests on the previous step, then beta. Returns ST_RUNNING (beta set) or the terminal
+// status (an earlier terminal status is kept).
+__device__ __forceinline__ int step_p(int status, int iter, int it0, int maxit, double thr2, double rho_new, double rr,
+                                      double ss, double rho_prev, double alpha, double omega, bool dev_error,
+                                      double &beta) {
+    if (status != ST_RUNNING) return status;
+    if (dev_error) return ST_DEVICE_ERROR;
+    if (thr2 >= 0.0 && iter > it0 && ss <= thr2) return ST_CONVERGED_HALF;
+    if (thr2 >= 0.0 && rr <= thr2) return ST_CONVERGED;
+    if (iter >= maxit) return ST_MAXIT;
+    if (!finite_nonzero(rho_new) || !isfinite(rr)) return ST_BREAKDOWN;
+    beta = (rho_new / rho_prev) * (alpha / omega);
+    return ST_RUNNING;
+}
+
 // Scalar work (divisions, tests) is done once per block by thread 0 and broadcast through shared
 // memory: on GB300 an FP64 division is a sequence of FP64 instructions on the slowest pipe, so
 // evaluating the scalar recurrence in every thread would cost more than the vector update.
@@ -218,11 +233,9 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
             // raw ||r||^2: the host forms sqrt(rr / rr0), keeping FP64 sqrt and division off the
             // loop's critical path
             if (lead && iter > it0 && iter - 1 < hist_cap) hist[iter - 1] = rr;
-            if (*reinterpret_cast<volatile const int *>(dev_err) != DEV_OK) term = ST_DEVICE_ERROR;
-            else if (thr2 >= 0.0 && iter > it0 && ss <= thr2) term = ST_CONVERGED_HALF;
-            else if (thr2 >= 0.0 && rr <= thr2) term = ST_CONVERGED;
-            else if (iter >= sc->maxit) term = ST_MAXIT;
-            else if (!finite_nonzero(rho_new) || !isfinite(rr)) term = ST_BREAKDOWN;
+            double beta = 0.0;
+            term = step_p(st, iter, it0, sc->maxit, thr2, rho_new, rr, ss, sc->rho_prev, sc->alpha, sc->omega,
+                          *reinterpret_cast<volatile const int *>(dev_err) != DEV_OK, beta);
             if (term != ST_RUNNING) {
                 if (lead) {
                     sc->status = term;
@@ -230,7 +243,6 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
                     if (use_cond) cudaGraphSetConditional(cond, 0);
                 }
             } else {
-                const double beta = (rho_new / sc->rho_prev) * (sc->alpha / sc->omega);
                 bc[0] = beta;
                 bc[1] = -sc->omega;
                 if (lead) {
@@ -479,47 +491,98 @@ __global__ void __launch_bounds__(512) k_mix_init(DevScal *sc, const double *Rd,
 // (a factor 1e5 in the norm: BiCGStab's residual peaks stay far below it when it converges).
 constexpr double kDivergence2 = 1e10;
 
-// After K_XR: decide whether this iteration ends with an FP64 update; if so x += d, d = 0.
-__global__ void __launch_bounds__(512) k_ru_check(DevScal *sc, double *X, float *D32, int nu4,
-                                                  const double *part_xr32, int nparts) {
+// Mixed form, after K_XR: the reliable-update test fused with K_P. The FP32 residual triggers an
+// FP64 update when it has dropped by delta since the last one (or looks converged, or the budget
+// is spent). Without an update this kernel is K_P (stop tests, beta, p update) and clears the IF
+// condition; with one it folds d into x (x += d, d = 0) and sets the IF condition, whose body runs
+// the FP64 residual, the residual replacement and K_P. Iterations without an update so launch no
+// kernel for it. An FP32 residual that has grown far above the last true residual (or is not
+// finite) means the FP32 recurrences came apart: the pass ends as a breakdown with d not folded.
+__global__ void __launch_bounds__(512) k_p_ru(DevScal *sc, double *X, float *D32, float *P, const float *V,
+                                              const float *R, int nu4, const double *part_xr,
+                                              const double *part_s, int nparts, double *hist, int hist_cap,
+                                              cudaGraphConditionalHandle wcond, cudaGraphConditionalHandle icond,
+                                              int first_in_body, const int *dev_err) {
     __shared__ double red[kRedScratch];
-    __shared__ int go;
-    double v[2];
-    reduce_partials<2>(part_xr32, nparts, nullptr, 0, v, red);
+    __shared__ float bc[2];
+    __shared__ int go;  // 0: nothing, 1: p update, 2: fold d into x
+    double v[2], w[2];
+    reduce_pair<2>(part_xr, nparts, nullptr, 0, part_s, nparts, v, w, red);
     if (threadIdx.x == 0) {
-        int update = 0;
-        if (sc->status == ST_RUNNING) {
-            const double rr = v[1];
+        const bool lead = blockIdx.x == 0;
+        const double rho_new = v[0], rr = v[1];
+        const int st = sc->status;
+        int what = 0;
+        if (lead && first_in_body) sc->bodies += 1;
+        if (st == ST_RUNNING) {
             const int it = sc->iter;
             const double mx = sc->rr_max[it & 1];
-            // An FP32 recursive residual that has grown far above the true residual of the last
-            // update (or is not finite) means the FP32 recurrences have come apart: its increment
-            // is not folded into x, and the solve ends this pass as a breakdown (the host restarts
-            // it from x).
             if (!isfinite(rr) || rr > kDivergence2 * sc->true_rr) {
-                if (blockIdx.x == 0) sc->status = ST_BREAKDOWN;
+                if (lead) sc->status = ST_BREAKDOWN;  // d is not folded into x
+            } else if (rr <= sc->thr2 || rr < sc->inner_rtol2 * mx || it >= sc->maxit) {
+                if (lead) {
+                    sc->rr_max[(it + 1) & 1] = mx;
+                    sc->ru_flag = 1;
+                }
+                what = 2;
             } else {
-                update = rr <= sc->thr2 || rr < sc->inner_rtol2 * mx || it >= sc->maxit;
-                if (blockIdx.x == 0) sc->rr_max[(it + 1) & 1] = update ? mx : fmax(mx, rr);
+                if (lead) sc->rr_max[(it + 1) & 1] = fmax(mx, rr);
+                const int it0 = sc->iter_start;
+                if (lead && it > it0 && it - 1 < hist_cap) hist[it - 1] = rr;
+                double beta = 0.0;
+                const int term = step_p(st, it, it0, sc->maxit, sc->thr2_rec, rho_new, rr, w[0], sc->rho_prev,
+                                        sc->alpha, sc->omega, *reinterpret_cast<volatile const int *>(dev_err) != DEV_OK,
+                                        beta);
+                if (term != ST_RUNNING) {
+                    if (lead) {
+                        sc->status = term;
+                        sc->rr_last = rr;
+                    }
+                } else {
+                    bc[0] = static_cast<float>(beta);
+                    bc[1] = static_cast<float>(-sc->omega);
+                    if (lead) {
+                        sc->rho_cur = rho_new;
+                        sc->beta = beta;
+                        sc->rr_last = rr;
+                    }
+                    what = 1;
+                }
             }
         }
-        if (blockIdx.x == 0) sc->ru_flag = update;
-        go = update;
+        if (lead) {
+            cudaGraphSetConditional(icond, what == 2 ? 1u : 0u);
+            if (what == 0) cudaGraphSetConditional(wcond, 0);
+        }
+        go = what;
     }
     __syncthreads();
-    if (!go) return;
-    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu4; u += gridDim.x * blockDim.x) {
-        const float4 d = reinterpret_cast<const float4 *>(D32)[u];
-        double2 a = reinterpret_cast<double2 *>(X)[2 * u];
-        double2 b = reinterpret_cast<double2 *>(X)[2 * u + 1];
-        a.x += static_cast<double>(d.x);
-        a.y += static_cast<double>(d.y);
-        b.x += static_cast<double>(d.z);
-        b.y += static_cast<double>(d.w);
-        reinterpret_cast<double2 *>(X)[2 * u] = a;
-        reinterpret_cast<double2 *>(X)[2 * u + 1] = b;
-        reinterpret_cast<float4 *>(D32)[u] = z;
+    const int stride = gridDim.x * blockDim.x;
+    if (go == 1) {
+        const float tb = bc[0], tw = bc[1];
+        for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu4; u += stride) {
+            float p[4], vv[4], r[4];
+            ldu(p, P, u);
+            ldu(vv, V, u);
+            ldu(r, R, u);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) p[e] = fmaf(tb, fmaf(tw, vv[e], p[e]), r[e]);
+            stu(P, u, p);
+        }
+    } else if (go == 2) {
+        const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu4; u += stride) {
+            const float4 d = reinterpret_cast<const float4 *>(D32)[u];
+            double2 a = reinterpret_cast<double2 *>(X)[2 * u];
+            double2 b = reinterpret_cast<double2 *>(X)[2 * u + 1];
+            a.x += static_cast<double>(d.x);
+            a.y += static_cast<double>(d.y);
+            b.x += static_cast<double>(d.z);
+            b.y += static_cast<double>(d.w);
+            reinterpret_cast<double2 *>(X)[2 * u] = a;
+            reinterpret_cast<double2 *>(X)[2 * u + 1] = b;
+            reinterpret_cast<float4 *>(D32)[u] = z;
+        }
     }
 }
 
@@ -624,7 +687,8 @@ hhp_status ensure_solver(hhp_mat *A, Solver **out, int maxit) {
         s->sc32 = dalloc<DevScal>(1, st);
         if (st == HHP_OK && cudaMallocHost(&s->h_sc, sizeof(DevScal)) != cudaSuccess) st = HHP_ERR_OOM;
         if (st == HHP_OK && cudaMallocHost(&s->h_sc32, sizeof(DevScal)) != cudaSuccess) st = HHP_ERR_OOM;
-        if (st == HHP_OK && cudaStreamCreateWithFlags(&s->s2, cudaStreamNonBlocking) != cudaSuccess)
+        if (st == HHP_OK && (cudaStreamCreateWithFlags(&s->s2, cudaStreamNonBlocking) != cudaSuccess ||
+                             cudaStreamCreateWithFlags(&s->s3, cudaStreamNonBlocking) != cudaSuccess))
             st = HHP_ERR_CUDA;
         A->solver = s;
         if (st != HHP_OK) return st;
@@ -704,6 +768,46 @@ hhp_status end_loop_body(Solver *s, hhp_status rc) {
     return HHP_OK;
 }
 
+// An IF node's handle in the graph being captured on `stream` (the loop body); its value starts
+// at 0 at every launch of that body and K_P_RU sets it.
+hhp_status make_cond_if(cudaStream_t stream, cudaGraphConditionalHandle *cond) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    HHP_CUDA(cudaStreamGetCaptureInfo(stream, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+    HHP_CUDA(cudaGraphConditionalHandleCreate(cond, g, 0, cudaGraphCondAssignDefault));
+    return HHP_OK;
+}
+
+// Adds an IF node on `cond` after the work captured so far on s->s2, makes later work on s->s2
+// depend on it, and captures its body on s->s3 (ended by end_if_body).
+hhp_status begin_if_body(Solver *s, cudaGraphConditionalHandle cond) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t nd = 0;
+    HHP_CUDA(cudaStreamGetCaptureInfo(s->s2, &cs, nullptr, &g, &deps, nullptr, &nd));
+    cudaGraphNodeParams cp = {};
+    memset(&cp, 0, sizeof(cp));
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = cond;
+    cp.conditional.type = cudaGraphCondTypeIf;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cn;
+    HHP_CUDA(cudaGraphAddNode(&cn, g, deps, nullptr, nd, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    HHP_CUDA(cudaStreamUpdateCaptureDependencies(s->s2, &cn, nullptr, 1, cudaStreamSetCaptureDependencies));
+    HHP_CUDA(cudaStreamBeginCaptureToGraph(s->s3, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    return HHP_OK;
+}
+
+hhp_status end_if_body(Solver *s, hhp_status rc) {
+    cudaGraph_t body_out = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s->s3, &body_out);
+    if (rc != HHP_OK) return rc;
+    HHP_CUDA(e);
+    return HHP_OK;
+}
+
 // The FP64 (or FP32-inner) iteration loop as graph nodes on `stream`: the first K_P (stop tests
 // on the initial residual) before a WHILE node whose body holds `unroll` iterations, each
 // [SpMV + r0.v, K_S, SpMV + t.s/t.t, K_XR, (mixed: update check, gated FP64 residual, residual
@@ -751,22 +855,30 @@ hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R,
             st = HHP_ERR_CUDA;
             break;
         }
-        if (fp32) {
-            // reliable update: decide, gated FP64 residual, gated residual replacement
-            if (launch_k(k_ru_check, dim3(s->nblk), dim3(s->nthr), 0, s->s2, s->sc32, s->X, s->D32, nu4,
-                         s->part_xr32, s->nblk) != cudaSuccess) {
-                st = HHP_ERR_CUDA;
-                break;
-            }
-            st = launch_spmv64(A, s->s2, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0, &s->sc32->ru_flag);
-            if (st != HHP_OK) break;
-            if (launch_k(k_ru_apply, dim3(s->nblk), dim3(s->nthr), 0, s->s2, s->sc32, s->Y, s->R32, s->R0_32, nu4,
-                         parts_of(A->plan64), s->part_xr32) != cudaSuccess) {
-                st = HHP_ERR_CUDA;
-                break;
-            }
+        if (!fp32) {
+            st = kp(s->s2, cond, k == 0 ? 1 : 0);
+            continue;
         }
-        st = kp(s->s2, cond, k == 0 ? 1 : 0);
+        // reliable update: the update test fused with K_P, then IF(update) { FP64 residual,
+        // residual replacement, K_P }
+        cudaGraphConditionalHandle icond;
+        st = make_cond_if(s->s2, &icond);
+        if (st != HHP_OK) break;
+        if (launch_k(k_p_ru, dim3(s->nblk), dim3(s->nthr), 0, s->s2, s->sc32, s->X, s->D32, s->P32, s->V32, s->R32,
+                     nu4, s->part_xr32, s->part_s32, s->nblk, s->hist, s->hist_cap, cond, icond, k == 0 ? 1 : 0,
+                     A->ctx->dev_err) != cudaSuccess) {
+            st = HHP_ERR_CUDA;
+            break;
+        }
+        st = begin_if_body(s, icond);
+        if (st != HHP_OK) break;
+        st = launch_spmv64(A, s->s3, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0);
+        if (st == HHP_OK &&
+            launch_k(k_ru_apply, dim3(s->nblk), dim3(s->nthr), 0, s->s3, s->sc32, s->Y, s->R32, s->R0_32, nu4,
+                     parts_of(A->plan64), s->part_xr32) != cudaSuccess)
+            st = HHP_ERR_CUDA;
+        if (st == HHP_OK) st = kp(s->s3, cond, 0);
+        st = end_if_body(s, st);
     }
     return end_loop_body(s, st);
 }
@@ -1013,10 +1125,13 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
         h32.first_outer = 1;
         for (int pass = 0; pass < 2; ++pass) {
             h32.restart = pass > 0 ? 1 : 0;
+            const int upd0 = pass > 0 ? h32.updates : 0;
             HHP_CUDA(cudaGraphLaunch(s->gmix, st));
             HHP_CUDA(cudaMemcpyAsync(s->h_sc32, s->sc32, sizeof(DevScal), cudaMemcpyDeviceToHost, st));
             HHP_CUDA(cudaStreamSynchronize(st));
-            ctx->kernel_launches += s->gmix_kernels_pro + s->gmix_kernels_epi + 8LL * s->unroll * h32.bodies;
+            // 5 kernels per iteration, 3 more per FP64 update (the IF body)
+            ctx->kernel_launches += s->gmix_kernels_pro + s->gmix_kernels_epi + 5LL * s->unroll * h32.bodies +
+                                    3LL * (h32.updates - upd0);
             // an inner breakdown or divergence after some progress restarts the FP32 recurrences
             // once from the last FP64 iterate (its true residual becomes the new shadow
             // residual); a second one hands the solve to FP64 below
@@ -1103,6 +1218,7 @@ void solver_release(Solver *s) {
     cudaFreeHost(s->h_sc);
     cudaFreeHost(s->h_sc32);
     if (s->s2) cudaStreamDestroy(s->s2);
+    if (s->s3) cudaStreamDestroy(s->s3);
     delete s;
 }
 
