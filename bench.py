@@ -384,6 +384,8 @@ def run_ours(args, rk):
                                       "L = 1/2||x - x_t||^2, forward and adjoint to true rel-res 1e-12",
                           "forward_s": tf, "adjoint_s": ta, "fwd_plus_adj_s": tf + ta, "ratio_total_to_forward":
                           (tf + ta) / tf, "forward_iters": rf.iters, "adjoint_iters": ra.iters,
+                          "rel_res_true_forward": rf.rel_res_true, "rel_res_true_adjoint": ra.rel_res_true,
+                          "adjoint_passes": ra.outer_iters, "adjoint_status": ra.status,
                           "note": "transpose built once beforehand (not in the timed adjoint); ratio_to_fp64_forward "
                                   "= (FP64 forward + mixed adjoint) / FP64 forward"}
         try:

@@ -193,6 +193,9 @@ __device__ __forceinline__ int step_p(int status, int iter, int it0, int maxit, 
     return ST_RUNNING;
 }
 
+// Vector units per thread whose operands the vector kernels request before their reductions.
+constexpr int kPre = 4;
+
 // Scalar work (divisions, tests) is done once per block by thread 0 and broadcast through shared
 // memory: on GB300 an FP64 division is a sequence of FP64 instructions on the slowest pipe, so
 // evaluating the scalar recurrence in every thread would cost more than the vector update.
@@ -207,14 +210,18 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
     __shared__ double bc[2];
     __shared__ int go;
     constexpr int E = Unit<T>::E;
-    const int stride = gridDim.x * blockDim.x;
-    int u = blockIdx.x * blockDim.x + threadIdx.x;
-    // the first unit's operands are requested before the reductions: their latency overlaps them
-    T p[E], vv[E], r[E];
-    if (u < nu) {
-        ldu(p, P, u);
-        ldu(vv, V, u);
-        ldu(r, R, u);
+    const int stride = gridDim.x * blockDim.x, u0 = blockIdx.x * blockDim.x + threadIdx.x;
+    // the operands of the thread's first kPre units are requested before the reductions: their
+    // latency overlaps the reductions and the scalar step
+    T p[kPre][E], vv[kPre][E], r[kPre][E];
+#pragma unroll
+    for (int k = 0; k < kPre; ++k) {
+        const int u = u0 + k * stride;
+        if (u < nu) {
+            ldu(p[k], P, u);
+            ldu(vv[k], V, u);
+            ldu(r[k], R, u);
+        }
     }
     double v[2], w[2];
     reduce_pair<2>(part_xr, nparts, nullptr, 0, part_s, nparts, v, w, red);
@@ -257,16 +264,23 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
     __syncthreads();
     if (!go) return;
     const T tb = static_cast<T>(bc[0]), tw = static_cast<T>(bc[1]);
-    while (u < nu) {
 #pragma unroll
-        for (int e = 0; e < E; ++e) p[e] = tfma(tb, tfma(tw, vv[e], p[e]), r[e]);
-        stu(P, u, p);
-        u += stride;
+    for (int k = 0; k < kPre; ++k) {
+        const int u = u0 + k * stride;
         if (u < nu) {
-            ldu(p, P, u);
-            ldu(vv, V, u);
-            ldu(r, R, u);
+#pragma unroll
+            for (int e = 0; e < E; ++e) p[k][e] = tfma(tb, tfma(tw, vv[k][e], p[k][e]), r[k][e]);
+            stu(P, u, p[k]);
         }
+    }
+    for (int u = u0 + kPre * stride; u < nu; u += stride) {
+        T pp[E], vx[E], rx[E];
+        ldu(pp, P, u);
+        ldu(vx, V, u);
+        ldu(rx, R, u);
+#pragma unroll
+        for (int e = 0; e < E; ++e) pp[e] = tfma(tb, tfma(tw, vx[e], pp[e]), rx[e]);
+        stu(P, u, pp);
     }
 }
 
@@ -278,12 +292,15 @@ __global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const 
     __shared__ double bc[1];
     __shared__ int go;
     constexpr int E = Unit<T>::E;
-    const int stride = gridDim.x * blockDim.x;
-    int u = blockIdx.x * blockDim.x + threadIdx.x;
-    T r[E], vv[E];
-    if (u < nu) {
-        ldu(r, R, u);
-        ldu(vv, V, u);
+    const int stride = gridDim.x * blockDim.x, u0 = blockIdx.x * blockDim.x + threadIdx.x;
+    T r[kPre][E], vv[kPre][E];
+#pragma unroll
+    for (int k = 0; k < kPre; ++k) {
+        const int u = u0 + k * stride;
+        if (u < nu) {
+            ldu(r[k], R, u);
+            ldu(vv[k], V, u);
+        }
     }
     double v[2];
     reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
@@ -310,17 +327,25 @@ __global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const 
     if (!go) return;
     const T ta = static_cast<T>(bc[0]);
     double acc[1] = {0.0};
-    while (u < nu) {
-        T s[E];
 #pragma unroll
-        for (int e = 0; e < E; ++e) s[e] = tfma(ta, vv[e], r[e]);
-        acc[0] = dunit<E>(acc[0], s, s);
-        stu(S, u, s);
-        u += stride;
+    for (int k = 0; k < kPre; ++k) {
+        const int u = u0 + k * stride;
         if (u < nu) {
-            ldu(r, R, u);
-            ldu(vv, V, u);
+            T sv[E];
+#pragma unroll
+            for (int e = 0; e < E; ++e) sv[e] = tfma(ta, vv[k][e], r[k][e]);
+            acc[0] = dunit<E>(acc[0], sv, sv);
+            stu(S, u, sv);
         }
+    }
+    for (int u = u0 + kPre * stride; u < nu; u += stride) {
+        T rx[E], vx[E], sv[E];
+        ldu(rx, R, u);
+        ldu(vx, V, u);
+#pragma unroll
+        for (int e = 0; e < E; ++e) sv[e] = tfma(ta, vx[e], rx[e]);
+        acc[0] = dunit<E>(acc[0], sv, sv);
+        stu(S, u, sv);
     }
     block_sum<1>(acc, red);
     if (threadIdx.x == 0) {
@@ -339,17 +364,20 @@ __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P,
     __shared__ double bc[2];
     __shared__ int go, hf;
     constexpr int E = Unit<T>::E;
-    const int stride = gridDim.x * blockDim.x;
-    int u = blockIdx.x * blockDim.x + threadIdx.x;
-    // operands of the first unit requested before the reductions (t too: the rare half step,
-    // known only after them, does not need it)
-    T x[E], p[E], s[E], r0[E], t[E];
-    if (u < nu) {
-        ldu(x, X, u);
-        ldu(p, P, u);
-        ldu(s, S, u);
-        ldu(r0, R0, u);
-        ldu(t, Tv, u);
+    const int stride = gridDim.x * blockDim.x, u0 = blockIdx.x * blockDim.x + threadIdx.x;
+    // operands of the first kPre units requested before the reductions (t too: the rare half
+    // step, known only after them, does not need it)
+    T x[kPre][E], p[kPre][E], s[kPre][E], r0[kPre][E], t[kPre][E];
+#pragma unroll
+    for (int k = 0; k < kPre; ++k) {
+        const int u = u0 + k * stride;
+        if (u < nu) {
+            ldu(x[k], X, u);
+            ldu(p[k], P, u);
+            ldu(s[k], S, u);
+            ldu(r0[k], R0, u);
+            ldu(t[k], Tv, u);
+        }
     }
     double v[2], w[2];
     reduce_pair<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, part_s, nparts, v, w, red);
@@ -380,33 +408,40 @@ __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P,
     const bool half = hf != 0;
     const T ta = static_cast<T>(bc[0]), tw = static_cast<T>(bc[1]), tnw = static_cast<T>(-bc[1]);
     double acc[2] = {0.0, 0.0};
-    while (u < nu) {
+    // x += alpha p + omega s, r = s - omega t (half step: x += alpha p, r = s); (r.r0, r.r)
+    auto unit = [&](int u, T(&xx)[E], const T(&pp)[E], const T(&ss)[E], const T(&rr0)[E], const T(&tt)[E]) {
         T r[E];
         if (!half) {
 #pragma unroll
             for (int e = 0; e < E; ++e) {
-                x[e] = tfma(tw, s[e], tfma(ta, p[e], x[e]));
-                r[e] = tfma(tnw, t[e], s[e]);
+                xx[e] = tfma(tw, ss[e], tfma(ta, pp[e], xx[e]));
+                r[e] = tfma(tnw, tt[e], ss[e]);
             }
         } else {
 #pragma unroll
             for (int e = 0; e < E; ++e) {
-                x[e] = tfma(ta, p[e], x[e]);
-                r[e] = s[e];
+                xx[e] = tfma(ta, pp[e], xx[e]);
+                r[e] = ss[e];
             }
         }
-        acc[0] = dunit<E>(acc[0], r, r0);
+        acc[0] = dunit<E>(acc[0], r, rr0);
         acc[1] = dunit<E>(acc[1], r, r);
-        stu(X, u, x);
+        stu(X, u, xx);
         stu(R, u, r);
-        u += stride;
-        if (u < nu) {
-            ldu(x, X, u);
-            ldu(p, P, u);
-            ldu(s, S, u);
-            ldu(r0, R0, u);
-            ldu(t, Tv, u);
-        }
+    };
+#pragma unroll
+    for (int k = 0; k < kPre; ++k) {
+        const int u = u0 + k * stride;
+        if (u < nu) unit(u, x[k], p[k], s[k], r0[k], t[k]);
+    }
+    for (int u = u0 + kPre * stride; u < nu; u += stride) {
+        T xx[E], pp[E], ss[E], rr0[E], tt[E];
+        ldu(xx, X, u);
+        ldu(pp, P, u);
+        ldu(ss, S, u);
+        ldu(rr0, R0, u);
+        ldu(tt, Tv, u);
+        unit(u, xx, pp, ss, rr0, tt);
     }
     block_sum<2>(acc, red);
     if (threadIdx.x == 0) {
@@ -1076,6 +1111,7 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
         if (use_graph && !s->g64) HHP_TRY(build_g64(s));
         h.maxit = o->maxit - it_before;
         int dev_status = ST_RUNNING;
+        double prev_true = INFINITY;
         for (int pass = 0; pass < max_outer; ++pass) {
             h.restart = pass > 0 ? 1 : 0;
             h.first_outer = 0;
@@ -1093,7 +1129,14 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
             // did not (rounding drift); restart from the current iterate, whose true residual
             // becomes the new r and shadow residual.
             const bool conv = dev_status == ST_CONVERGED || dev_status == ST_CONVERGED_HALF;
-            if (conv && !h.fixed && h.true_rr > h.thr2 && h.iter < h.maxit) continue;
+            if (conv && !h.fixed && h.true_rr > h.thr2 && h.iter < h.maxit) {
+                // Stagnation: a pass after a restart that did not halve the true residual's norm
+                // means rounding, not convergence, limits it (the attainable accuracy of this
+                // system and right-hand side is above rtol): stop instead of restarting again.
+                if (h.true_rr > 0.25 * prev_true) break;
+                prev_true = h.true_rr;
+                continue;
+            }
             // Breakdown (rho or omega vanished) after some progress: restart from the current
             // iterate with a fresh shadow residual.
             if (dev_status == ST_BREAKDOWN && !h.fixed && h.iter > h.iter_start && h.iter < h.maxit) continue;
