@@ -244,7 +244,7 @@ def run_ours(args, rk):
         x_h[:] = 0.0
         flush_l2()
         t0 = time.perf_counter()
-        x_out, r2 = bicgstab(ctx, A, b_h, x_h, None, rtol=RTOL, maxit=5000)
+        x_out, r2 = bicgstab(ctx, A, b_h, x_h, None, rtol=RTOL, maxit=5000, inplace=True)
         e2e.append(time.perf_counter() - t0)
     assert r2.status == 0
     t_e2e = dist.max_over_ranks(rk, statistics.median(e2e))

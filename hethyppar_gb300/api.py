@@ -214,10 +214,12 @@ def _opts(rtol, maxit, precision, inner_rtol, max_outer, fixed_iters, print_ever
 def bicgstab(ctx: Context, A: Matrix, b, x=None, x_target=None, *, rtol: float = 1e-10, maxit: int = 2000,
              precision: str = "fp64", inner_rtol: float = 0.1, max_outer: int = 50, fixed_iters: bool = False,
              record_history: bool = False, callback: Optional[Callable[[int, float], None]] = None,
-             print_every: int = 1, raise_on_error: bool = True, precond: str = "none"):
+             print_every: int = 1, raise_on_error: bool = True, precond: str = "none", inplace: bool = False):
     """Solves A x = b. Host numpy arrays use hhp_bicgstab (copies in/out); CUDA tensors use
-    hhp_bicgstab_dev. x is the initial guess (zeros if None) and is overwritten for tensors.
-    Returns (x, SolveResult)."""
+    hhp_bicgstab_dev. x is the initial guess (zeros if None) and is overwritten for tensors; a host
+    x is copied first unless inplace=True and it is a writable C-contiguous float64 array, which
+    then receives the solution directly (no host copy; a pinned array keeps the transfers at full
+    speed). Returns (x, SolveResult)."""
     hist: List[float] = []
 
     def _cb(it, rr, _user):
@@ -239,7 +241,13 @@ def bicgstab(ctx: Context, A: Matrix, b, x=None, x_target=None, *, rtol: float =
         out = x
     else:
         bv = _host(b, np.float64)
-        out = np.zeros(A.shape[1], np.float64) if x is None else _host(x, np.float64).copy()
+        if x is None:
+            out = np.zeros(A.shape[1], np.float64)
+        elif (inplace and isinstance(x, np.ndarray) and x.dtype == np.float64 and x.flags.c_contiguous
+              and x.flags.writeable and x.size == A.shape[1]):
+            out = x
+        else:
+            out = _host(x, np.float64).copy()
         xt = None if x_target is None else _host(x_target, np.float64)
         st = lib().hhp_bicgstab(ctx.handle, A.handle, _ptr(bv), _ptr(out), _ptr(xt), ctypes.byref(o),
                                 ctypes.byref(info))

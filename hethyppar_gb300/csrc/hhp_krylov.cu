@@ -67,6 +67,7 @@ struct Solver {
     double *hist = nullptr;
     int hist_cap = 0;
     cudaStream_t s2 = nullptr, s3 = nullptr;  // capture streams: loop body, IF body
+    cudaEvent_t ev_in = nullptr;              // joins the two input uploads
     cudaGraphExec_t g64 = nullptr, gmix = nullptr;
     int g64_kernels_pro = 0, g64_kernels_epi = 0, gmix_kernels_pro = 0, gmix_kernels_epi = 0, unroll = 4;
 };
@@ -723,7 +724,8 @@ hhp_status ensure_solver(hhp_mat *A, Solver **out, int maxit) {
         if (st == HHP_OK && cudaMallocHost(&s->h_sc, sizeof(DevScal)) != cudaSuccess) st = HHP_ERR_OOM;
         if (st == HHP_OK && cudaMallocHost(&s->h_sc32, sizeof(DevScal)) != cudaSuccess) st = HHP_ERR_OOM;
         if (st == HHP_OK && (cudaStreamCreateWithFlags(&s->s2, cudaStreamNonBlocking) != cudaSuccess ||
-                             cudaStreamCreateWithFlags(&s->s3, cudaStreamNonBlocking) != cudaSuccess))
+                             cudaStreamCreateWithFlags(&s->s3, cudaStreamNonBlocking) != cudaSuccess ||
+                             cudaEventCreateWithFlags(&s->ev_in, cudaEventDisableTiming) != cudaSuccess))
             st = HHP_ERR_CUDA;
         A->solver = s;
         if (st != HHP_OK) return st;
@@ -1090,8 +1092,29 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
     if (mixed) HHP_TRY(ensure_fp32_inner(A, s));
     HHP_CUDA(cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), st));
     HHP_TRY(copy_in(s->B, b_in, A->m, st, host));
-    HHP_TRY(copy_in(s->X, x_io, A->n, st, host));
+    if (host) {
+        // the two uploads run side by side (x0 on the second stream, joined by an event)
+        HHP_CUDA(cudaEventRecord(s->ev_in, st));
+        HHP_CUDA(cudaStreamWaitEvent(s->s2, s->ev_in, 0));
+        HHP_TRY(copy_in(s->X, x_io, A->n, s->s2, host));
+        HHP_CUDA(cudaEventRecord(s->ev_in, s->s2));
+        HHP_CUDA(cudaStreamWaitEvent(st, s->ev_in, 0));
+    } else {
+        HHP_TRY(copy_in(s->X, x_io, A->n, st, host));
+    }
     HHP_CUDA(cudaEventRecord(ctx->ev0, st));
+    int dev_err = 0;
+    // After each pass: end-of-solve event, the iterate out to the caller, the device scalars and
+    // the error word back -- one synchronisation for all (a restart repeats them).
+    auto readback = [&](DevScal *hs, const DevScal *ds) -> hhp_status {
+        HHP_CUDA(cudaEventRecord(ctx->ev1, st));
+        HHP_CUDA(cudaMemcpyAsync(x_io, s->X, sizeof(double) * static_cast<size_t>(A->n),
+                                 host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
+        HHP_CUDA(cudaMemcpyAsync(hs, ds, sizeof(DevScal), cudaMemcpyDeviceToHost, st));
+        HHP_CUDA(cudaMemcpyAsync(&dev_err, ctx->dev_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        HHP_CUDA(cudaStreamSynchronize(st));
+        return HHP_OK;
+    };
 
     DevScal &h = *s->h_sc;
     h.rtol2 = o->rtol * o->rtol;
@@ -1120,8 +1143,7 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
             } else {
                 HHP_TRY(run_direct64(s));
             }
-            HHP_CUDA(cudaMemcpyAsync(s->h_sc, s->sc, sizeof(DevScal), cudaMemcpyDeviceToHost, st));
-            HHP_CUDA(cudaStreamSynchronize(st));
+            HHP_TRY(readback(s->h_sc, s->sc));
             ++outer;
             if (use_graph) ctx->kernel_launches += s->g64_kernels_pro + s->g64_kernels_epi + 5LL * s->unroll * h.bodies;
             dev_status = h.status;
@@ -1170,8 +1192,7 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
             h32.restart = pass > 0 ? 1 : 0;
             const int upd0 = pass > 0 ? h32.updates : 0;
             HHP_CUDA(cudaGraphLaunch(s->gmix, st));
-            HHP_CUDA(cudaMemcpyAsync(s->h_sc32, s->sc32, sizeof(DevScal), cudaMemcpyDeviceToHost, st));
-            HHP_CUDA(cudaStreamSynchronize(st));
+            HHP_TRY(readback(s->h_sc32, s->sc32));
             // 5 kernels per iteration, 3 more per FP64 update (the IF body)
             ctx->kernel_launches += s->gmix_kernels_pro + s->gmix_kernels_epi + 5LL * s->unroll * h32.bodies +
                                     3LL * (h32.updates - upd0);
@@ -1197,9 +1218,6 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
             HHP_TRY(fp64_passes(total_iters));
         }
     }
-    HHP_CUDA(cudaEventRecord(ctx->ev1, st));
-    HHP_CUDA(cudaMemcpyAsync(x_io, s->X, sizeof(double) * static_cast<size_t>(A->n),
-                             host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
     double err = NAN;
     if (xt && !host) {
         double *dmax = s->Y;  // scratch slot; Y is not needed after the solve
@@ -1207,10 +1225,8 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
         k_err_vs_target<<<ctx->num_sms, 256, 0, st>>>(s->X, xt, A->n, dmax);
         ctx->kernel_launches += 1;
         HHP_CUDA(cudaMemcpyAsync(&err, dmax, sizeof(double), cudaMemcpyDeviceToHost, st));
+        HHP_CUDA(cudaStreamSynchronize(st));
     }
-    int dev_err = 0;
-    HHP_CUDA(cudaMemcpyAsync(&dev_err, ctx->dev_err, sizeof(int), cudaMemcpyDeviceToHost, st));
-    HHP_CUDA(cudaStreamSynchronize(st));
     if (dev_err != DEV_OK) {
         set_error("a bounded device wait timed out inside the SpMV kernel");
         result = HHP_ERR_TIMEOUT;
@@ -1262,6 +1278,7 @@ void solver_release(Solver *s) {
     cudaFreeHost(s->h_sc32);
     if (s->s2) cudaStreamDestroy(s->s2);
     if (s->s3) cudaStreamDestroy(s->s3);
+    if (s->ev_in) cudaEventDestroy(s->ev_in);
     delete s;
 }
 

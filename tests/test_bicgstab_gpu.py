@@ -143,3 +143,15 @@ def test_permutation_solve(ctx):
     xx = np.empty_like(x)
     xx[p] = x
     assert np.max(np.abs(xx - np.arange(1, 321))) < 1e-8
+
+
+def test_host_solve_in_place(ctx):
+    g = load_golden("sample320")
+    A = Matrix.from_csr(ctx, g["rowptr"], g["col"], g["val"])
+    x0 = np.array(g["x0"], np.float64)
+    keep = x0.copy()
+    x_copy, r1 = bicgstab(ctx, A, g["b"], x0, rtol=1e-10, maxit=500)
+    assert np.array_equal(x0, keep)  # the default leaves the caller's array alone
+    x_in, r2 = bicgstab(ctx, A, g["b"], x0, rtol=1e-10, maxit=500, inplace=True)
+    assert x_in is x0 and np.array_equal(x0, x_copy) and r1.iters == r2.iters
+    A.close()
