@@ -235,6 +235,23 @@ def run_ours(args, rk):
     clk = clocks.stop()
     t_solve = dist.max_over_ranks(rk, statistics.mean(step_ms) / 1e3)
 
+    # the same solve with the classic 5-kernel iteration (the reference's dot-product order), for
+    # comparison with the merged 4-kernel default timed above
+    for _ in range(2):
+        x_d.zero_()
+        res_c = bicgstab(ctx, A, b_d, x_d, xt_d, rtol=RTOL, maxit=5000, loop="classic")[1]
+    classic_ms = []
+    for _ in range(args.steps):
+        x_d.zero_()
+        torch.cuda.synchronize()
+        flush_l2(sync=False)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        res_c = bicgstab(ctx, A, b_d, x_d, xt_d, rtol=RTOL, maxit=5000, loop="classic")[1]
+        e1.record(stream)
+        e1.synchronize()
+        classic_ms.append(e0.elapsed_time(e1))
+
     # ---- e2e: host buffers through hhp_bicgstab (H2D b, x0; D2H x) ---------------------------------
     b_h = torch.empty(s.n, dtype=torch.float64, pin_memory=True).numpy()
     b_h[:] = s.b
@@ -314,6 +331,9 @@ def run_ours(args, rk):
            "iters": res.iters, "iters_per_s": res.iters / (statistics.mean(step_ms) / 1e3),
            "us_per_iter": statistics.mean(step_ms) * 1e3 / max(res.iters, 1),
            "solve_graph_ms": statistics.mean(lib_ms),
+           "classic_loop": {"ms": statistics.mean(classic_ms), "iters": res_c.iters,
+                            "rel_res_true": res_c.rel_res_true,
+                            "note": "same solve, 5 kernels per iteration (rho and ||r|| as direct dot products)"},
            "rel_res_true": res.rel_res_true, "err_vs_target": res.err_vs_target,
            "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": 2 * 8 * s.n, "d2h_bytes_per_step": 8 * s.n},
            "roofline": roof,

@@ -34,6 +34,7 @@ class SolveOpts(ctypes.Structure):
         ("cb", ITER_CB),
         ("user", ctypes.c_void_p),
         ("precond", ctypes.c_int),
+        ("loop", ctypes.c_int),
     ]
 
 

@@ -194,11 +194,17 @@ class SolveResult:
 
 
 PRECONDS = {"none": 0, "jacobi": 1}
+# FP64 iteration schedule (hhp_loop): "merged" = 4 kernels per iteration, stop tests and beta from
+# the t = A s dot products; "classic" = the reference's order, rho and ||r|| as direct dot
+# products; "auto" = merged for forward solves, classic for the adjoint solve
+LOOPS = {"auto": 0, "merged": 1, "classic": 2}
 
 
-def _opts(rtol, maxit, precision, inner_rtol, max_outer, fixed_iters, print_every, cb, precond="none") -> SolveOpts:
+def _opts(rtol, maxit, precision, inner_rtol, max_outer, fixed_iters, print_every, cb, precond="none",
+          loop="auto") -> SolveOpts:
     o = SolveOpts()
     o.precond = PRECONDS[precond] if isinstance(precond, str) else int(precond)
+    o.loop = LOOPS[loop] if isinstance(loop, str) else int(loop)
     o.rtol = rtol
     o.maxit = maxit
     o.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
@@ -214,7 +220,8 @@ def _opts(rtol, maxit, precision, inner_rtol, max_outer, fixed_iters, print_ever
 def bicgstab(ctx: Context, A: Matrix, b, x=None, x_target=None, *, rtol: float = 1e-10, maxit: int = 2000,
              precision: str = "fp64", inner_rtol: float = 0.1, max_outer: int = 50, fixed_iters: bool = False,
              record_history: bool = False, callback: Optional[Callable[[int, float], None]] = None,
-             print_every: int = 1, raise_on_error: bool = True, precond: str = "none", inplace: bool = False):
+             print_every: int = 1, raise_on_error: bool = True, precond: str = "none", inplace: bool = False,
+             loop: str = "auto"):
     """Solves A x = b. Host numpy arrays use hhp_bicgstab (copies in/out); CUDA tensors use
     hhp_bicgstab_dev. x is the initial guess (zeros if None) and is overwritten for tensors; a host
     x is copied first unless inplace=True and it is a writable C-contiguous float64 array, which
@@ -230,7 +237,7 @@ def bicgstab(ctx: Context, A: Matrix, b, x=None, x_target=None, *, rtol: float =
     want_cb = record_history or callback is not None
     cfun = ITER_CB(_cb) if want_cb else None
     o = _opts(rtol, maxit, precision, inner_rtol, max_outer, fixed_iters, print_every if want_cb else 0, cfun,
-              precond)
+              precond, loop)
     info = SolveInfo()
     if _is_dev(b):
         import torch
@@ -259,9 +266,9 @@ def bicgstab(ctx: Context, A: Matrix, b, x=None, x_target=None, *, rtol: float =
 
 
 def bicgstab_backward(ctx: Context, A: Matrix, x, dldx, *, rtol: float = 1e-12, maxit: int = 20000,
-                      precision: str = "fp64", want_dlda: bool = True):
+                      precision: str = "fp64", want_dlda: bool = True, loop: str = "auto"):
     """Adjoint of x = A^-1 b: returns (dL/db, dL/dA over A's stored entries, SolveResult)."""
-    o = _opts(rtol, maxit, precision, 0.1, 50, False, 0, None)
+    o = _opts(rtol, maxit, precision, 0.1, 50, False, 0, None, "none", loop)
     info = SolveInfo()
     if _is_dev(x):
         import torch

@@ -18,6 +18,8 @@
  *   --print-every K   print "Iteration = i; Error Norm = e" every K iterations
  *                     (gpu_BiCGStab's per-iteration line, bicgstab_gpu.c:156)
  *   --out-format F    compat (default, "%lf" like vector_write) | exact ("%.17g")
+ *   --loop L          auto (default: merged) | merged (4 kernels per iteration) | classic (the
+ *                     reference's dot products; --fixed always runs it)
  */
 #include <argp.h>
 #include <math.h>
@@ -29,11 +31,11 @@
 
 #include "hhp_gpu.h"
 
-enum { OPT_RTOL = 1000, OPT_FIXED, OPT_PREC, OPT_XT, OPT_PERM, OPT_PRINT, OPT_OUTFMT, OPT_DEVICE, OPT_WCSR, OPT_PRECOND };
+enum { OPT_RTOL = 1000, OPT_FIXED, OPT_PREC, OPT_XT, OPT_PERM, OPT_PRINT, OPT_OUTFMT, OPT_DEVICE, OPT_WCSR, OPT_PRECOND, OPT_LOOP };
 
 struct arguments {
     char *input_matrix, *input_x, *input_y, *output_x, *x_target, *perm, *write_csr;
-    int n_iters, fixed, mixed, print_every, exact, device, jacobi;
+    int n_iters, fixed, mixed, print_every, exact, device, jacobi, loop;
     double rtol;
 };
 
@@ -53,6 +55,8 @@ static struct argp_option options[] = {
     {"device", OPT_DEVICE, "ID", 0, "CUDA device (default 0)", 0},
     {"write-csr", OPT_WCSR, "FILE", 0, "Also store the matrix as a binary CSR file (later runs: -m FILE)", 0},
     {"precond", OPT_PRECOND, "none|jacobi", 0, "Preconditioner (default none, as the reference)", 0},
+    {"loop", OPT_LOOP, "auto|merged|classic", 0,
+     "FP64 iteration schedule: merged (the default for a solve, 4 kernels per iteration) or classic (the reference's dot products)", 0},
     {0}};
 
 static error_t parse_opt(int key, char *arg, struct argp_state *state) {
@@ -81,6 +85,12 @@ static error_t parse_opt(int key, char *arg, struct argp_state *state) {
             break;
         case OPT_DEVICE: a->device = (int)strtol(arg, &end, 10); break;
         case OPT_WCSR: a->write_csr = arg; break;
+        case OPT_LOOP:
+            if (strcmp(arg, "classic") == 0) a->loop = HHP_LOOP_CLASSIC;
+            else if (strcmp(arg, "merged") == 0) a->loop = HHP_LOOP_MERGED;
+            else if (strcmp(arg, "auto") == 0) a->loop = HHP_LOOP_AUTO;
+            else argp_error(state, "unknown loop '%s'", arg);
+            break;
         case OPT_PRECOND:
             if (strcmp(arg, "jacobi") == 0) a->jacobi = 1;
             else if (strcmp(arg, "none") == 0) a->jacobi = 0;
@@ -207,6 +217,7 @@ int main(int argc, char **argv) {
     o.precision = a.mixed ? HHP_PREC_MIXED : HHP_PREC_FP64;
     o.inner_rtol = 0.1;
     o.precond = a.jacobi ? HHP_PRECOND_JACOBI : HHP_PRECOND_NONE;
+    o.loop = a.loop;
     o.fixed_iters = a.fixed;
     o.print_every = a.print_every;
     o.cb = a.print_every > 0 ? print_iter : NULL;

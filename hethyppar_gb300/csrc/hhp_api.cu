@@ -447,9 +447,10 @@ static hhp_status check_solve(hhp_ctx *ctx, hhp_mat *A, const void *b, const voi
         return HHP_ERR_ARG;
     }
     if (o && (o->maxit < 0 || !(o->rtol >= 0.0) || (o->precision != HHP_PREC_FP64 && o->precision != HHP_PREC_MIXED) ||
-              (o->precond != HHP_PRECOND_NONE && o->precond != HHP_PRECOND_JACOBI))) {
-        set_error("bicgstab: invalid options (maxit %d, rtol %g, precision %d, precond %d)", o->maxit, o->rtol,
-                  o->precision, o->precond);
+              (o->precond != HHP_PRECOND_NONE && o->precond != HHP_PRECOND_JACOBI) ||
+              (o->loop != HHP_LOOP_AUTO && o->loop != HHP_LOOP_MERGED && o->loop != HHP_LOOP_CLASSIC))) {
+        set_error("bicgstab: invalid options (maxit %d, rtol %g, precision %d, precond %d, loop %d)", o->maxit,
+                  o->rtol, o->precision, o->precond, o->loop);
         return HHP_ERR_ARG;
     }
     return HHP_OK;

@@ -58,8 +58,9 @@ __device__ __forceinline__ void warp_sum2(double &a, double &b, int lane) {
 
 // NQ warp sums at once with a transposed butterfly: at each of the first levels a lane hands
 // half of the quantities it still carries to its partner and keeps the other half, so the FP64
-// adds per warp are 5 (NQ = 1), 5 (NQ = 2) or 6 (NQ = 4) instead of 5 * NQ. On return `r` holds,
-// in lanes [q * 32/NQ, (q+1) * 32/NQ), the warp's sum of quantity q. Fixed order: reproducible.
+// adds per warp are 5 (NQ = 1), 5 (NQ = 2), 6 (NQ = 4) or 9 (NQ = 8) instead of 5 * NQ. On
+// return `r` holds, in lanes [q * 32/NQ, (q+1) * 32/NQ), the warp's sum of quantity q. Fixed
+// order: reproducible.
 template <int NQ>
 __device__ __forceinline__ double warp_reduce(const double (&v)[NQ], int lane);
 template <>
@@ -84,6 +85,32 @@ __device__ __forceinline__ double warp_reduce<4>(const double (&v)[4], int lane)
     k += __shfl_xor_sync(0xffffffffu, g, 8);
 #pragma unroll
     for (int o = 4; o >= 1; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+    return k;
+}
+template <>
+__device__ __forceinline__ double warp_reduce<8>(const double (&v)[8], int lane) {
+    // three halving levels (4 + 2 + 1 adds) leave quantity q in lanes [4q, 4q + 4); two more
+    // levels finish it: 9 FP64 adds per warp instead of 40
+    double k4[4];
+    const bool h16 = (lane & 16) != 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const double keep = h16 ? v[i + 4] : v[i], give = h16 ? v[i] : v[i + 4];
+        k4[i] = keep + __shfl_xor_sync(0xffffffffu, give, 16);
+    }
+    double k2[2];
+    const bool h8 = (lane & 8) != 0;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const double keep = h8 ? k4[i + 2] : k4[i], give = h8 ? k4[i] : k4[i + 2];
+        k2[i] = keep + __shfl_xor_sync(0xffffffffu, give, 8);
+    }
+    const bool h4 = (lane & 4) != 0;
+    double k = h4 ? k2[1] : k2[0];
+    const double g = h4 ? k2[0] : k2[1];
+    k += __shfl_xor_sync(0xffffffffu, g, 4);
+    k += __shfl_xor_sync(0xffffffffu, k, 2);
+    k += __shfl_xor_sync(0xffffffffu, k, 1);
     return k;
 }
 

@@ -69,8 +69,8 @@ struct PlanDev {
     int *long_first = nullptr, *chunk_long = nullptr;
     double *chunk_part = nullptr;     // n_chunks
     unsigned *long_cnt = nullptr;     // n_long (kept at zero between launches)
-    double *long_dot = nullptr;       // n_long * 2 epilogue contributions of long rows
-    double *cta_part = nullptr;       // ctas * 2 epilogue partials
+    double *long_dot = nullptr;       // n_long * 4 epilogue contributions of long rows
+    double *cta_part = nullptr;       // ctas * 4 epilogue partials (records of 2, or 4 for EP_DOT3)
     bool built() const { return slice_ptr != nullptr; }
     void release();
 };
@@ -121,16 +121,21 @@ enum EpKind : int {
     EP_DOT2 = 2,    // y = A x; partial[0] += y.w1, partial[1] += y.y
     EP_RESID = 3,   // y = w1 - A x (residual); partial[0] += y.y, partial[1] += w1.w1
     EP_Y = 4,       // y = A x (EP_AXPBY with alpha 1, beta 0; chosen by the launcher)
+    EP_DOT3 = 5,    // y = A x; partial[0] += y.w1, partial[1] += y.y, partial[2] += y.w2 (records
+                    // of 4 doubles, the last zero; every other epilogue writes records of 2)
 };
 
 hhp_status ensure_plan(hhp_mat *A, bool fp32);
 // Rewrites the slice values of existing plans from the CSR values (after a value change).
 hhp_status refresh_plan_values(hhp_mat *A);
 // Launches the FP64 SpMV with an epilogue on `stream` (x, y, w1 length-padded device vectors).
-// gate (nullable, device int): the launch does nothing when *gate == 0 at kernel start.
+// gate (nullable, device int): the launch does nothing when *gate == 0 at kernel start; stop
+// (nullable, device int): the launch does nothing when *stop != 0 (a solver's status word).
 hhp_status launch_spmv64(hhp_mat *A, cudaStream_t stream, EpKind ep, const double *x, double *y, const double *w1,
-                         double alpha, double beta, const int *gate = nullptr);
-hhp_status launch_spmv32(hhp_mat *A, cudaStream_t stream, EpKind ep, const float *x, float *y, const float *w1);
+                         double alpha, double beta, const int *gate = nullptr, const double *w2 = nullptr,
+                         const int *stop = nullptr);
+hhp_status launch_spmv32(hhp_mat *A, cudaStream_t stream, EpKind ep, const float *x, float *y, const float *w1,
+                         const int *stop = nullptr);
 // Number of partial records (ctas) and long-row records of the last-used plan, for the reducers.
 inline int plan_ctas(const hhp_mat *A, bool fp32) { return fp32 ? A->plan32.ctas : A->plan64.ctas; }
 

@@ -47,7 +47,8 @@ struct DevScal {
     double thr2_rec;      // threshold for the recursive-residual tests (-1: none, mixed form)
     double rr_max[2];     // mixed form: largest recursive ||r||^2 since the last FP64 update,
                           // double-buffered by iteration parity (read one, write the other)
-    int iter, iter_start, status, bodies, outer_conv, ru_flag, updates, pad_;
+    int iter, iter_start, status, bodies, outer_conv, ru_flag, updates;
+    int arrivals;         // K_XRP blocks that have read the status this launch (0 between launches)
 };
 constexpr size_t kCtlBytes = offsetof(DevScal, rho_prev);
 
@@ -68,7 +69,7 @@ struct Solver {
     int hist_cap = 0;
     cudaStream_t s2 = nullptr, s3 = nullptr;  // capture streams: loop body, IF body
     cudaEvent_t ev_in = nullptr;              // joins the two input uploads
-    cudaGraphExec_t g64 = nullptr, gmix = nullptr;
+    cudaGraphExec_t g64 = nullptr, g64m = nullptr, gmix = nullptr;  // FP64 classic / merged, mixed
     int g64_kernels_pro = 0, g64_kernels_epi = 0, gmix_kernels_pro = 0, gmix_kernels_epi = 0, unroll = 4;
 };
 
@@ -285,22 +286,24 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
     }
 }
 
-// K_S: alpha = rho / (r0.v), s = r - alpha v, partial s.s.
-template <typename T>
-__global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const T *V, int nu, SpmvParts sp,
-                                           double *part_s) {
+// K_S: alpha = rho / (r0.v), s = r - alpha v, partial s.s. Merged loop (M): also r0.s, in
+// records of 4 (s.s, r0.s, 0, 0) for K_XRP.
+template <typename T, bool M = false>
+__global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const T *V, const T *R0, int nu,
+                                           SpmvParts sp, double *part_s) {
     __shared__ double red[kRedScratch];
     __shared__ double bc[1];
     __shared__ int go;
     constexpr int E = Unit<T>::E;
     const int stride = gridDim.x * blockDim.x, u0 = blockIdx.x * blockDim.x + threadIdx.x;
-    T r[kPre][E], vv[kPre][E];
+    T r[kPre][E], vv[kPre][E], q[M ? kPre : 1][E];
 #pragma unroll
     for (int k = 0; k < kPre; ++k) {
         const int u = u0 + k * stride;
         if (u < nu) {
             ldu(r[k], R, u);
             ldu(vv[k], V, u);
+            if constexpr (M) ldu(q[k], R0, u);
         }
     }
     double v[2];
@@ -327,7 +330,7 @@ __global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const 
     __syncthreads();
     if (!go) return;
     const T ta = static_cast<T>(bc[0]);
-    double acc[1] = {0.0};
+    double acc[M ? 2 : 1] = {};
 #pragma unroll
     for (int k = 0; k < kPre; ++k) {
         const int u = u0 + k * stride;
@@ -336,6 +339,7 @@ __global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const 
 #pragma unroll
             for (int e = 0; e < E; ++e) sv[e] = tfma(ta, vv[k][e], r[k][e]);
             acc[0] = dunit<E>(acc[0], sv, sv);
+            if constexpr (M) acc[M ? 1 : 0] = dunit<E>(acc[M ? 1 : 0], sv, q[k]);
             stu(S, u, sv);
         }
     }
@@ -346,12 +350,24 @@ __global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const 
 #pragma unroll
         for (int e = 0; e < E; ++e) sv[e] = tfma(ta, vx[e], rx[e]);
         acc[0] = dunit<E>(acc[0], sv, sv);
+        if constexpr (M) {
+            T qx[E];
+            ldu(qx, R0, u);
+            acc[M ? 1 : 0] = dunit<E>(acc[M ? 1 : 0], sv, qx);
+        }
         stu(S, u, sv);
     }
-    block_sum<1>(acc, red);
+    block_sum<M ? 2 : 1>(acc, red);
     if (threadIdx.x == 0) {
-        part_s[2 * blockIdx.x] = acc[0];
-        part_s[2 * blockIdx.x + 1] = 0.0;
+        if constexpr (M) {
+            part_s[4 * blockIdx.x] = acc[0];
+            part_s[4 * blockIdx.x + 1] = acc[M ? 1 : 0];
+            part_s[4 * blockIdx.x + 2] = 0.0;
+            part_s[4 * blockIdx.x + 3] = 0.0;
+        } else {
+            part_s[2 * blockIdx.x] = acc[0];
+            part_s[2 * blockIdx.x + 1] = 0.0;
+        }
     }
 }
 
@@ -448,6 +464,148 @@ __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P,
     if (threadIdx.x == 0) {
         part_xr[2 * blockIdx.x] = acc[0];
         part_xr[2 * blockIdx.x + 1] = acc[1];
+    }
+}
+
+// Merged loop: the stop tests and beta need no pass over r. With omega = (t.s)/(t.t),
+//   ||r_new||^2 = ||s - omega t||^2 = s.s - omega (t.s)   and   r0.r_new = r0.s - omega r0.t,
+// from the partials of K_S (s.s, r0.s) and of the t = A s SpMV (t.s, t.t, r0.t). So K_XR and K_P
+// become one kernel: one kernel boundary, one reduction and one pass over p and v fewer per
+// iteration. The difference form loses relative accuracy only when ||r_new|| << ||s||; the
+// convergence test therefore uses max(s.s - omega t.s, kCancel s.s), which can only delay a stop
+// (never report one that the recursive residual has not reached), and the final true residual
+// b - A x, recomputed after the loop, is what the caller's tolerance is checked against.
+constexpr double kCancel = 64.0 * 2.220446049250313e-16;
+
+// K_XRP: omega, x += alpha p + omega s, r = s - omega t, the stop tests of the finished iteration,
+// beta = (rho_new / rho)(alpha / omega) and p = r + beta (p - omega v). Half step (||s|| below the
+// threshold): x += alpha p, r = s, stop.
+template <typename T>
+__global__ void __launch_bounds__(512) k_xrp(DevScal *sc, T *X, T *R, T *P, const T *S, const T *Tv, const T *V,
+                                             int nu, SpmvParts sp, const double *part_s, int nparts, double *hist,
+                                             int hist_cap, cudaGraphConditionalHandle cond, int first_in_body,
+                                             const int *dev_err, int use_cond) {
+    __shared__ double red[kRedScratch];
+    __shared__ double bc[3];
+    __shared__ int go;  // 0: nothing to do, 1: full step and p, 2: half step, 3: full step, last
+    constexpr int E = Unit<T>::E;
+    const int stride = gridDim.x * blockDim.x, u0 = blockIdx.x * blockDim.x + threadIdx.x;
+    T x[kPre][E], p[kPre][E], s[kPre][E], t[kPre][E], vv[kPre][E];
+#pragma unroll
+    for (int k = 0; k < kPre; ++k) {
+        const int u = u0 + k * stride;
+        if (u < nu) {
+            ldu(x[k], X, u);
+            ldu(p[k], P, u);
+            ldu(s[k], S, u);
+            ldu(t[k], Tv, u);
+            ldu(vv[k], V, u);
+        }
+    }
+    double v[4], w[4];
+    reduce_pair<4>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, part_s, nparts, v, w, red);
+    if (threadIdx.x == 0) {
+        const bool lead = blockIdx.x == 0;
+        int mode = 0, term = *reinterpret_cast<volatile const int *>(&sc->status);
+        if (lead && first_in_body) sc->bodies += 1;  // bodies executed (kernel-launch accounting)
+        if (term == ST_RUNNING) {
+            const double ts = v[0], tt = v[1], r0t = v[2], ss = w[0], r0s = w[1];
+            const double thr2 = sc->thr2_rec, alpha = sc->alpha;
+            const int iter = sc->iter;  // this iteration (K_S counted it)
+            double rr = ss;
+            bc[0] = alpha;
+            bc[1] = 0.0;
+            if (*reinterpret_cast<volatile const int *>(dev_err) != DEV_OK) {
+                term = ST_DEVICE_ERROR;
+            } else if (thr2 >= 0.0 && ss <= thr2) {
+                mode = 2;
+                term = ST_CONVERGED_HALF;
+            } else {
+                const double omega = ts / tt;
+                if (!finite_nonzero(tt) || !isfinite(omega)) {
+                    term = ST_BREAKDOWN;
+                } else {
+                    bc[1] = omega;
+                    rr = fmax(ss - omega * ts, 0.0);
+                    mode = 3;
+                    if (thr2 >= 0.0 && fmax(rr, kCancel * ss) <= thr2) {
+                        term = ST_CONVERGED;
+                    } else if (iter >= sc->maxit) {
+                        term = ST_MAXIT;
+                    } else {
+                        const double rho_new = r0s - omega * r0t;
+                        if (!finite_nonzero(rho_new) || !isfinite(rr)) {
+                            term = ST_BREAKDOWN;
+                        } else {
+                            const double beta = (rho_new / sc->rho_prev) * (alpha / omega);
+                            bc[2] = beta;
+                            mode = 1;
+                            if (lead) {
+                                sc->rho_cur = rho_new;
+                                sc->beta = beta;
+                            }
+                        }
+                    }
+                    if (lead) sc->omega = omega;
+                }
+            }
+            if (lead && mode != 0) {
+                if (iter - 1 < hist_cap && iter >= 1) hist[iter - 1] = rr;
+                sc->rr_last = rr;
+            }
+        }
+        // Every block must see the status as it was at launch (a terminal step still updates x
+        // and r in every block), so the block that arrives last -- after all have read it --
+        // stores the new status; no block waits for another.
+        __threadfence();
+        if (atomicAdd(&sc->arrivals, 1) == static_cast<int>(gridDim.x) - 1) {
+            sc->arrivals = 0;
+            if (term != ST_RUNNING) sc->status = term;
+        }
+        if (lead && use_cond && term != ST_RUNNING) cudaGraphSetConditional(cond, 0);
+        go = mode;
+    }
+    __syncthreads();
+    const int mode = go;
+    if (mode == 0) return;
+    const T ta = static_cast<T>(bc[0]), tw = static_cast<T>(bc[1]), tnw = static_cast<T>(-bc[1]),
+            tb = static_cast<T>(bc[2]);
+    auto unit = [&](int u, T(&xx)[E], T(&pp)[E], const T(&ss)[E], const T(&tt)[E], const T(&vx)[E]) {
+        T r[E];
+        if (mode == 2) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                xx[e] = tfma(ta, pp[e], xx[e]);
+                r[e] = ss[e];
+            }
+        } else {
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                xx[e] = tfma(tw, ss[e], tfma(ta, pp[e], xx[e]));
+                r[e] = tfma(tnw, tt[e], ss[e]);
+            }
+            if (mode == 1) {
+#pragma unroll
+                for (int e = 0; e < E; ++e) pp[e] = tfma(tb, tfma(tnw, vx[e], pp[e]), r[e]);
+                stu(P, u, pp);
+            }
+        }
+        stu(X, u, xx);
+        stu(R, u, r);
+    };
+#pragma unroll
+    for (int k = 0; k < kPre; ++k) {
+        const int u = u0 + k * stride;
+        if (u < nu) unit(u, x[k], p[k], s[k], t[k], vv[k]);
+    }
+    for (int u = u0 + kPre * stride; u < nu; u += stride) {
+        T xx[E], pp[E], ss[E], tt[E], vx[E];
+        ldu(xx, X, u);
+        ldu(pp, P, u);
+        ldu(ss, S, u);
+        ldu(tt, Tv, u);
+        ldu(vx, V, u);
+        unit(u, xx, pp, ss, tt, vx);
     }
 }
 
@@ -716,7 +874,7 @@ hhp_status ensure_solver(hhp_mat *A, Solver **out, int maxit) {
         s->T = dalloc<double>(np, st);
         s->Y = dalloc<double>(np, st);
         s->part_xr = dalloc<double>(2 * s->nblk, st);
-        s->part_s = dalloc<double>(2 * s->nblk, st);
+        s->part_s = dalloc<double>(4 * s->nblk, st);  // records of 2, or 4 in the merged loop
         s->part_xr32 = dalloc<double>(2 * s->nblk, st);
         s->part_s32 = dalloc<double>(2 * s->nblk, st);
         s->sc = dalloc<DevScal>(1, st);
@@ -740,8 +898,9 @@ hhp_status ensure_solver(hhp_mat *A, Solver **out, int maxit) {
         s->hist_cap = need;
         // graphs hold the old history pointer
         if (s->g64) cudaGraphExecDestroy(s->g64);
+        if (s->g64m) cudaGraphExecDestroy(s->g64m);
         if (s->gmix) cudaGraphExecDestroy(s->gmix);
-        s->g64 = s->gmix = nullptr;
+        s->g64 = s->g64m = s->gmix = nullptr;
     }
     *out = s;
     return HHP_OK;
@@ -848,15 +1007,18 @@ hhp_status end_if_body(Solver *s, hhp_status rc) {
 // The FP64 (or FP32-inner) iteration loop as graph nodes on `stream`: the first K_P (stop tests
 // on the initial residual) before a WHILE node whose body holds `unroll` iterations, each
 // [SpMV + r0.v, K_S, SpMV + t.s/t.t, K_XR, (mixed: update check, gated FP64 residual, residual
-// replacement), K_P]. K_P ends the body, so the body that meets the stop test ends at the test:
-// no kernel after it runs for nothing.
+// replacement), K_P], or in the merged FP64 loop [SpMV + r0.v, K_S + r0.s, SpMV + t.s/t.t/r0.t,
+// K_XRP]. The kernel with the stop tests ends each iteration, and the loop's SpMVs read the status
+// word and do nothing once it is terminal, so the body that meets the stop test wastes at most
+// the skipped launches after it.
 template <typename T>
 hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R, T *R0, T *P, T *V, T *S, T *Tv,
-                        double *part_xr, double *part_s, bool fp32) {
+                        double *part_xr, double *part_s, bool fp32, bool merged) {
     hhp_mat *A = s->A;
     constexpr int E = Unit<T>::E;
     const int nu = s->n_pad / E, nu4 = s->n_pad / 4;
     const PlanDev &pl = fp32 ? A->plan32 : A->plan64;
+    const int *stop = &sc->status;
     hhp_status st = HHP_OK;
     auto kp = [&](cudaStream_t q, cudaGraphConditionalHandle c, int first_in_body) -> hhp_status {
         HHP_CUDA(launch_k(k_p<T>, dim3(s->nblk), dim3(s->nthr), 0, q, sc, P, V, R, nu, part_xr, part_s, s->nblk,
@@ -868,24 +1030,43 @@ hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R,
     HHP_TRY(kp(stream, cond, 0));  // stop tests on the initial residual, before the node
     HHP_TRY(begin_loop_body(s, stream, cond));
     for (int k = 0; k < s->unroll && st == HHP_OK; ++k) {
+        if constexpr (std::is_same<T, double>::value) {
+            if (merged) {
+                st = launch_spmv64(A, s->s2, EP_DOT1, P, V, R0, 1.0, 0.0, nullptr, nullptr, stop);
+                if (st != HHP_OK) break;
+                if (launch_k(k_s<double, true>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, sc, S, R, V, R0, nu,
+                             parts_of(pl), part_s) != cudaSuccess) {
+                    st = HHP_ERR_CUDA;
+                    break;
+                }
+                st = launch_spmv64(A, s->s2, EP_DOT3, S, Tv, S, 1.0, 0.0, nullptr, R0, stop);
+                if (st != HHP_OK) break;
+                if (launch_k(k_xrp<double>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, sc, X, R, P, S, Tv, V, nu,
+                             parts_of(pl), part_s, s->nblk, s->hist, s->hist_cap, cond, k == 0 ? 1 : 0,
+                             A->ctx->dev_err, 1) != cudaSuccess)
+                    st = HHP_ERR_CUDA;
+                continue;
+            }
+        }
         if (fp32)
             st = launch_spmv32(A, s->s2, EP_DOT1, reinterpret_cast<const float *>(P), reinterpret_cast<float *>(V),
-                               reinterpret_cast<const float *>(R0));
+                               reinterpret_cast<const float *>(R0), stop);
         else
             st = launch_spmv64(A, s->s2, EP_DOT1, reinterpret_cast<const double *>(P), reinterpret_cast<double *>(V),
-                               reinterpret_cast<const double *>(R0), 1.0, 0.0);
+                               reinterpret_cast<const double *>(R0), 1.0, 0.0, nullptr, nullptr, stop);
         if (st != HHP_OK) break;
-        if (launch_k(k_s<T>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, sc, S, R, V, nu, parts_of(pl), part_s) !=
+        if (launch_k(k_s<T>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, sc, S, R, V, R0, nu, parts_of(pl), part_s) !=
             cudaSuccess) {
             st = HHP_ERR_CUDA;
             break;
         }
         if (fp32)
             st = launch_spmv32(A, s->s2, EP_DOT2, reinterpret_cast<const float *>(S), reinterpret_cast<float *>(Tv),
-                               reinterpret_cast<const float *>(S));
+                               reinterpret_cast<const float *>(S), stop);
         else
             st = launch_spmv64(A, s->s2, EP_DOT2, reinterpret_cast<const double *>(S),
-                               reinterpret_cast<double *>(Tv), reinterpret_cast<const double *>(S), 1.0, 0.0);
+                               reinterpret_cast<double *>(Tv), reinterpret_cast<const double *>(S), 1.0, 0.0, nullptr,
+                               nullptr, stop);
         if (st != HHP_OK) break;
         if (launch_k(k_xr<T>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, sc, X, R, P, S, Tv, R0, nu, parts_of(pl),
                      part_s, s->nblk, part_xr) != cudaSuccess) {
@@ -923,28 +1104,46 @@ hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R,
 // The FP64 loop launched kernel by kernel (no graph), for profilers that cannot see inside
 // conditional graph nodes: same kernels and order; the host reads the status every `unroll`
 // iterations. Selected with HHP_SOLVE_GRAPH=0.
-hhp_status run_direct64(Solver *s) {
+hhp_status run_direct64(Solver *s, bool merged) {
     hhp_mat *A = s->A;
     cudaStream_t st = A->ctx->stream;
     const int nu = s->n_pad / 2;
+    const int *stop = &s->sc->status;
     HHP_CUDA(cudaMemcpyAsync(s->sc, s->h_sc, kCtlBytes, cudaMemcpyHostToDevice, st));
     HHP_TRY(launch_spmv64(A, st, EP_RESID, s->X, s->R, s->B, 1.0, 0.0));
     HHP_CUDA(launch_k(k_init<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->R, s->R0, s->P, s->V, nu,
                       parts_of(A->plan64), s->part_xr, s->part_s));
     A->ctx->kernel_launches += 1;
     const PlanDev &pl = A->plan64;
+    auto kp = [&](int first) -> hhp_status {
+        HHP_CUDA(launch_k(k_p<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->P, s->V, s->R, nu, s->part_xr,
+                          s->part_s, s->nblk, s->hist, s->hist_cap, cudaGraphConditionalHandle(), first,
+                          A->ctx->dev_err, 0));
+        A->ctx->kernel_launches += 1;
+        return HHP_OK;
+    };
+    if (merged) HHP_TRY(kp(0));  // stop tests on the initial residual
     for (;;) {
         for (int k = 0; k < s->unroll; ++k) {
-            HHP_CUDA(launch_k(k_p<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->P, s->V, s->R, nu,
-                              s->part_xr, s->part_s, s->nblk, s->hist, s->hist_cap, cudaGraphConditionalHandle(),
-                              k == 0, A->ctx->dev_err, 0));
-            HHP_TRY(launch_spmv64(A, st, EP_DOT1, s->P, s->V, s->R0, 1.0, 0.0));
-            HHP_CUDA(launch_k(k_s<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->S, s->R, s->V, nu,
+            if (merged) {
+                HHP_TRY(launch_spmv64(A, st, EP_DOT1, s->P, s->V, s->R0, 1.0, 0.0, nullptr, nullptr, stop));
+                HHP_CUDA(launch_k(k_s<double, true>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->S, s->R, s->V,
+                                  s->R0, nu, parts_of(pl), s->part_s));
+                HHP_TRY(launch_spmv64(A, st, EP_DOT3, s->S, s->T, s->S, 1.0, 0.0, nullptr, s->R0, stop));
+                HHP_CUDA(launch_k(k_xrp<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->X, s->R, s->P, s->S,
+                                  s->T, s->V, nu, parts_of(pl), s->part_s, s->nblk, s->hist, s->hist_cap,
+                                  cudaGraphConditionalHandle(), k == 0 ? 1 : 0, A->ctx->dev_err, 0));
+                A->ctx->kernel_launches += 2;
+                continue;
+            }
+            HHP_TRY(kp(k == 0));
+            HHP_TRY(launch_spmv64(A, st, EP_DOT1, s->P, s->V, s->R0, 1.0, 0.0, nullptr, nullptr, stop));
+            HHP_CUDA(launch_k(k_s<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->S, s->R, s->V, s->R0, nu,
                               parts_of(pl), s->part_s));
-            HHP_TRY(launch_spmv64(A, st, EP_DOT2, s->S, s->T, s->S, 1.0, 0.0));
+            HHP_TRY(launch_spmv64(A, st, EP_DOT2, s->S, s->T, s->S, 1.0, 0.0, nullptr, nullptr, stop));
             HHP_CUDA(launch_k(k_xr<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->X, s->R, s->P, s->S, s->T,
                               s->R0, nu, parts_of(pl), s->part_s, s->nblk, s->part_xr));
-            A->ctx->kernel_launches += 3;
+            A->ctx->kernel_launches += 2;
         }
         HHP_CUDA(cudaMemcpyAsync(s->h_sc, s->sc, sizeof(DevScal), cudaMemcpyDeviceToHost, st));
         HHP_CUDA(cudaStreamSynchronize(st));
@@ -957,8 +1156,9 @@ hhp_status run_direct64(Solver *s) {
     return HHP_OK;
 }
 
-// FP64 solve graph: ctl copy, residual SpMV, init, WHILE{loop}, true-residual SpMV, finish.
-hhp_status build_g64(Solver *s) {
+// FP64 solve graph (classic or merged loop): ctl copy, residual SpMV, init, WHILE{loop},
+// true-residual SpMV, finish.
+hhp_status build_g64(Solver *s, bool merged) {
     hhp_mat *A = s->A;
     cudaStream_t st = A->ctx->stream;
     HHP_TRY(ensure_plan(A, false));
@@ -975,7 +1175,7 @@ hhp_status build_g64(Solver *s) {
         HHP_CUDA(launch_k(k_init<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->R, s->R0, s->P, s->V, nu,
                           parts_of(A->plan64), s->part_xr, s->part_s));
         rc = capture_loop<double>(s, st, s->sc, s->X, s->R, s->R0, s->P, s->V, s->S, s->T, s->part_xr, s->part_s,
-                                  false);
+                                  false, merged);
         if (rc != HHP_OK) break;
         rc = launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0);
         if (rc != HHP_OK) break;
@@ -988,7 +1188,8 @@ hhp_status build_g64(Solver *s) {
         return rc;
     }
     HHP_CUDA(e);
-    cudaError_t ie = cudaGraphInstantiate(&s->g64, g, 0);
+    cudaGraphExec_t &ge = merged ? s->g64m : s->g64;
+    cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
     cudaGraphDestroy(g);
     HHP_CUDA(ie);
     s->g64_kernels_pro = 3;
@@ -1019,7 +1220,7 @@ hhp_status build_gmix(Solver *s) {
         HHP_CUDA(launch_k(k_mix_init, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc32, s->Y, s->R32, s->R0_32, s->D32,
                           s->P32, s->V32, nu4, parts_of(A->plan64), s->part_xr32, s->part_s32));
         rc = capture_loop<float>(s, st, s->sc32, s->D32, s->R32, s->R0_32, s->P32, s->V32, s->S32, s->T32,
-                                 s->part_xr32, s->part_s32, true);
+                                 s->part_xr32, s->part_s32, true, false);
         if (rc != HHP_OK) break;
         HHP_CUDA(launch_k(k_mix_final, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc32, s->X, s->D32, nu4));
         rc = launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0);
@@ -1131,7 +1332,13 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
     // after a breakdown, each pass a fresh residual and shadow residual of X.
     auto fp64_passes = [&](int it_before) -> hhp_status {
         const bool use_graph = env_int("HHP_SOLVE_GRAPH", 1) != 0;
-        if (use_graph && !s->g64) HHP_TRY(build_g64(s));
+        // the merged loop unless the caller asked for the classic one or for the reference's
+        // fixed-iteration runs (which follow its dot products exactly); an adjoint solve has
+        // resolved AUTO to CLASSIC before it gets here
+        const bool merged = o->loop != HHP_LOOP_CLASSIC && !h.fixed;
+        cudaGraphExec_t &ge = merged ? s->g64m : s->g64;
+        if (use_graph && !ge) HHP_TRY(build_g64(s, merged));
+        const long long per_iter = merged ? 4 : 5;
         h.maxit = o->maxit - it_before;
         int dev_status = ST_RUNNING;
         double prev_true = INFINITY;
@@ -1139,13 +1346,14 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
             h.restart = pass > 0 ? 1 : 0;
             h.first_outer = 0;
             if (use_graph) {
-                HHP_CUDA(cudaGraphLaunch(s->g64, st));
+                HHP_CUDA(cudaGraphLaunch(ge, st));
             } else {
-                HHP_TRY(run_direct64(s));
+                HHP_TRY(run_direct64(s, merged));
             }
             HHP_TRY(readback(s->h_sc, s->sc));
             ++outer;
-            if (use_graph) ctx->kernel_launches += s->g64_kernels_pro + s->g64_kernels_epi + 5LL * s->unroll * h.bodies;
+            if (use_graph)
+                ctx->kernel_launches += s->g64_kernels_pro + s->g64_kernels_epi + per_iter * s->unroll * h.bodies;
             dev_status = h.status;
             // Residual replacement: the recursive residual met the threshold but the true one
             // did not (rounding drift); restart from the current iterate, whose true residual
@@ -1266,6 +1474,7 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
 void solver_release(Solver *s) {
     if (!s) return;
     if (s->g64) cudaGraphExecDestroy(s->g64);
+    if (s->g64m) cudaGraphExecDestroy(s->g64m);
     if (s->gmix) cudaGraphExecDestroy(s->gmix);
     double *d[] = {s->X, s->B, s->R, s->R0, s->P, s->V, s->S, s->T, s->Y, s->part_xr, s->part_s, s->part_xr32,
                    s->part_s32, s->hist};
@@ -1292,7 +1501,9 @@ hhp_status backward_dev(hhp_mat *A, const double *x_dev, const double *g_dev, do
     cudaStream_t st = ctx->stream;
     // lambda starts from zero
     HHP_CUDA(cudaMemsetAsync(dldb_dev, 0, sizeof(double) * static_cast<size_t>(A->n), st));
-    hhp_status rc = solve_dev(A->t, g_dev, dldb_dev, nullptr, o, info);
+    hhp_solve_opts oa = *o;
+    if (oa.loop == HHP_LOOP_AUTO) oa.loop = HHP_LOOP_CLASSIC;
+    hhp_status rc = solve_dev(A->t, g_dev, dldb_dev, nullptr, &oa, info);
     if (rc != HHP_OK && rc != HHP_ERR_MAXIT) return rc;
     if (dlda_dev) HHP_TRY(launch_dlda(A, st, dldb_dev, x_dev, dlda_dev));
     HHP_CUDA(cudaStreamSynchronize(st));

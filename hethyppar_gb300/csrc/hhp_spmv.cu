@@ -23,8 +23,9 @@
 //    chunk. Work units (slices and chunks) are dealt to warps at plan time, longest first to the
 //    least-loaded warp, so power-law matrices stay balanced; every warp walks a fixed list, so
 //    every reduction has a fixed order and results are reproducible run to run.
-//  * Epilogues fuse the BiCGStab dot products (r0.v, t.s, t.t) and the residual r = b - A x into
-//    the store of y; one partial per CTA, summed in a fixed order by the consumer.
+//  * Epilogues fuse the BiCGStab dot products (r0.v, t.s, t.t, and r0.t for the merged loop) and
+//    the residual r = b - A x into the store of y; one partial per CTA, summed in a fixed order by
+//    the consumer.
 #include <algorithm>
 #include <cstring>
 #include <mutex>
@@ -122,9 +123,11 @@ struct SellArgs {
     const VT *x;
     VT *y;
     const VT *w1;
+    const VT *w2;      // EP_DOT3's second dot operand
     double alpha, beta;
     int scale, accum;  // alpha != 1, beta != 0 (decided on the host)
     const int *gate;   // nullable: skip the whole launch when *gate == 0
+    const int *stop;   // nullable: skip the whole launch when *stop != 0
     int *err;
     int m, n_slices, n_chunks;
     bool has_perm;
@@ -138,10 +141,10 @@ __device__ __forceinline__ T comp(const V &v, int t) {
     return reinterpret_cast<const T *>(&v)[t];
 }
 
-// Row epilogue: stores y[r]; accumulates dot partials into (d0, d1), in the value type (the
+// Row epilogue: stores y[r]; accumulates dot partials into (d0, d1, d2), in the value type (the
 // caller folds them into FP64 once per slice for FP32 data).
 template <typename VT, int EP, typename DT>
-__device__ __forceinline__ void row_epilogue(const SellArgs<VT> &a, int r, VT acc, DT &d0, DT &d1) {
+__device__ __forceinline__ void row_epilogue(const SellArgs<VT> &a, int r, VT acc, DT &d0, DT &d1, DT &d2) {
     if (EP == EP_Y) {
         a.y[r] = acc;
     } else if (EP == EP_AXPBY) {
@@ -156,6 +159,11 @@ __device__ __forceinline__ void row_epilogue(const SellArgs<VT> &a, int r, VT ac
         a.y[r] = acc;
         d0 = vfma(static_cast<DT>(acc), static_cast<DT>(__ldg(a.w1 + r)), d0);
         d1 = vfma(static_cast<DT>(acc), static_cast<DT>(acc), d1);
+    } else if (EP == EP_DOT3) {
+        a.y[r] = acc;
+        d0 = vfma(static_cast<DT>(acc), static_cast<DT>(__ldg(a.w1 + r)), d0);
+        d1 = vfma(static_cast<DT>(acc), static_cast<DT>(acc), d1);
+        d2 = vfma(static_cast<DT>(acc), static_cast<DT>(__ldg(a.w2 + r)), d2);
     } else {  // EP_RESID
         const VT b = __ldg(a.w1 + r);
         const VT res = b - acc;
@@ -166,7 +174,8 @@ __device__ __forceinline__ void row_epilogue(const SellArgs<VT> &a, int r, VT ac
 }
 
 template <typename VT, int R, int U, int EP, bool D16>
-__device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, int lane, double &d0, double &d1) {
+__device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, int lane, double &d0, double &d1,
+                                         double &d2) {
     using VV = typename Vec<VT, R>::V;
     using IV = typename Vec<VT, R>::I;
     using CW = typename std::conditional<D16, typename Vec<VT, R>::I16, IV>::type;  // index word
@@ -249,16 +258,17 @@ __device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, int lane,
         for (int t = 0; t < R; ++t)
             if (j < len[t]) acc[t] = vfma(comp<VV, VT>(vt, t), xt[t], acc[t]);
     }
-    VT e0 = VT(0), e1 = VT(0);
+    VT e0 = VT(0), e1 = VT(0), e2 = VT(0);
 #pragma unroll
     for (int t = 0; t < R; ++t) {
         const int r = row[t];
-        if (r >= 0 && r < a.m) row_epilogue<VT, EP>(a, r, acc[t], e0, e1);
+        if (r >= 0 && r < a.m) row_epilogue<VT, EP>(a, r, acc[t], e0, e1, e2);
     }
     if (EP != EP_AXPBY && EP != EP_Y) {
         d0 += static_cast<double>(e0);
         d1 += static_cast<double>(e1);
     }
+    if (EP == EP_DOT3) d2 += static_cast<double>(e2);
 }
 
 template <typename VT, int EP>
@@ -293,9 +303,14 @@ __device__ __forceinline__ void do_chunk(const SellArgs<VT> &a, int c, int lane)
             double tot = 0.0;
             for (int q = 0; q < nch; ++q) tot += __ldcg(a.chunk_part + c_first + q);
             a.long_cnt[l] = 0u;  // ready for the next launch
-            double e0 = 0.0, e1 = 0.0;
-            row_epilogue<VT, EP, double>(a, d.x, static_cast<VT>(tot), e0, e1);
-            if (EP != EP_AXPBY && EP != EP_Y) {
+            double e0 = 0.0, e1 = 0.0, e2 = 0.0;
+            row_epilogue<VT, EP, double>(a, d.x, static_cast<VT>(tot), e0, e1, e2);
+            if (EP == EP_DOT3) {
+                a.long_dot[4 * l] = e0;
+                a.long_dot[4 * l + 1] = e1;
+                a.long_dot[4 * l + 2] = e2;
+                a.long_dot[4 * l + 3] = 0.0;
+            } else if (EP != EP_AXPBY && EP != EP_Y) {
                 a.long_dot[2 * l] = e0;
                 a.long_dot[2 * l + 1] = e1;
             }
@@ -314,18 +329,32 @@ __global__ void __launch_bounds__(256, MinCtas<R, U>::value) k_spmv(const SellAr
     // After a recorded device error every later launch returns at once (uniform across the grid).
     if (*reinterpret_cast<volatile const int *>(a.err) != DEV_OK) return;
     if (a.gate && *a.gate == 0) return;
-    __shared__ double red[16];
+    if (a.stop && *reinterpret_cast<volatile const int *>(a.stop) != 0) return;
+    __shared__ double red[32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int gw = blockIdx.x * nw + warp;
-    double d0 = 0.0, d1 = 0.0;
+    double d0 = 0.0, d1 = 0.0, d2 = 0.0;
     // this warp's units, balanced at plan time (fixed order: reductions are reproducible)
     const int ub = a.warp_ptr[gw], ue = a.warp_ptr[gw + 1];
     for (int i = ub; i < ue; ++i) {
         const int u = __ldg(a.warp_units + i);
-        if (u < a.n_slices) do_slice<VT, R, U, EP, D16>(a, u, lane, d0, d1);
+        if (u < a.n_slices) do_slice<VT, R, U, EP, D16>(a, u, lane, d0, d1, d2);
         else do_chunk<VT, EP>(a, u - a.n_slices, lane);
     }
-    if (EP != EP_AXPBY && EP != EP_Y) {
+    if (EP == EP_DOT3) {
+        // records of 4: (d0, d1, d2, 0); each warp's transposed butterfly leaves quantity q in
+        // lanes [8q, 8q + 8), warp 0 adds the warps' results within each group of 8 lanes
+        const double dv[4] = {d0, d1, d2, 0.0};
+        const double r = warp_reduce<4>(dv, lane);
+        if ((lane & 7) == 0) red[lane + warp] = r;  // red[8q + warp], nw <= 8
+        __syncthreads();
+        if (warp == 0) {
+            double s = (lane < 24 && (lane & 7) < nw) ? red[lane] : 0.0;
+#pragma unroll
+            for (int o = 4; o >= 1; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if ((lane & 7) == 0) a.cta_part[4 * blockIdx.x + (lane >> 3)] = s;
+        }
+    } else if (EP != EP_AXPBY && EP != EP_Y) {
         // per-CTA partial: each warp folds its lanes' (d0, d1) with a transposed butterfly
         // (5 FP64 adds for both sums), warp 0 adds the warps' results; fixed order throughout
         warp_sum2(d0, d1, lane);
@@ -349,6 +378,10 @@ cudaError_t launch_rud(EpKind ep, const PlanDev &p, const SellArgs<VT> &a, cudaS
     switch (ep) {
         case EP_DOT1: return launch_k(k_spmv<VT, R, U, EP_DOT1, D16>, grid, block, 0, s, a);
         case EP_DOT2: return launch_k(k_spmv<VT, R, U, EP_DOT2, D16>, grid, block, 0, s, a);
+        case EP_DOT3:
+            if constexpr (std::is_same<VT, double>::value)
+                return launch_k(k_spmv<VT, R, U, EP_DOT3, D16>, grid, block, 0, s, a);
+            return cudaErrorInvalidValue;
         case EP_RESID: return launch_k(k_spmv<VT, R, U, EP_RESID, D16>, grid, block, 0, s, a);
         default:
             // y = A x needs no epilogue arithmetic: a separate instantiation keeps the FP64 pipe
@@ -516,10 +549,10 @@ hhp_status build_plan_dev(hhp_mat *A, PlanDev &p) {
     HHP_CUDA(cudaMalloc(&p.chunk_part, sizeof(double) * std::max(1, p.n_chunks)));
     HHP_CUDA(cudaMalloc(&p.long_cnt, sizeof(unsigned) * std::max(1, p.n_long)));
     HHP_CUDA(cudaMemset(p.long_cnt, 0, sizeof(unsigned) * std::max(1, p.n_long)));
-    HHP_CUDA(cudaMalloc(&p.long_dot, sizeof(double) * 2 * std::max(1, p.n_long)));
-    HHP_CUDA(cudaMemset(p.long_dot, 0, sizeof(double) * 2 * std::max(1, p.n_long)));
-    HHP_CUDA(cudaMalloc(&p.cta_part, sizeof(double) * 2 * p.ctas));
-    HHP_CUDA(cudaMemset(p.cta_part, 0, sizeof(double) * 2 * p.ctas));
+    HHP_CUDA(cudaMalloc(&p.long_dot, sizeof(double) * 4 * std::max(1, p.n_long)));
+    HHP_CUDA(cudaMemset(p.long_dot, 0, sizeof(double) * 4 * std::max(1, p.n_long)));
+    HHP_CUDA(cudaMalloc(&p.cta_part, sizeof(double) * 4 * p.ctas));
+    HHP_CUDA(cudaMemset(p.cta_part, 0, sizeof(double) * 4 * p.ctas));
     HHP_TRY(fill_values<VT>(A, p, true));
     HHP_CUDA(cudaStreamSynchronize(ctx->stream));
     return HHP_OK;
@@ -549,11 +582,13 @@ SellArgs<VT> make_args(hhp_mat *A, const PlanDev &p, const VT *csr_val, const VT
     a.x = x;
     a.y = y;
     a.w1 = w1;
+    a.w2 = nullptr;
     a.alpha = alpha;
     a.beta = beta;
     a.scale = alpha != 1.0 ? 1 : 0;
     a.accum = beta != 0.0 ? 1 : 0;
     a.gate = nullptr;
+    a.stop = nullptr;
     a.err = A->ctx->dev_err;
     a.m = A->m;
     a.n_slices = p.n_slices;
@@ -597,17 +632,20 @@ hhp_status refresh_plan_values(hhp_mat *A) {
 }
 
 hhp_status launch_spmv64(hhp_mat *A, cudaStream_t stream, EpKind ep, const double *x, double *y, const double *w1,
-                         double alpha, double beta, const int *gate) {
+                         double alpha, double beta, const int *gate, const double *w2, const int *stop) {
     HHP_TRY(ensure_plan(A, false));
     const PlanDev &p = A->plan64;
     SellArgs<double> a = make_args<double>(A, p, A->val, x, y, w1, alpha, beta);
     a.gate = gate;
+    a.w2 = w2;
+    a.stop = stop;
     HHP_CUDA(launch_ep<double>(ep, p, a, stream));
     A->ctx->kernel_launches += 1;
     return HHP_OK;
 }
 
-hhp_status launch_spmv32(hhp_mat *A, cudaStream_t stream, EpKind ep, const float *x, float *y, const float *w1) {
+hhp_status launch_spmv32(hhp_mat *A, cudaStream_t stream, EpKind ep, const float *x, float *y, const float *w1,
+                         const int *stop) {
     if (!A->val32) {
         set_error("FP32 SpMV requested before the FP32 copy of the values was built");
         return HHP_ERR_STATE;
@@ -615,6 +653,7 @@ hhp_status launch_spmv32(hhp_mat *A, cudaStream_t stream, EpKind ep, const float
     HHP_TRY(ensure_plan(A, true));
     const PlanDev &p = A->plan32;
     SellArgs<float> a = make_args<float>(A, p, A->val32, x, y, w1, 1.0, 0.0);
+    a.stop = stop;
     HHP_CUDA(launch_ep<float>(ep, p, a, stream));
     A->ctx->kernel_launches += 1;
     return HHP_OK;

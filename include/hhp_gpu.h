@@ -52,6 +52,16 @@ typedef enum { HHP_PREC_FP64 = 0, HHP_PREC_MIXED = 1 } hhp_precision;
  * reported residual are those of A x = b. Needs a nonzero diagonal (HHP_ERR_ARG otherwise). */
 typedef enum { HHP_PRECOND_NONE = 0, HHP_PRECOND_JACOBI = 1 } hhp_precond;
 
+/* FP64 iteration schedule. MERGED: the stop tests and beta come from the dot products of the
+ * t = A s step (||r_new||^2 = s.s - omega t.s, r0.r_new = r0.s - omega r0.t), so one iteration is
+ * 4 kernels (two SpMVs and two fused vector kernels) instead of 5. CLASSIC: the reference's order
+ * (src/entry/bicgstab_gpu_dp.c:165-196): rho_new = r.r0 and ||r|| as direct dot products of the
+ * new residual. AUTO (0, the default): MERGED for hhp_bicgstab*, CLASSIC for the adjoint solve of
+ * hhp_bicgstab_backward* (whose tolerances sit near the rounding floor, where the direct dot
+ * products reach a lower true residual). Fixed-iteration runs always use CLASSIC; the FP32 inner
+ * loop of the mixed form is classic. */
+typedef enum { HHP_LOOP_AUTO = 0, HHP_LOOP_MERGED = 1, HHP_LOOP_CLASSIC = 2 } hhp_loop;
+
 typedef struct {
     double rtol;        /* stop when ||b - A x|| <= rtol * ||b|| (the relative residual the reference
                            prints, bicgstab_cpu.c:251-255; equal to gpu_BiCGStab's threshold
@@ -68,6 +78,7 @@ typedef struct {
     hhp_iter_cb cb;
     void *user;
     int precond;        /* hhp_precond (forward solves; the adjoint runs unpreconditioned)        */
+    int loop;           /* hhp_loop                                                               */
 } hhp_solve_opts;
 
 typedef struct {

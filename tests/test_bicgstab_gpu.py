@@ -155,3 +155,43 @@ def test_host_solve_in_place(ctx):
     x_in, r2 = bicgstab(ctx, A, g["b"], x0, rtol=1e-10, maxit=500, inplace=True)
     assert x_in is x0 and np.array_equal(x0, x_copy) and r1.iters == r2.iters
     A.close()
+
+
+@pytest.mark.parametrize("name", SOLVE_CASES)
+def test_merged_and_classic_loops_both_meet_the_reference_bar(ctx, name):
+    """The merged schedule (||r||^2 and r0.r of the new residual from the t = A s dot products,
+    4 kernels per iteration) and the classic one (the reference's direct dot products) each reach
+    the tolerance within the reference's iteration bar, and agree with each other on x."""
+    g = load_golden(name)
+    k_ref = int(g["iters_to_1e-10"])
+    if k_ref < 0:
+        pytest.skip("the reference does not reach 1e-10 on this case")
+    A = Matrix.from_csr(ctx, g["rowptr"], g["col"], g["val"])
+    xs = {}
+    for loop in ("merged", "classic"):
+        x, r = bicgstab(ctx, A, g["b"], g["x0"], rtol=1e-10, maxit=max(len(g["relres_hist"]), 10), loop=loop)
+        assert r.status == 0 and r.rel_res_true <= 1e-10, (loop, r)
+        assert _within_5pct(r.iters, k_ref), (loop, r.iters, k_ref)
+        res = g["b"] - orc.spmv(g["rowptr"], g["col"], g["val"], x)
+        assert math.sqrt(orc.dot(res, res) / orc.dot(g["b"], g["b"])) <= 1.0000001e-10
+        xs[loop] = x
+    scale = np.max(np.abs(xs["classic"]))
+    assert np.max(np.abs(xs["merged"] - xs["classic"])) <= 1e-6 * scale
+
+
+@pytest.mark.parametrize("cfg", ["c1", "c2"])
+def test_merged_loop_is_four_kernels_per_iteration(ctx, cfg):
+    s = synth.config(cfg)
+    A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
+    for loop, per_iter in (("merged", 4), ("classic", 5)):
+        bicgstab(ctx, A, s.b, s.x0, rtol=1e-10, maxit=3000, loop=loop)  # builds the graph
+        n0 = ctx.kernel_launches
+        x, r = bicgstab(ctx, A, s.b, s.x0, s.x_target, rtol=1e-10, maxit=3000, loop=loop)
+        n = ctx.kernel_launches - n0
+        assert r.status == 0 and r.rel_res_true <= 1e-10 and r.err_vs_target <= 1e-6
+        if r.outer_iters == 1:
+            # residual SpMV, init, first stop test; 2 iterations per loop body (a body that
+            # stops after its first iteration still launches its second, which returns at once);
+            # true-residual SpMV and finish
+            assert n == 3 + per_iter * 2 * math.ceil(r.iters / 2) + 2, (loop, n, r.iters)
+    A.close()
