@@ -171,7 +171,7 @@ def traffic_from_profile():
 
 def run_ours(args, rk):
     import torch
-    from hethyppar_gb300 import Context, Matrix, bicgstab, bicgstab_backward, spmv_bytes, synth
+    from hethyppar_gb300 import Context, Matrix, bicgstab, bicgstab_backward, reorder_rcm, spmv_bytes, synth
     from hethyppar_gb300 import dist
 
     dev = rk.local_rank
@@ -423,6 +423,55 @@ def run_ours(args, rk):
                 "max_rel_diff_x_vs_fp64": float((x5_mixed - x5_64).abs().max().item() / x5_64.abs().max().item())}
         except Exception as e:  # reported, not fatal: the FP64 numbers above stand
             out["adjoint"]["mixed"] = {"error": str(e)}
+
+        # locality reordering: the 1024^2 stencil with its rows and columns scrambled by a seeded
+        # permutation, then put back in order by reverse Cuthill-McKee (host, one-time)
+        try:
+            q = np.random.default_rng(11).permutation(s5.m).astype(np.int32)
+            As = Matrix.from_csr(ctx, s5.rowptr, s5.col, s5.val, perm=q)
+            rp_s, cl_s, vl_s = As.get_csr()
+            t0 = time.perf_counter()
+            p = reorder_rcm(rp_s, cl_s)
+            t_rcm = time.perf_counter() - t0
+            Ar = Matrix.from_csr(ctx, rp_s, cl_s, vl_s, perm=p)
+            xr = torch.randn(s5.n, dtype=torch.float64, device="cuda")
+            yr = torch.empty(s5.m, dtype=torch.float64, device="cuda")
+
+            def spmv_us(M):
+                for _ in range(3):
+                    M.spmv_dev(xr, yr)
+                ts = []
+                for _ in range(20):
+                    torch.cuda.synchronize()
+                    flush_l2(sync=False)
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    M.spmv_dev(xr, yr)
+                    e1.record(stream)
+                    e1.synchronize()
+                    ts.append(e0.elapsed_time(e1))
+                return statistics.mean(ts) * 1e3
+
+            def solve_s(M, bb):
+                xx = torch.zeros_like(b5)
+                bicgstab(ctx, M, bb, xx, rtol=1e-10, maxit=50000)
+                xx.zero_()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                r = bicgstab(ctx, M, bb, xx, rtol=1e-10, maxit=50000)[1]
+                return time.perf_counter() - t0, r.iters
+
+            b_s = b5[torch.as_tensor(q, device="cuda").long()]
+            b_r = b_s[torch.as_tensor(p, device="cuda").long()]
+            t_s, it_s = solve_s(As, b_s)
+            t_r, it_r = solve_s(Ar, b_r)
+            out["reorder"] = {"workload": "c5 (2D 5-point 1024^2) with rows and columns scrambled by a seeded permutation",
+                              "rcm_host_s": t_rcm, "spmv_us_original": spmv_us(A5), "spmv_us_scrambled": spmv_us(As),
+                              "spmv_us_rcm": spmv_us(Ar), "solve_s_scrambled": t_s, "solve_s_rcm": t_r,
+                              "iters_scrambled": it_s, "iters_rcm": it_r}
+            del As, Ar
+        except Exception as e:  # reported, not fatal
+            out["reorder"] = {"error": str(e)}
 
     if rk.rank == 0 and rk.world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(s)

@@ -90,6 +90,7 @@ SIGNATURES = [
     ("hhp_mtx_read", _I, [_S, _PI, _PI, _PI, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P)]),
     ("hhp_free", None, [_P]),
     ("hhp_csr_file_write", _I, [_S, _I, _I, _I, _P, _P, _P]),
+    ("hhp_reorder_rcm", _I, [_I, _P, _P, _P]),
     ("hhp_plan_stats", _I, [_I, _I, _P, _I, _I, _PI, _PI, _PI, _PI, _PD]),
     ("hhp_plan_dump", _I, [_I, _I, _P, _I, _I, _I, _P, _P, _PI, _PI]),
     ("hhp_dp_vecop_P", None, [_P, _P, _P, _P, _P, _I, _P]),

@@ -297,6 +297,16 @@ def csr_file_write(path: str, rowptr, col, val, n: Optional[int] = None):
                                    _ptr(vl)), "hhp_csr_file_write")
 
 
+def reorder_rcm(rowptr, col) -> np.ndarray:
+    """Reverse Cuthill-McKee permutation of a square CSR pattern (hhp_reorder_rcm, host only), in
+    csr_permute's convention: pass it as Matrix.from_csr(..., perm=p), and b[p], x0[p] with it."""
+    rp, cl = _host(rowptr, np.int32), _host(col, np.int32)
+    m = rp.size - 1
+    perm = np.empty(max(m, 0), np.int32)
+    check(lib().hhp_reorder_rcm(m, _ptr(rp), _ptr(cl), _ptr(perm)), "hhp_reorder_rcm")
+    return perm
+
+
 def vector_read(path: str, size: int) -> np.ndarray:
     out = np.empty(size, np.float64)
     check(lib().hhp_vector_read(path.encode(), size, _ptr(out)), "hhp_vector_read")

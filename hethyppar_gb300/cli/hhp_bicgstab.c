@@ -18,6 +18,7 @@
  *   --print-every K   print "Iteration = i; Error Norm = e" every K iterations
  *                     (gpu_BiCGStab's per-iteration line, bicgstab_gpu.c:156)
  *   --out-format F    compat (default, "%lf" like vector_write) | exact ("%.17g")
+ *   --reorder rcm     reverse Cuthill-McKee row/column order (instead of a --perm file)
  *   --loop L          auto (default: merged) | merged (4 kernels per iteration) | classic (the
  *                     reference's dot products; --fixed always runs it)
  */
@@ -31,11 +32,11 @@
 
 #include "hhp_gpu.h"
 
-enum { OPT_RTOL = 1000, OPT_FIXED, OPT_PREC, OPT_XT, OPT_PERM, OPT_PRINT, OPT_OUTFMT, OPT_DEVICE, OPT_WCSR, OPT_PRECOND, OPT_LOOP };
+enum { OPT_RTOL = 1000, OPT_FIXED, OPT_PREC, OPT_XT, OPT_PERM, OPT_PRINT, OPT_OUTFMT, OPT_DEVICE, OPT_WCSR, OPT_PRECOND, OPT_LOOP, OPT_REORDER };
 
 struct arguments {
     char *input_matrix, *input_x, *input_y, *output_x, *x_target, *perm, *write_csr;
-    int n_iters, fixed, mixed, print_every, exact, device, jacobi, loop;
+    int n_iters, fixed, mixed, print_every, exact, device, jacobi, loop, rcm;
     double rtol;
 };
 
@@ -55,6 +56,8 @@ static struct argp_option options[] = {
     {"device", OPT_DEVICE, "ID", 0, "CUDA device (default 0)", 0},
     {"write-csr", OPT_WCSR, "FILE", 0, "Also store the matrix as a binary CSR file (later runs: -m FILE)", 0},
     {"precond", OPT_PRECOND, "none|jacobi", 0, "Preconditioner (default none, as the reference)", 0},
+    {"reorder", OPT_REORDER, "none|rcm", 0,
+     "Row/column reordering for locality: rcm = reverse Cuthill-McKee (instead of a --perm file)", 0},
     {"loop", OPT_LOOP, "auto|merged|classic", 0,
      "FP64 iteration schedule: merged (the default for a solve, 4 kernels per iteration) or classic (the reference's dot products)", 0},
     {0}};
@@ -85,6 +88,11 @@ static error_t parse_opt(int key, char *arg, struct argp_state *state) {
             break;
         case OPT_DEVICE: a->device = (int)strtol(arg, &end, 10); break;
         case OPT_WCSR: a->write_csr = arg; break;
+        case OPT_REORDER:
+            if (strcmp(arg, "rcm") == 0) a->rcm = 1;
+            else if (strcmp(arg, "none") == 0) a->rcm = 0;
+            else argp_error(state, "unknown reordering '%s'", arg);
+            break;
         case OPT_LOOP:
             if (strcmp(arg, "classic") == 0) a->loop = HHP_LOOP_CLASSIC;
             else if (strcmp(arg, "merged") == 0) a->loop = HHP_LOOP_MERGED;
@@ -159,6 +167,7 @@ int main(int argc, char **argv) {
     if (access(a.input_x, F_OK) == -1) FAIL("Input X '%s' does not exist", a.input_x);
     if (access(a.input_y, F_OK) == -1) FAIL("Input B '%s' does not exist", a.input_y);
     if (a.n_iters < 0) FAIL("-n must be >= 0");
+    if (a.rcm && a.perm) FAIL("--reorder rcm and --perm are exclusive");
 
     const double t_begin = now_s();
     hhp_ctx *ctx = NULL;
@@ -187,12 +196,14 @@ int main(int argc, char **argv) {
         XT = malloc(sizeof(double) * (size_t)n);
         CHECK(hhp_vector_read(a.x_target, n, XT));
     }
-    if (a.perm) {
+    if (a.perm || a.rcm) {
         perm = malloc(sizeof(int) * (size_t)m);
-        if (read_part(a.perm, m, perm) != 0) FAIL("cannot read a %d-entry partition vector from '%s'", m, a.perm);
+        if (a.perm && read_part(a.perm, m, perm) != 0)
+            FAIL("cannot read a %d-entry partition vector from '%s'", m, a.perm);
         int *rp = malloc(sizeof(int) * ((size_t)m + 1)), *cl = malloc(sizeof(int) * (size_t)(nnz > 0 ? nnz : 1));
         double *vl = malloc(sizeof(double) * (size_t)(nnz > 0 ? nnz : 1));
         CHECK(hhp_mat_get_csr(A, rp, cl, vl));
+        if (a.rcm) CHECK(hhp_reorder_rcm(m, rp, cl, perm));
         hhp_mat_destroy(A);
         A = NULL;
         CHECK(hhp_mat_from_csr(ctx, m, n, nnz, rp, cl, vl, perm, &A));

@@ -181,6 +181,14 @@ void hhp_free(void *p);
 hhp_status hhp_csr_file_write(const char *path, int m, int n, int nnz, const int *rowptr, const int *col,
                               const double *val);
 
+/* ---- locality reordering ------------------------------------------------------------------ */
+/* Reverse Cuthill-McKee order of the symmetrised pattern A + A^T of a square CSR (host only, no
+ * device needed): perm[m] in csr_permute's convention (src/util/hhp_dp_helpers.c:18-37), ready for
+ * hhp_mat_from_csr's perm argument. Replaces the offline PaToH partition files the reference
+ * orders rows by (src/entry/bicgstab_hybrid_dist_dp.c:217-233) when none is at hand. Deterministic;
+ * HHP_ERR_ARG for a malformed CSR. */
+hhp_status hhp_reorder_rcm(int m, const int *rowptr, const int *col, int *perm);
+
 /* ---- host-side helpers exposed for testing the work plan without a GPU ---------------------- */
 /* The SpMV work plan of a host CSR (rows_per_lane 2 = the FP64 kernel's slices of 64 rows, 4 =
  * the FP32 kernel's slices of 128 rows): number of slices, of long rows (cut into chunks of at

@@ -73,6 +73,20 @@ def test_cli_partition_permutation():
         assert np.max(np.abs(np.loadtxt(out) - np.arange(1, 17))) < 1e-8
 
 
+def test_cli_rcm_reorder():
+    g = load_golden("sample320")
+    with tempfile.TemporaryDirectory() as td:
+        p = _files(td, g)
+        out = os.path.join(td, "X.txt")
+        kv, _ = _run(["-m", p["A"], "-x", p["x0"], "-y", p["b"], "-o", out, "--reorder", "rcm", "-n", "500",
+                      "--rtol", "1e-12", "--out-format", "exact"])
+        assert float(kv["relative_residual"]) <= 1e-12
+        assert np.max(np.abs(np.loadtxt(out) - np.arange(1, 321))) < 1e-6
+        r = subprocess.run([EXE, "-m", p["A"], "-x", p["x0"], "-y", p["b"], "-o", out, "--reorder", "rcm", "--perm",
+                            p["x0"]], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        assert r.returncode != 0 and "exclusive" in r.stdout
+
+
 def test_cli_binary_csr_rerun_matches_text_run():
     g = load_golden("sample320")
     with tempfile.TemporaryDirectory() as td:
