@@ -23,8 +23,7 @@ enum : int {
 enum : int {
     ST_RUNNING = 0,
     ST_CONVERGED = 1,      // ||r|| <= threshold after a full iteration
-    ST_HALF = 2,           // ||s|| <= threshold: x += alpha*p is the last update (set mid-iteration)
-    ST_CONVERGED_HALF = 3, // terminal form of ST_HALF
+    ST_CONVERGED_HALF = 3, // ||s|| <= threshold: x += alpha*p was the last update
     ST_BREAKDOWN = 4,      // rho, (r0,v) or (t,t) is zero or not finite
     ST_MAXIT = 5,          // iteration cap reached
     ST_DEVICE_ERROR = 6,   // a kernel recorded a device error (e.g. a wait timeout)

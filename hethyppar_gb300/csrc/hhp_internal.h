@@ -135,7 +135,7 @@ hhp_status launch_spmv64(hhp_mat *A, cudaStream_t stream, EpKind ep, const doubl
                          double alpha, double beta, const int *gate = nullptr, const double *w2 = nullptr,
                          const int *stop = nullptr);
 hhp_status launch_spmv32(hhp_mat *A, cudaStream_t stream, EpKind ep, const float *x, float *y, const float *w1,
-                         const int *stop = nullptr);
+                         const int *stop = nullptr, const float *w2 = nullptr);
 // Number of partial records (ctas) and long-row records of the last-used plan, for the reducers.
 inline int plan_ctas(const hhp_mat *A, bool fp32) { return fp32 ? A->plan32.ctas : A->plan64.ctas; }
 

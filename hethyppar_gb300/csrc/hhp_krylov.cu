@@ -69,7 +69,7 @@ struct Solver {
     int hist_cap = 0;
     cudaStream_t s2 = nullptr, s3 = nullptr;  // capture streams: loop body, IF body
     cudaEvent_t ev_in = nullptr;              // joins the two input uploads
-    cudaGraphExec_t g64 = nullptr, g64m = nullptr, gmix = nullptr;  // FP64 classic / merged, mixed
+    cudaGraphExec_t g64 = nullptr, g64m = nullptr, gmix = nullptr, gmixm = nullptr;  // classic / merged
     int g64_kernels_pro = 0, g64_kernels_epi = 0, gmix_kernels_pro = 0, gmix_kernels_epi = 0, unroll = 4;
 };
 
@@ -171,6 +171,7 @@ __global__ void __launch_bounds__(512) k_init(DevScal *sc, const T *R, T *R0, T 
         }
         sc->iter_start = sc->iter;
         sc->bodies = 0;
+        sc->arrivals = 0;
         sc->rho_prev = 1.0;
         sc->alpha = 1.0;
         sc->omega = 1.0;
@@ -668,6 +669,7 @@ __global__ void __launch_bounds__(512) k_mix_init(DevScal *sc, const double *Rd,
             sc->updates = 0;
         }
         sc->thr2_rec = -1.0;
+        sc->arrivals = 0;
         sc->iter_start = sc->iter;
         sc->rho_prev = 1.0;
         sc->alpha = 1.0;
@@ -780,6 +782,138 @@ __global__ void __launch_bounds__(512) k_p_ru(DevScal *sc, double *X, float *D32
     }
 }
 
+// Mixed form, merged loop: K_XR and the reliable-update test of K_P_RU in one kernel, with
+// omega, ||r_new||^2 = s.s - omega t.s and r0.r_new = r0.s - omega r0.t from the partials of K_S
+// and of the t = A s SpMV (as in K_XRP). Without an update: d += alpha p + omega s,
+// r = s - omega t, beta, p = r + beta (p - omega v). With one: x += d + alpha p + omega s, d = 0,
+// and the IF node runs the FP64 residual, the residual replacement and K_P (r and p are left to
+// it). Divergence or a vanished t.t / rho ends the pass as a breakdown with d not folded.
+__global__ void __launch_bounds__(512) k_xrp_ru(DevScal *sc, double *X, float *D32, float *R, float *P, const float *S,
+                                                const float *Tv, const float *V, int nu4, SpmvParts sp,
+                                                const double *part_s, int nparts, double *hist, int hist_cap,
+                                                cudaGraphConditionalHandle wcond, cudaGraphConditionalHandle icond,
+                                                int first_in_body, const int *dev_err) {
+    __shared__ double red[kRedScratch];
+    __shared__ float bc[3];
+    __shared__ int go;  // 0: nothing, 1: d, r, p updates, 2: fold d + alpha p + omega s into x
+    const int stride = gridDim.x * blockDim.x, u0 = blockIdx.x * blockDim.x + threadIdx.x;
+    float d[kPre][4], p[kPre][4], s[kPre][4], t[kPre][4], vv[kPre][4];
+#pragma unroll
+    for (int k = 0; k < kPre; ++k) {
+        const int u = u0 + k * stride;
+        if (u < nu4) {
+            ldu(d[k], D32, u);
+            ldu(p[k], P, u);
+            ldu(s[k], S, u);
+            ldu(t[k], Tv, u);
+            ldu(vv[k], V, u);
+        }
+    }
+    double v[4], w[4];
+    reduce_pair<4>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, part_s, nparts, v, w, red);
+    if (threadIdx.x == 0) {
+        const bool lead = blockIdx.x == 0;
+        int what = 0, term = *reinterpret_cast<volatile const int *>(&sc->status);
+        if (lead && first_in_body) sc->bodies += 1;
+        if (term == ST_RUNNING) {
+            const double ts = v[0], tt = v[1], r0t = v[2], ss = w[0], r0s = w[1];
+            const double omega = ts / tt, alpha = sc->alpha;
+            const int it = sc->iter;
+            if (*reinterpret_cast<volatile const int *>(dev_err) != DEV_OK) {
+                term = ST_DEVICE_ERROR;
+            } else if (!finite_nonzero(tt) || !isfinite(omega)) {
+                term = ST_BREAKDOWN;
+            } else {
+                const double rr = fmax(ss - omega * ts, 0.0);
+                const double mx = sc->rr_max[it & 1];
+                bc[0] = static_cast<float>(alpha);
+                bc[1] = static_cast<float>(omega);
+                if (lead) sc->omega = omega;
+                if (!isfinite(rr) || rr > kDivergence2 * sc->true_rr) {
+                    term = ST_BREAKDOWN;  // d is not folded into x
+                } else if (rr <= sc->thr2 || rr < sc->inner_rtol2 * mx || it >= sc->maxit) {
+                    if (lead) {
+                        sc->rr_max[(it + 1) & 1] = mx;
+                        sc->ru_flag = 1;
+                    }
+                    what = 2;
+                } else {
+                    if (lead) sc->rr_max[(it + 1) & 1] = fmax(mx, rr);
+                    if (lead && it > sc->iter_start && it - 1 < hist_cap) hist[it - 1] = rr;
+                    const double rho_new = r0s - omega * r0t;
+                    if (!finite_nonzero(rho_new)) {
+                        term = ST_BREAKDOWN;
+                    } else {
+                        const double beta = (rho_new / sc->rho_prev) * (alpha / omega);
+                        bc[2] = static_cast<float>(beta);
+                        if (lead) {
+                            sc->rho_cur = rho_new;
+                            sc->beta = beta;
+                            sc->rr_last = rr;
+                        }
+                        what = 1;
+                    }
+                }
+            }
+        }
+        // the status as every block read it at launch stays until all have read it (see K_XRP)
+        __threadfence();
+        if (atomicAdd(&sc->arrivals, 1) == static_cast<int>(gridDim.x) - 1) {
+            sc->arrivals = 0;
+            if (term != ST_RUNNING && what == 0) sc->status = term;
+        }
+        if (lead) {
+            cudaGraphSetConditional(icond, what == 2 ? 1u : 0u);
+            if (what == 0) cudaGraphSetConditional(wcond, 0);
+        }
+        go = what;
+    }
+    __syncthreads();
+    const int what = go;
+    if (what == 0) return;
+    const float ta = bc[0], tw = bc[1], tb = bc[2];
+    auto unit = [&](int u, float(&dd)[4], float(&pp)[4], const float(&ss)[4], const float(&tt)[4],
+                    const float(&vx)[4]) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) dd[e] = fmaf(tw, ss[e], fmaf(ta, pp[e], dd[e]));
+        if (what == 2) {
+            double2 a = reinterpret_cast<double2 *>(X)[2 * u];
+            double2 b = reinterpret_cast<double2 *>(X)[2 * u + 1];
+            a.x += static_cast<double>(dd[0]);
+            a.y += static_cast<double>(dd[1]);
+            b.x += static_cast<double>(dd[2]);
+            b.y += static_cast<double>(dd[3]);
+            reinterpret_cast<double2 *>(X)[2 * u] = a;
+            reinterpret_cast<double2 *>(X)[2 * u + 1] = b;
+            reinterpret_cast<float4 *>(D32)[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+            return;
+        }
+        float r[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            r[e] = fmaf(-tw, tt[e], ss[e]);
+            pp[e] = fmaf(tb, fmaf(-tw, vx[e], pp[e]), r[e]);
+        }
+        stu(D32, u, dd);
+        stu(R, u, r);
+        stu(P, u, pp);
+    };
+#pragma unroll
+    for (int k = 0; k < kPre; ++k) {
+        const int u = u0 + k * stride;
+        if (u < nu4) unit(u, d[k], p[k], s[k], t[k], vv[k]);
+    }
+    for (int u = u0 + kPre * stride; u < nu4; u += stride) {
+        float dd[4], pp[4], ss[4], tt[4], vx[4];
+        ldu(dd, D32, u);
+        ldu(pp, P, u);
+        ldu(ss, S, u);
+        ldu(tt, Tv, u);
+        ldu(vx, V, u);
+        unit(u, dd, pp, ss, tt, vx);
+    }
+}
+
 // After the gated FP64 residual SpMV: replace the FP32 residual, recompute its dot partials,
 // test convergence on the FP64 true residual.
 __global__ void __launch_bounds__(512) k_ru_apply(DevScal *sc, const double *Rd, float *R32, const float *R0_32,
@@ -876,7 +1010,7 @@ hhp_status ensure_solver(hhp_mat *A, Solver **out, int maxit) {
         s->part_xr = dalloc<double>(2 * s->nblk, st);
         s->part_s = dalloc<double>(4 * s->nblk, st);  // records of 2, or 4 in the merged loop
         s->part_xr32 = dalloc<double>(2 * s->nblk, st);
-        s->part_s32 = dalloc<double>(2 * s->nblk, st);
+        s->part_s32 = dalloc<double>(4 * s->nblk, st);
         s->sc = dalloc<DevScal>(1, st);
         s->sc32 = dalloc<DevScal>(1, st);
         if (st == HHP_OK && cudaMallocHost(&s->h_sc, sizeof(DevScal)) != cudaSuccess) st = HHP_ERR_OOM;
@@ -900,7 +1034,8 @@ hhp_status ensure_solver(hhp_mat *A, Solver **out, int maxit) {
         if (s->g64) cudaGraphExecDestroy(s->g64);
         if (s->g64m) cudaGraphExecDestroy(s->g64m);
         if (s->gmix) cudaGraphExecDestroy(s->gmix);
-        s->g64 = s->g64m = s->gmix = nullptr;
+        if (s->gmixm) cudaGraphExecDestroy(s->gmixm);
+        s->g64 = s->g64m = s->gmix = s->gmixm = nullptr;
     }
     *out = s;
     return HHP_OK;
@@ -1047,6 +1182,39 @@ hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R,
                     st = HHP_ERR_CUDA;
                 continue;
             }
+        } else if (merged) {
+            // mixed form, merged: [SpMV + r0.v, K_S + r0.s, SpMV + t.s/t.t/r0.t, K_XRP_RU],
+            // IF(update) { FP64 residual, residual replacement, K_P }
+            st = launch_spmv32(A, s->s2, EP_DOT1, P, V, R0, stop);
+            if (st != HHP_OK) break;
+            if (launch_k(k_s<float, true>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, sc, S, R, V, R0, nu,
+                         parts_of(pl), part_s) != cudaSuccess) {
+                st = HHP_ERR_CUDA;
+                break;
+            }
+            st = launch_spmv32(A, s->s2, EP_DOT3, S, Tv, S, stop, R0);
+            if (st != HHP_OK) break;
+            cudaGraphConditionalHandle icond;
+            st = make_cond_if(s->s2, &icond);
+            if (st != HHP_OK) break;
+            if (launch_k(k_xrp_ru, dim3(s->nblk), dim3(s->nthr), 0, s->s2, s->sc32, s->X, s->D32, s->R32, s->P32,
+                         s->S32, s->T32, s->V32, nu4, parts_of(pl), part_s, s->nblk, s->hist, s->hist_cap, cond,
+                         icond, k == 0 ? 1 : 0, A->ctx->dev_err) != cudaSuccess) {
+                st = HHP_ERR_CUDA;
+                break;
+            }
+            st = begin_if_body(s, icond);
+            if (st != HHP_OK) break;
+            st = launch_spmv64(A, s->s3, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0);
+            if (st == HHP_OK &&
+                launch_k(k_ru_apply, dim3(s->nblk), dim3(s->nthr), 0, s->s3, s->sc32, s->Y, s->R32, s->R0_32, nu4,
+                         parts_of(A->plan64), s->part_xr32) != cudaSuccess)
+                st = HHP_ERR_CUDA;
+            // K_P's s.s operand (the half-step test) is unused here: the mixed form has no recursive
+            // stop tests, so the 4-wide K_S records need no 2-wide copy
+            if (st == HHP_OK) st = kp(s->s3, cond, 0);
+            st = end_if_body(s, st);
+            continue;
         }
         if (fp32)
             st = launch_spmv32(A, s->s2, EP_DOT1, reinterpret_cast<const float *>(P), reinterpret_cast<float *>(V),
@@ -1201,8 +1369,8 @@ hhp_status build_g64(Solver *s, bool merged) {
 
 // Mixed-form graph: FP64 residual, init, first stop test, WHILE{ unroll x [FP32 iteration,
 // update check, gated FP64 residual, gated residual replacement, stop test] }, fold d into x,
-// FP64 true residual, finish.
-hhp_status build_gmix(Solver *s) {
+// FP64 true residual, finish. The FP32 iteration is the classic or the merged one.
+hhp_status build_gmix(Solver *s, bool merged) {
     hhp_mat *A = s->A;
     cudaStream_t st = A->ctx->stream;
     HHP_TRY(ensure_plan(A, false));
@@ -1220,7 +1388,7 @@ hhp_status build_gmix(Solver *s) {
         HHP_CUDA(launch_k(k_mix_init, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc32, s->Y, s->R32, s->R0_32, s->D32,
                           s->P32, s->V32, nu4, parts_of(A->plan64), s->part_xr32, s->part_s32));
         rc = capture_loop<float>(s, st, s->sc32, s->D32, s->R32, s->R0_32, s->P32, s->V32, s->S32, s->T32,
-                                 s->part_xr32, s->part_s32, true, false);
+                                 s->part_xr32, s->part_s32, true, merged);
         if (rc != HHP_OK) break;
         HHP_CUDA(launch_k(k_mix_final, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc32, s->X, s->D32, nu4));
         rc = launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0);
@@ -1236,7 +1404,7 @@ hhp_status build_gmix(Solver *s) {
         return rc;
     }
     HHP_CUDA(e);
-    cudaError_t ie = cudaGraphInstantiate(&s->gmix, g, 0);
+    cudaError_t ie = cudaGraphInstantiate(merged ? &s->gmixm : &s->gmix, g, 0);
     cudaGraphDestroy(g);
     HHP_CUDA(ie);
     s->gmix_kernels_pro = 3;
@@ -1388,7 +1556,9 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
     if (!mixed) {
         HHP_TRY(fp64_passes(0));
     } else {
-        if (!s->gmix) HHP_TRY(build_gmix(s));
+        const bool merged32 = o->loop != HHP_LOOP_CLASSIC;
+        cudaGraphExec_t &gm = merged32 ? s->gmixm : s->gmix;
+        if (!gm) HHP_TRY(build_gmix(s, merged32));
         DevScal &h32 = *s->h_sc32;
         h32.rtol2 = o->rtol * o->rtol;
         const double delta = o->inner_rtol > 0.0 ? o->inner_rtol : 0.1;
@@ -1399,11 +1569,11 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
         for (int pass = 0; pass < 2; ++pass) {
             h32.restart = pass > 0 ? 1 : 0;
             const int upd0 = pass > 0 ? h32.updates : 0;
-            HHP_CUDA(cudaGraphLaunch(s->gmix, st));
+            HHP_CUDA(cudaGraphLaunch(gm, st));
             HHP_TRY(readback(s->h_sc32, s->sc32));
-            // 5 kernels per iteration, 3 more per FP64 update (the IF body)
-            ctx->kernel_launches += s->gmix_kernels_pro + s->gmix_kernels_epi + 5LL * s->unroll * h32.bodies +
-                                    3LL * (h32.updates - upd0);
+            // 4 (merged) or 5 kernels per iteration, 3 more per FP64 update (the IF body)
+            ctx->kernel_launches += s->gmix_kernels_pro + s->gmix_kernels_epi +
+                                    (merged32 ? 4LL : 5LL) * s->unroll * h32.bodies + 3LL * (h32.updates - upd0);
             // an inner breakdown or divergence after some progress restarts the FP32 recurrences
             // once from the last FP64 iterate (its true residual becomes the new shadow
             // residual); a second one hands the solve to FP64 below
@@ -1476,6 +1646,7 @@ void solver_release(Solver *s) {
     if (s->g64) cudaGraphExecDestroy(s->g64);
     if (s->g64m) cudaGraphExecDestroy(s->g64m);
     if (s->gmix) cudaGraphExecDestroy(s->gmix);
+    if (s->gmixm) cudaGraphExecDestroy(s->gmixm);
     double *d[] = {s->X, s->B, s->R, s->R0, s->P, s->V, s->S, s->T, s->Y, s->part_xr, s->part_s, s->part_xr32,
                    s->part_s32, s->hist};
     for (double *p : d) cudaFree(p);

@@ -378,10 +378,7 @@ cudaError_t launch_rud(EpKind ep, const PlanDev &p, const SellArgs<VT> &a, cudaS
     switch (ep) {
         case EP_DOT1: return launch_k(k_spmv<VT, R, U, EP_DOT1, D16>, grid, block, 0, s, a);
         case EP_DOT2: return launch_k(k_spmv<VT, R, U, EP_DOT2, D16>, grid, block, 0, s, a);
-        case EP_DOT3:
-            if constexpr (std::is_same<VT, double>::value)
-                return launch_k(k_spmv<VT, R, U, EP_DOT3, D16>, grid, block, 0, s, a);
-            return cudaErrorInvalidValue;
+        case EP_DOT3: return launch_k(k_spmv<VT, R, U, EP_DOT3, D16>, grid, block, 0, s, a);
         case EP_RESID: return launch_k(k_spmv<VT, R, U, EP_RESID, D16>, grid, block, 0, s, a);
         default:
             // y = A x needs no epilogue arithmetic: a separate instantiation keeps the FP64 pipe
@@ -645,7 +642,7 @@ hhp_status launch_spmv64(hhp_mat *A, cudaStream_t stream, EpKind ep, const doubl
 }
 
 hhp_status launch_spmv32(hhp_mat *A, cudaStream_t stream, EpKind ep, const float *x, float *y, const float *w1,
-                         const int *stop) {
+                         const int *stop, const float *w2) {
     if (!A->val32) {
         set_error("FP32 SpMV requested before the FP32 copy of the values was built");
         return HHP_ERR_STATE;
@@ -654,6 +651,7 @@ hhp_status launch_spmv32(hhp_mat *A, cudaStream_t stream, EpKind ep, const float
     const PlanDev &p = A->plan32;
     SellArgs<float> a = make_args<float>(A, p, A->val32, x, y, w1, 1.0, 0.0);
     a.stop = stop;
+    a.w2 = w2;
     HHP_CUDA(launch_ep<float>(ep, p, a, stream));
     A->ctx->kernel_launches += 1;
     return HHP_OK;

@@ -32,3 +32,31 @@ def test_mixed_reaches_fp64_tolerance(ctx, sysname):
     scale = np.max(np.abs(s.x_target))
     assert rm.err_vs_target <= 10 * max(r64.err_vs_target, 1e-12 * scale) + 1e-8 * scale
     assert np.max(np.abs(xm - x64)) <= 1e-6 * scale
+
+
+@pytest.mark.parametrize("sysname", ["c1", "cd3d_48"])
+def test_mixed_merged_and_classic_inner_loops(ctx, sysname):
+    """The FP32 inner loop in both schedules: merged (4 kernels per iteration, the update test and
+    beta from the t = A s dot products) and classic (5). Both reach the FP64 tolerance with
+    iteration counts close to each other; the launch count follows 4 (or 5) per iteration plus 3
+    per FP64 update."""
+    import math
+    s = synth.config("c1") if sysname == "c1" else synth.convdiff3d(48, 20.0, seed=3)
+    A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
+    res = {}
+    for loop, per_iter in (("merged", 4), ("classic", 5)):
+        bicgstab(ctx, A, s.b, s.x0, rtol=1e-10, maxit=5000, precision="mixed", loop=loop)  # builds the graph
+        n0 = ctx.kernel_launches
+        x, r = bicgstab(ctx, A, s.b, s.x0, s.x_target, rtol=1e-10, maxit=5000, precision="mixed", loop=loop)
+        n = ctx.kernel_launches - n0
+        assert r.status == 0 and r.rel_res_true <= 1e-10 and not r.fp64_fallback, (loop, r)
+        resid = s.b - orc.spmv(s.rowptr, s.col, s.val, x)
+        assert np.sqrt(orc.dot(resid, resid) / orc.dot(s.b, s.b)) <= 1.0000001e-10
+        # residual SpMV, init, first stop test; bodies of 2 iterations; 3 per update; fold, true
+        # residual, finish
+        assert n == 3 + per_iter * 2 * math.ceil(r.iters / 2) + 3 * r.outer_iters + 3, (loop, n, r.iters,
+                                                                                        r.outer_iters)
+        res[loop] = (x, r)
+    assert res["merged"][1].iters <= 1.1 * res["classic"][1].iters + 3
+    scale = np.max(np.abs(s.x_target))
+    assert np.max(np.abs(res["merged"][0] - res["classic"][0])) <= 1e-6 * scale
