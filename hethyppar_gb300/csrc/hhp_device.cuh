@@ -174,10 +174,10 @@ __device__ __forceinline__ void block_sum(double (&v)[NC], double *scratch) {
     for (int c = 0; c < NC; ++c) v[c] = r[c];
 }
 
-// One thread's running sums over records i = k, k + K, ... of part[i*NC + c] (i < n) followed
-// by extra[(i-n)*NC + c]; the first record is assigned, not added. ld.global.cg: the records were
-// written by an earlier kernel.
-template <int NC>
+// One thread's running sums over records i = k, k + K, ... of part[i*S + c] (i < n, c < NC)
+// followed by extra[(i-n)*S + c]: the first NC components of records S doubles wide. The first
+// record is assigned, not added. ld.global.cg: the records were written by an earlier kernel.
+template <int NC, int S = NC>
 __device__ __forceinline__ void thread_records(const double *__restrict__ part, int n, const double *__restrict__ extra,
                                                int n_extra, double *s, int k, int K) {
     const int tot = n + n_extra;
@@ -185,12 +185,12 @@ __device__ __forceinline__ void thread_records(const double *__restrict__ part, 
 #pragma unroll
     for (int c = 0; c < NC; ++c) s[c] = 0.0;
     if (i < tot) {
-        const double *src = i < n ? part + i * NC : extra + (i - n) * NC;
+        const double *src = i < n ? part + i * S : extra + (i - n) * S;
 #pragma unroll
         for (int c = 0; c < NC; ++c) s[c] = __ldcg(src + c);
     }
     for (i += K; i < tot; i += K) {
-        const double *src = i < n ? part + i * NC : extra + (i - n) * NC;
+        const double *src = i < n ? part + i * S : extra + (i - n) * S;
 #pragma unroll
         for (int c = 0; c < NC; ++c) s[c] += __ldcg(src + c);
     }
@@ -200,37 +200,37 @@ __device__ __forceinline__ void thread_records(const double *__restrict__ part, 
 // adds and no warp's adds are spent on empty lanes of a mostly idle block.
 __device__ __forceinline__ int reducing_warps() { return min(static_cast<int>((blockDim.x + 31) >> 5), 4); }
 
-// Sum of per-block partials part[i*NC + c] for i in [0, n), plus extra[j*NC + c] for j in
-// [0, n_extra), computed identically by every calling block and returned to every thread.
-// The first four warps take records t, t + 128, ... in order and group_allreduce combines them
-// (GB300's FP64 pipe, ~64 cycles per warp instruction per scheduler, is the scarcest unit).
-template <int NC>
+// Sum of the first NC components of per-block records part[i*S + c] for i in [0, n), plus
+// extra[j*S + c] for j in [0, n_extra), computed identically by every calling block and returned
+// to every thread. The first four warps take records t, t + 128, ... in order and group_allreduce
+// combines them (GB300's FP64 pipe, ~64 cycles per warp instruction per scheduler, is the scarcest
+// unit, so only the components a consumer uses are added).
+template <int NC, int S = NC>
 __device__ __forceinline__ void reduce_partials(const double *__restrict__ part, int n,
                                                 const double *__restrict__ extra, int n_extra,
                                                 double (&out)[NC], double *scratch /* kRedScratch */) {
     const int nwa = reducing_warps(), K = nwa * 32, t = threadIdx.x;
-    if (t < K) thread_records<NC>(part, n, extra, n_extra, out, t, K);
+    if (t < K) thread_records<NC, S>(part, n, extra, n_extra, out, t, K);
     group_allreduce<NC>(out, nwa, scratch);
 }
 
-// Two independent reductions (A = part_a + extra_a, B = part_b) in one pass: one memory round
-// trip and one group_allreduce over 2*NC quantities. Same order guarantees as reduce_partials.
-template <int NC>
-__device__ __forceinline__ void reduce_pair(const double *__restrict__ part_a, int na, const double *__restrict__ extra_a,
-                                            int nea, const double *__restrict__ part_b, int nb, double (&out_a)[NC],
-                                            double (&out_b)[NC], double *scratch /* kRedScratch */) {
+// Two independent reductions in one pass: out[0 .. NA) = the first NA components of records
+// part_a (+ extra_a), S_A wide; out[NA .. NA+NB) = the first NB components of records part_b, S_B
+// wide; the rest of out[NQ] is zero (NQ a power of two >= NA + NB). One memory round trip and one
+// group_allreduce. Same order guarantees as reduce_partials.
+template <int NA, int SA, int NB, int SB, int NQ>
+__device__ __forceinline__ void reduce_two(const double *__restrict__ part_a, int na, const double *__restrict__ extra_a,
+                                           int nea, const double *__restrict__ part_b, int nb, double (&out)[NQ],
+                                           double *scratch /* kRedScratch */) {
+    static_assert(NA + NB <= NQ, "NQ too small");
     const int nwa = reducing_warps(), K = nwa * 32, t = threadIdx.x;
-    double v[2 * NC];
-    if (t < K) {
-        thread_records<NC>(part_a, na, extra_a, nea, v, t, K);
-        thread_records<NC>(part_b, nb, nullptr, 0, v + NC, t, K);
-    }
-    group_allreduce<2 * NC>(v, nwa, scratch);
 #pragma unroll
-    for (int c = 0; c < NC; ++c) {
-        out_a[c] = v[c];
-        out_b[c] = v[NC + c];
+    for (int c = 0; c < NQ; ++c) out[c] = 0.0;
+    if (t < K) {
+        thread_records<NA, SA>(part_a, na, extra_a, nea, out, t, K);
+        thread_records<NB, SB>(part_b, nb, nullptr, 0, out + NA, t, K);
     }
+    group_allreduce<NQ>(out, nwa, scratch);
 }
 
 __device__ __forceinline__ bool finite_nonzero(double v) { return isfinite(v) && v != 0.0; }

@@ -156,8 +156,7 @@ __global__ void __launch_bounds__(512) k_init(DevScal *sc, const T *R, T *R0, T 
     if (threadIdx.x == 0) {
         part_xr[2 * blockIdx.x] = blockIdx.x == 0 ? rr : 0.0;
         part_xr[2 * blockIdx.x + 1] = blockIdx.x == 0 ? rr : 0.0;
-        part_s[2 * blockIdx.x] = 0.0;
-        part_s[2 * blockIdx.x + 1] = 0.0;
+        part_s[4 * blockIdx.x] = 0.0;  // K_S records are 4 wide (s.s, r0.s, -, -)
     }
     if (b0t0()) {
         if (!sc->restart) {
@@ -196,8 +195,11 @@ __device__ __forceinline__ int step_p(int status, int iter, int it0, int maxit, 
     return ST_RUNNING;
 }
 
-// Vector units per thread whose operands the vector kernels request before their reductions.
+// Vector units per thread whose operands the vector kernels request before their reductions
+// (kPreX for the merged loop's kernels, whose wider reductions and operand sets would spill at
+// 4 units under the 128-register limit of 512-thread blocks).
 constexpr int kPre = 4;
+constexpr int kPreX = 3;
 
 // Scalar work (divisions, tests) is done once per block by thread 0 and broadcast through shared
 // memory: on GB300 an FP64 division is a sequence of FP64 instructions on the slowest pipe, so
@@ -226,10 +228,10 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
             ldu(r[k], R, u);
         }
     }
-    double v[2], w[2];
-    reduce_pair<2>(part_xr, nparts, nullptr, 0, part_s, nparts, v, w, red);
+    double q[4];  // r.r0, r.r (2-wide records), s.s (4-wide K_S records)
+    reduce_two<2, 2, 1, 4, 4>(part_xr, nparts, nullptr, 0, part_s, nparts, q, red);
     if (threadIdx.x == 0) {
-        const double rho_new = v[0], rr = v[1], ss = w[0];
+        const double rho_new = q[0], rr = q[1], ss = q[2];
         const bool lead = blockIdx.x == 0;
         const int st = sc->status;
         int term = ST_RUNNING;
@@ -296,10 +298,11 @@ __global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const 
     __shared__ double bc[1];
     __shared__ int go;
     constexpr int E = Unit<T>::E;
+    constexpr int KP = M ? kPreX : kPre;  // three vectors' operands in the merged form
     const int stride = gridDim.x * blockDim.x, u0 = blockIdx.x * blockDim.x + threadIdx.x;
-    T r[kPre][E], vv[kPre][E], q[M ? kPre : 1][E];
+    T r[KP][E], vv[KP][E], q[M ? KP : 1][E];
 #pragma unroll
-    for (int k = 0; k < kPre; ++k) {
+    for (int k = 0; k < KP; ++k) {
         const int u = u0 + k * stride;
         if (u < nu) {
             ldu(r[k], R, u);
@@ -307,8 +310,8 @@ __global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const 
             if constexpr (M) ldu(q[k], R0, u);
         }
     }
-    double v[2];
-    reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
+    double v[1];  // r0.v: the first component of the SpMV's 2-wide records
+    reduce_partials<1, 2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
     if (threadIdx.x == 0) {
         int ok = sc->status == ST_RUNNING;
         if (ok) {
@@ -333,7 +336,7 @@ __global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const 
     const T ta = static_cast<T>(bc[0]);
     double acc[M ? 2 : 1] = {};
 #pragma unroll
-    for (int k = 0; k < kPre; ++k) {
+    for (int k = 0; k < KP; ++k) {
         const int u = u0 + k * stride;
         if (u < nu) {
             T sv[E];
@@ -344,7 +347,7 @@ __global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const 
             stu(S, u, sv);
         }
     }
-    for (int u = u0 + kPre * stride; u < nu; u += stride) {
+    for (int u = u0 + KP * stride; u < nu; u += stride) {
         T rx[E], vx[E], sv[E];
         ldu(rx, R, u);
         ldu(vx, V, u);
@@ -360,15 +363,9 @@ __global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const 
     }
     block_sum<M ? 2 : 1>(acc, red);
     if (threadIdx.x == 0) {
-        if constexpr (M) {
-            part_s[4 * blockIdx.x] = acc[0];
-            part_s[4 * blockIdx.x + 1] = acc[M ? 1 : 0];
-            part_s[4 * blockIdx.x + 2] = 0.0;
-            part_s[4 * blockIdx.x + 3] = 0.0;
-        } else {
-            part_s[2 * blockIdx.x] = acc[0];
-            part_s[2 * blockIdx.x + 1] = 0.0;
-        }
+        // records 4 wide: s.s, then r0.s in the merged loop; consumers read only those
+        part_s[4 * blockIdx.x] = acc[0];
+        if constexpr (M) part_s[4 * blockIdx.x + 1] = acc[M ? 1 : 0];
     }
 }
 
@@ -397,19 +394,19 @@ __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P,
             ldu(t[k], Tv, u);
         }
     }
-    double v[2], w[2];
-    reduce_pair<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, part_s, nparts, v, w, red);
+    double q[4];  // t.s, t.t (2-wide SpMV records), s.s (4-wide K_S records)
+    reduce_two<2, 2, 1, 4, 4>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, part_s, nparts, q, red);
     if (threadIdx.x == 0) {
         int ok = sc->status == ST_RUNNING;
         int half = 0;
         if (ok) {
             const double thr2 = sc->thr2_rec;
-            half = thr2 >= 0.0 && w[0] <= thr2;
+            half = thr2 >= 0.0 && q[2] <= thr2;
             bc[0] = sc->alpha;
             bc[1] = 0.0;
             if (!half) {
-                const double omega = v[0] / v[1];
-                if (!finite_nonzero(v[1]) || !isfinite(omega)) {
+                const double omega = q[0] / q[1];
+                if (!finite_nonzero(q[1]) || !isfinite(omega)) {
                     if (blockIdx.x == 0) sc->status = ST_BREAKDOWN;
                     ok = 0;
                 } else {
@@ -491,9 +488,9 @@ __global__ void __launch_bounds__(512) k_xrp(DevScal *sc, T *X, T *R, T *P, cons
     __shared__ int go;  // 0: nothing to do, 1: full step and p, 2: half step, 3: full step, last
     constexpr int E = Unit<T>::E;
     const int stride = gridDim.x * blockDim.x, u0 = blockIdx.x * blockDim.x + threadIdx.x;
-    T x[kPre][E], p[kPre][E], s[kPre][E], t[kPre][E], vv[kPre][E];
+    T x[kPreX][E], p[kPreX][E], s[kPreX][E], t[kPreX][E], vv[kPreX][E];
 #pragma unroll
-    for (int k = 0; k < kPre; ++k) {
+    for (int k = 0; k < kPreX; ++k) {
         const int u = u0 + k * stride;
         if (u < nu) {
             ldu(x[k], X, u);
@@ -503,14 +500,14 @@ __global__ void __launch_bounds__(512) k_xrp(DevScal *sc, T *X, T *R, T *P, cons
             ldu(vv[k], V, u);
         }
     }
-    double v[4], w[4];
-    reduce_pair<4>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, part_s, nparts, v, w, red);
+    double q[8];  // t.s, t.t, r0.t (4-wide SpMV records), s.s, r0.s (4-wide K_S records)
+    reduce_two<3, 4, 2, 4, 8>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, part_s, nparts, q, red);
     if (threadIdx.x == 0) {
         const bool lead = blockIdx.x == 0;
         int mode = 0, term = *reinterpret_cast<volatile const int *>(&sc->status);
         if (lead && first_in_body) sc->bodies += 1;  // bodies executed (kernel-launch accounting)
         if (term == ST_RUNNING) {
-            const double ts = v[0], tt = v[1], r0t = v[2], ss = w[0], r0s = w[1];
+            const double ts = q[0], tt = q[1], r0t = q[2], ss = q[3], r0s = q[4];
             const double thr2 = sc->thr2_rec, alpha = sc->alpha;
             const int iter = sc->iter;  // this iteration (K_S counted it)
             double rr = ss;
@@ -595,11 +592,11 @@ __global__ void __launch_bounds__(512) k_xrp(DevScal *sc, T *X, T *R, T *P, cons
         stu(R, u, r);
     };
 #pragma unroll
-    for (int k = 0; k < kPre; ++k) {
+    for (int k = 0; k < kPreX; ++k) {
         const int u = u0 + k * stride;
         if (u < nu) unit(u, x[k], p[k], s[k], t[k], vv[k]);
     }
-    for (int u = u0 + kPre * stride; u < nu; u += stride) {
+    for (int u = u0 + kPreX * stride; u < nu; u += stride) {
         T xx[E], pp[E], ss[E], tt[E], vx[E];
         ldu(xx, X, u);
         ldu(pp, P, u);
@@ -657,8 +654,7 @@ __global__ void __launch_bounds__(512) k_mix_init(DevScal *sc, const double *Rd,
     if (threadIdx.x == 0) {
         part_xr32[2 * blockIdx.x] = acc[0];
         part_xr32[2 * blockIdx.x + 1] = acc[0];
-        part_s32[2 * blockIdx.x] = 0.0;
-        part_s32[2 * blockIdx.x + 1] = 0.0;
+        part_s32[4 * blockIdx.x] = 0.0;  // K_S records are 4 wide
     }
     if (b0t0()) {
         if (!sc->restart) {  // a restart after a breakdown keeps the counts and the threshold
@@ -702,11 +698,11 @@ __global__ void __launch_bounds__(512) k_p_ru(DevScal *sc, double *X, float *D32
     __shared__ double red[kRedScratch];
     __shared__ float bc[2];
     __shared__ int go;  // 0: nothing, 1: p update, 2: fold d into x
-    double v[2], w[2];
-    reduce_pair<2>(part_xr, nparts, nullptr, 0, part_s, nparts, v, w, red);
+    double q[4];  // r.r0, r.r (2-wide records), s.s (4-wide K_S records)
+    reduce_two<2, 2, 1, 4, 4>(part_xr, nparts, nullptr, 0, part_s, nparts, q, red);
     if (threadIdx.x == 0) {
         const bool lead = blockIdx.x == 0;
-        const double rho_new = v[0], rr = v[1];
+        const double rho_new = q[0], rr = q[1];
         const int st = sc->status;
         int what = 0;
         if (lead && first_in_body) sc->bodies += 1;
@@ -726,7 +722,7 @@ __global__ void __launch_bounds__(512) k_p_ru(DevScal *sc, double *X, float *D32
                 const int it0 = sc->iter_start;
                 if (lead && it > it0 && it - 1 < hist_cap) hist[it - 1] = rr;
                 double beta = 0.0;
-                const int term = step_p(st, it, it0, sc->maxit, sc->thr2_rec, rho_new, rr, w[0], sc->rho_prev,
+                const int term = step_p(st, it, it0, sc->maxit, sc->thr2_rec, rho_new, rr, q[2], sc->rho_prev,
                                         sc->alpha, sc->omega, *reinterpret_cast<volatile const int *>(dev_err) != DEV_OK,
                                         beta);
                 if (term != ST_RUNNING) {
@@ -797,9 +793,9 @@ __global__ void __launch_bounds__(512) k_xrp_ru(DevScal *sc, double *X, float *D
     __shared__ float bc[3];
     __shared__ int go;  // 0: nothing, 1: d, r, p updates, 2: fold d + alpha p + omega s into x
     const int stride = gridDim.x * blockDim.x, u0 = blockIdx.x * blockDim.x + threadIdx.x;
-    float d[kPre][4], p[kPre][4], s[kPre][4], t[kPre][4], vv[kPre][4];
+    float d[kPreX][4], p[kPreX][4], s[kPreX][4], t[kPreX][4], vv[kPreX][4];
 #pragma unroll
-    for (int k = 0; k < kPre; ++k) {
+    for (int k = 0; k < kPreX; ++k) {
         const int u = u0 + k * stride;
         if (u < nu4) {
             ldu(d[k], D32, u);
@@ -809,14 +805,14 @@ __global__ void __launch_bounds__(512) k_xrp_ru(DevScal *sc, double *X, float *D
             ldu(vv[k], V, u);
         }
     }
-    double v[4], w[4];
-    reduce_pair<4>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, part_s, nparts, v, w, red);
+    double q[8];  // t.s, t.t, r0.t (4-wide SpMV records), s.s, r0.s (4-wide K_S records)
+    reduce_two<3, 4, 2, 4, 8>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, part_s, nparts, q, red);
     if (threadIdx.x == 0) {
         const bool lead = blockIdx.x == 0;
         int what = 0, term = *reinterpret_cast<volatile const int *>(&sc->status);
         if (lead && first_in_body) sc->bodies += 1;
         if (term == ST_RUNNING) {
-            const double ts = v[0], tt = v[1], r0t = v[2], ss = w[0], r0s = w[1];
+            const double ts = q[0], tt = q[1], r0t = q[2], ss = q[3], r0s = q[4];
             const double omega = ts / tt, alpha = sc->alpha;
             const int it = sc->iter;
             if (*reinterpret_cast<volatile const int *>(dev_err) != DEV_OK) {
@@ -899,11 +895,11 @@ __global__ void __launch_bounds__(512) k_xrp_ru(DevScal *sc, double *X, float *D
         stu(P, u, pp);
     };
 #pragma unroll
-    for (int k = 0; k < kPre; ++k) {
+    for (int k = 0; k < kPreX; ++k) {
         const int u = u0 + k * stride;
         if (u < nu4) unit(u, d[k], p[k], s[k], t[k], vv[k]);
     }
-    for (int u = u0 + kPre * stride; u < nu4; u += stride) {
+    for (int u = u0 + kPreX * stride; u < nu4; u += stride) {
         float dd[4], pp[4], ss[4], tt[4], vx[4];
         ldu(dd, D32, u);
         ldu(pp, P, u);
@@ -1210,8 +1206,6 @@ hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R,
                 launch_k(k_ru_apply, dim3(s->nblk), dim3(s->nthr), 0, s->s3, s->sc32, s->Y, s->R32, s->R0_32, nu4,
                          parts_of(A->plan64), s->part_xr32) != cudaSuccess)
                 st = HHP_ERR_CUDA;
-            // K_P's s.s operand (the half-step test) is unused here: the mixed form has no recursive
-            // stop tests, so the 4-wide K_S records need no 2-wide copy
             if (st == HHP_OK) st = kp(s->s3, cond, 0);
             st = end_if_body(s, st);
             continue;
