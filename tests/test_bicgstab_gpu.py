@@ -224,3 +224,38 @@ def test_rcm_reordered_solve_matches_original(ctx):
     x_back = np.empty(m)
     x_back[qp] = xr
     assert np.max(np.abs(x_back - x0)) <= 1e-6 * np.max(np.abs(x0))
+
+
+def test_merged_and_classic_loops_on_long_rows(ctx):
+    """Power-law rows (some cut into chunks combined by the last warp to finish): the long rows'
+    epilogue contributions feed the dot products of both schedules, FP64 and mixed."""
+    p = synth.powerlaw(100_000, max_len=20_000, n_dense=4, dense_lo=5_000, dense_hi=20_000, seed=21)
+    m = p.rowptr.size - 1
+    rows = np.repeat(np.arange(m), np.diff(p.rowptr))
+    off = rows != p.col
+    # each row's off-diagonal magnitudes sum to about 1 and the diagonal is 2: eigenvalues within
+    # [1, 3], so the solve converges in a few iterations however long the row
+    ln = np.maximum(np.bincount(rows[off], minlength=m), 1)
+    val = p.val.copy()
+    val[off] /= ln[rows[off]]
+    val[~off] = 2.0
+    xt = np.random.default_rng(3).standard_normal(m)
+    b = orc.spmv(p.rowptr, p.col, val, xt)
+    x0 = np.zeros(m)
+    k_ref, _, _ = orc.iters_to_tol(p.rowptr, p.col, val, b, x0, 1e-10, 500)
+    assert k_ref > 0
+    A = Matrix.from_csr(ctx, p.rowptr, p.col, val)
+    xs = {}
+    for loop in ("merged", "classic"):
+        for prec in ("fp64", "mixed"):
+            x, r = bicgstab(ctx, A, b, x0, rtol=1e-10, maxit=500, loop=loop, precision=prec)
+            assert r.status == 0 and r.rel_res_true <= 1e-10, (loop, prec, r)
+            res = b - orc.spmv(p.rowptr, p.col, val, x)
+            assert math.sqrt(orc.dot(res, res) / orc.dot(b, b)) <= 1.0000001e-10
+            if prec == "fp64":
+                assert _within_5pct(r.iters, k_ref), (loop, r.iters, k_ref)
+            xs[loop, prec] = x
+    scale = np.max(np.abs(xs["classic", "fp64"]))
+    for key, x in xs.items():
+        assert np.max(np.abs(x - xs["classic", "fp64"])) <= 1e-6 * scale, key
+    A.close()
