@@ -91,6 +91,11 @@ SIGNATURES = [
     ("hhp_free", None, [_P]),
     ("hhp_csr_file_write", _I, [_S, _I, _I, _I, _P, _P, _P]),
     ("hhp_reorder_rcm", _I, [_I, _P, _P, _P]),
+    ("hhp_dot_dev", _I, [_P, _I, _P, _P, _P]),
+    ("hhp_dot", _I, [_P, _I, _P, _P, _P]),
+    ("hhp_axpy_dev", _I, [_P, _I, ctypes.c_double, _P, _P]),
+    ("hhp_scal_dev", _I, [_P, _I, ctypes.c_double, _P]),
+    ("hhp_copy_dev", _I, [_P, _I, _P, _P]),
     ("hhp_plan_stats", _I, [_I, _I, _P, _I, _I, _PI, _PI, _PI, _PI, _PD]),
     ("hhp_plan_dump", _I, [_I, _I, _P, _I, _I, _I, _P, _P, _PI, _PI]),
     ("hhp_dp_vecop_P", None, [_P, _P, _P, _P, _P, _I, _P]),

@@ -64,6 +64,30 @@ class Context:
     def alive(self) -> bool:
         return bool(self._h)
 
+    # BLAS-1 on CUDA float64 tensors (hhp_dot / hhp_dot_dev / hhp_axpy_dev / hhp_scal_dev /
+    # hhp_copy_dev), on the context's stream
+    def dot(self, x, y, out=None):
+        """sum x*y: a Python float, or written into the 1-element CUDA tensor `out` (no sync)."""
+        n = int(x.numel())
+        if out is not None:
+            check(lib().hhp_dot_dev(self._h, n, _ptr(x), _ptr(y), _ptr(out)), "hhp_dot_dev")
+            return out
+        r = ctypes.c_double()
+        check(lib().hhp_dot(self._h, n, _ptr(x), _ptr(y), ctypes.byref(r)), "hhp_dot")
+        return r.value
+
+    def axpy(self, alpha: float, x, y):
+        check(lib().hhp_axpy_dev(self._h, int(x.numel()), float(alpha), _ptr(x), _ptr(y)), "hhp_axpy_dev")
+        return y
+
+    def scal(self, alpha: float, x):
+        check(lib().hhp_scal_dev(self._h, int(x.numel()), float(alpha), _ptr(x)), "hhp_scal_dev")
+        return x
+
+    def copy(self, src, dst):
+        check(lib().hhp_copy_dev(self._h, int(src.numel()), _ptr(src), _ptr(dst)), "hhp_copy_dev")
+        return dst
+
     def close(self):
         if self._h:
             for m in list(self._mats):

@@ -189,6 +189,7 @@ hhp_status hhp_ctx_create(int device, hhp_ctx **out) {
 void hhp_ctx_destroy(hhp_ctx *c) {
     if (!c) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
+    release_blas1(c);
     if (c->dev_err) cudaFree(c->dev_err);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);

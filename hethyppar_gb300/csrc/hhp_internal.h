@@ -88,6 +88,8 @@ struct hhp_ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int *dev_err = nullptr;           // device error word (hhp::DEV_*), zeroed
     long long kernel_launches = 0;
+    double *dot_part = nullptr;       // BLAS-1 dot: block partials (allocated on first use)
+    unsigned *dot_count = nullptr;    // BLAS-1 dot: blocks done (zero between launches)
 };
 
 struct hhp_mat {
@@ -138,6 +140,9 @@ hhp_status launch_spmv32(hhp_mat *A, cudaStream_t stream, EpKind ep, const float
                          const int *stop = nullptr, const float *w2 = nullptr);
 // Number of partial records (ctas) and long-row records of the last-used plan, for the reducers.
 inline int plan_ctas(const hhp_mat *A, bool fp32) { return fp32 ? A->plan32.ctas : A->plan64.ctas; }
+
+// ---- BLAS-1 (hhp_blas1.cu) -----------------------------------------------------------------------
+void release_blas1(hhp_ctx *ctx);
 
 // ---- Krylov solver (hhp_krylov.cu) ---------------------------------------------------------------
 // b, x, xt are device pointers when host == false, host pointers when host == true.

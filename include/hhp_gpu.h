@@ -181,6 +181,19 @@ void hhp_free(void *p);
 hhp_status hhp_csr_file_write(const char *path, int m, int n, int nnz, const int *rowptr, const int *col,
                               const double *val);
 
+/* ---- BLAS-1 on device vectors: replace device_vector_dot / _scale / _axpy / _GPUtoGPU
+ *      (src/util/hhp_cuda.c:163-202, cuBLAS Ddot/Dscal/Daxpy and a D2D copy) and the
+ *      device-pointer-mode cublasDdot of the dp loop (src/entry/bicgstab_gpu_dp.c:163-190) ------ */
+/* sum_i x[i] y[i] into device memory, asynchronously on the context's stream (cublasDdot with
+ * CUBLAS_POINTER_MODE_DEVICE). Deterministic: the same inputs give the same bits on every call. */
+hhp_status hhp_dot_dev(hhp_ctx *ctx, int n, const double *x_dev, const double *y_dev, double *result_dev);
+/* The same, result to host memory; synchronises the stream (cublasDdot with a host pointer). */
+hhp_status hhp_dot(hhp_ctx *ctx, int n, const double *x_dev, const double *y_dev, double *result);
+/* y += alpha x (cublasDaxpy), x *= alpha (cublasDscal), dst = src (device_vector_GPUtoGPU). */
+hhp_status hhp_axpy_dev(hhp_ctx *ctx, int n, double alpha, const double *x_dev, double *y_dev);
+hhp_status hhp_scal_dev(hhp_ctx *ctx, int n, double alpha, double *x_dev);
+hhp_status hhp_copy_dev(hhp_ctx *ctx, int n, const double *src_dev, double *dst_dev);
+
 /* ---- locality reordering ------------------------------------------------------------------ */
 /* Reverse Cuthill-McKee order of the symmetrised pattern A + A^T of a square CSR (host only, no
  * device needed): perm[m] in csr_permute's convention (src/util/hhp_dp_helpers.c:18-37), ready for
