@@ -19,6 +19,8 @@ OBJ_DIR = os.path.join(ROOT, "_build", "obj-" + MACHINE)
 LIB = os.path.join(PKG, "libhhp_gpu.so")
 CLI_SRC = os.path.join(PKG, "cli", "hhp_bicgstab.c")
 CLI_BIN = os.path.join(PKG, "bin", "hhp-bicgstab")
+SPMV_CLI_SRC = os.path.join(PKG, "cli", "hhp_spmv.c")
+SPMV_CLI_BIN = os.path.join(PKG, "bin", "hhp-spmv")
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 REFERENCE_DIR = "/root/reference"
 
@@ -98,6 +100,17 @@ def build_cli() -> str:
         _run([cc, "-O2", "-std=gnu11", "-Wall", "-I" + INCLUDE, CLI_SRC, "-o", CLI_BIN, "-L" + PKG, "-lhhp_gpu",
               "-Wl,-rpath,$ORIGIN/..", "-lm"])
         _stamp(CLI_BIN)
+    if _stale(SPMV_CLI_BIN, [SPMV_CLI_SRC, LIB, os.path.join(INCLUDE, "hhp_gpu.h")]):
+        cc = shutil.which("gcc") or "cc"
+        cuda = _cuda_home()
+        libdir = next((d for d in (os.path.join(cuda, "lib64"), os.path.join(cuda, "lib"),
+                                   os.path.join(cuda, "targets", "sbsa-linux", "lib"),
+                                   os.path.join(cuda, "targets", "x86_64-linux", "lib")) if os.path.isdir(d)),
+                      os.path.join(cuda, "lib64"))
+        _run([cc, "-O2", "-std=gnu11", "-Wall", "-I" + INCLUDE, "-I" + os.path.join(cuda, "include"), SPMV_CLI_SRC,
+              "-o", SPMV_CLI_BIN, "-L" + PKG, "-lhhp_gpu", "-L" + libdir, "-lcudart", "-Wl,-rpath,$ORIGIN/..",
+              "-Wl,-rpath," + libdir, "-lm"])
+        _stamp(SPMV_CLI_BIN)
     return CLI_BIN
 
 

@@ -87,6 +87,30 @@ def test_cli_rcm_reorder():
         assert r.returncode != 0 and "exclusive" in r.stdout
 
 
+def test_spmv_cli_known_answer():
+    """hhp-spmv, the spmv-gpu drop-in: A X_mul = [1..16] (the reference's data/sample X_mul), the
+    same stdout keys, and Y bit-identical to the oracle's fused row sums."""
+    from oracle import oracle as orc
+    g = load_golden("sample16")
+    exe = os.path.join(ROOT, "hethyppar_gb300", "bin", "hhp-spmv")
+    with tempfile.TemporaryDirectory() as td:
+        p = _files(td, g)
+        xm = os.path.join(td, "X_mul.txt")
+        np.savetxt(xm, g["vec_X_mul"], fmt="%.17g")
+        out = os.path.join(td, "Y.txt")
+        r = subprocess.run([exe, "-m", p["A"], "-x", xm, "-o", out, "-n", "50", "--out-format", "exact"],
+                           stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+        assert r.returncode == 0, r.stderr
+        kv = dict(re.findall(r"^(\w+)\s*:\s*(\S+)", r.stdout, re.M))
+        for key in ("n_iters", "spmv", "spmv_per_iter", "file_read", "max_abs_err_vs_1ton", "everything_total"):
+            assert key in kv, key
+        assert int(kv["n_iters"]) == 50 and float(kv["max_abs_err_vs_1ton"]) < 1e-10
+        y = np.loadtxt(out)
+        assert np.array_equal(y, orc.spmv(g["rowptr"], g["col"], g["val"], g["vec_X_mul"], fma=True))
+        r = subprocess.run([exe, "-m", p["A"], "-x", xm], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+        assert r.returncode != 0 and "must all be specified" in r.stderr
+
+
 def test_cli_binary_csr_rerun_matches_text_run():
     g = load_golden("sample320")
     with tempfile.TemporaryDirectory() as td:
