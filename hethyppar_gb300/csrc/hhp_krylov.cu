@@ -61,7 +61,9 @@ struct Solver {
     // FP32 inner vectors (mixed form)
     float *D32 = nullptr, *R32 = nullptr, *R0_32 = nullptr, *P32 = nullptr, *V32 = nullptr, *S32 = nullptr,
           *T32 = nullptr;
-    double *part_xr = nullptr, *part_s = nullptr;      // nblk*2 each (FP64 loop)
+    double *part_xr = nullptr, *part_s = nullptr;      // nblk*2 and nblk*4 (FP64 loop)
+    double *part_b = nullptr;                          // nblk: ||b||^2 partials of k_x0check
+    int *x0_nz = nullptr;                              // k_x0check: 1 if x0 has a nonzero
     double *part_xr32 = nullptr, *part_s32 = nullptr;  // nblk*2 each (FP32 inner loop)
     DevScal *sc = nullptr, *sc32 = nullptr;            // device
     DevScal *h_sc = nullptr, *h_sc32 = nullptr;        // pinned host mirrors
@@ -134,19 +136,51 @@ struct SpmvParts {
 };
 
 // ---------------------------------------------------------------------------------------------
-// Initialisation: after the residual SpMV (R = B - A X; partials ||R||^2, ||B||^2).
+// Before the residual SpMV: is x0 all zero (the usual start), and ||b||^2 in per-block partials.
+// With x0 = 0 the residual is b itself, so the SpMV (gated on *nz) is skipped and the
+// initialisation takes r = b with ||r||^2 = ||b||^2 from these partials.
+__global__ void __launch_bounds__(512) k_x0check(const double *__restrict__ X, const double *__restrict__ B, int nu2,
+                                                 int *nz, double *part_b) {
+    __shared__ double red[kRedScratch];
+    bool any = false;
+    double acc[1] = {0.0};
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu2; u += gridDim.x * blockDim.x) {
+        const double2 x = reinterpret_cast<const double2 *>(X)[u];
+        const double2 b = reinterpret_cast<const double2 *>(B)[u];
+        any = any || x.x != 0.0 || x.y != 0.0;  // NaN counts as nonzero; -0 as zero (b - A(-0) = b)
+        acc[0] = fma(b.y, b.y, fma(b.x, b.x, acc[0]));
+    }
+    any = __syncthreads_or(any);
+    block_sum<1>(acc, red);
+    if (threadIdx.x == 0) {
+        part_b[blockIdx.x] = acc[0];
+        if (any) atomicOr(nz, 1);
+    }
+}
+
+// Initialisation: after the residual SpMV (R = B - A X; partials ||R||^2, ||B||^2), or with x0 = 0
+// (*nz == 0: the SpMV was skipped) R = B and ||R||^2 = ||B||^2 from k_x0check's partials.
 // R0 = R, P = V = 0, scalars rho = alpha = omega = 1 (bicgstab_cpu.c:176-188).
 template <typename T>
-__global__ void __launch_bounds__(512) k_init(DevScal *sc, const T *R, T *R0, T *P, T *V, int nu, SpmvParts sp,
-                                              double *part_xr, double *part_s) {
+__global__ void __launch_bounds__(512) k_init(DevScal *sc, T *R, const T *B, T *R0, T *P, T *V, int nu, SpmvParts sp,
+                                              const int *nz, const double *part_b, int nparts, double *part_xr,
+                                              double *part_s) {
     __shared__ double red[kRedScratch];
+    const bool zero = *reinterpret_cast<volatile const int *>(nz) == 0;  // the same in every block
     double v[2];
-    reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
+    if (zero) {
+        double q[1];
+        reduce_partials<1>(part_b, nparts, nullptr, 0, q, red);
+        v[0] = v[1] = q[0];
+    } else {
+        reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
+    }
     const double rr = v[0], bb = v[1];
     constexpr int E = Unit<T>::E;
     for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += gridDim.x * blockDim.x) {
         T r[E], z[E];
-        ldu(r, R, u);
+        ldu(r, zero ? B : R, u);
+        if (zero) stu(R, u, r);
 #pragma unroll
         for (int e = 0; e < E; ++e) z[e] = T(0);
         stu(R0, u, r);
@@ -629,12 +663,22 @@ __global__ void k_finish(DevScal *sc, SpmvParts sp) {
 // decided on the FP64 true residual only.
 
 // After the FP64 residual SpMV (Rd = B - A X; partials ||Rd||^2, ||B||^2): start the FP32 loop.
-__global__ void __launch_bounds__(512) k_mix_init(DevScal *sc, const double *Rd, float *R32, float *R0_32,
-                                                  float *D32, float *P32, float *V32, int nu4, SpmvParts sp,
+__global__ void __launch_bounds__(512) k_mix_init(DevScal *sc, const double *Yd, const double *B, float *R32,
+                                                  float *R0_32, float *D32, float *P32, float *V32, int nu4,
+                                                  SpmvParts sp, const int *nz, const double *part_b, int nparts,
                                                   double *part_xr32, double *part_s32) {
     __shared__ double red[kRedScratch];
+    // x0 = 0 (*nz == 0): the residual SpMV was skipped and b is the residual (see k_x0check)
+    const bool zero = *reinterpret_cast<volatile const int *>(nz) == 0;
+    const double *Rd = zero ? B : Yd;
     double v[2];
-    reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
+    if (zero) {
+        double q[1];
+        reduce_partials<1>(part_b, nparts, nullptr, 0, q, red);
+        v[0] = v[1] = q[0];
+    } else {
+        reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
+    }
     const double rd2 = v[0], bb = v[1];
     double acc[1] = {0.0};
     const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -1004,7 +1048,9 @@ hhp_status ensure_solver(hhp_mat *A, Solver **out, int maxit) {
         s->T = dalloc<double>(np, st);
         s->Y = dalloc<double>(np, st);
         s->part_xr = dalloc<double>(2 * s->nblk, st);
-        s->part_s = dalloc<double>(4 * s->nblk, st);  // records of 2, or 4 in the merged loop
+        s->part_s = dalloc<double>(4 * s->nblk, st);  // K_S records are 4 wide
+        s->part_b = dalloc<double>(s->nblk, st);
+        s->x0_nz = dalloc<int>(1, st);
         s->part_xr32 = dalloc<double>(2 * s->nblk, st);
         s->part_s32 = dalloc<double>(4 * s->nblk, st);
         s->sc = dalloc<DevScal>(1, st);
@@ -1263,6 +1309,14 @@ hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R,
     return end_loop_body(s, st);
 }
 
+// Zeroes the x0 flag and runs k_x0check on `st` (captured into the solve graphs).
+hhp_status launch_x0check(Solver *s, cudaStream_t st) {
+    HHP_CUDA(cudaMemsetAsync(s->x0_nz, 0, sizeof(int), st));
+    HHP_CUDA(launch_k(k_x0check, dim3(s->nblk), dim3(s->nthr), 0, st, s->X, s->B, s->n_pad / 2, s->x0_nz,
+                      s->part_b));
+    return HHP_OK;
+}
+
 // The FP64 loop launched kernel by kernel (no graph), for profilers that cannot see inside
 // conditional graph nodes: same kernels and order; the host reads the status every `unroll`
 // iterations. Selected with HHP_SOLVE_GRAPH=0.
@@ -1272,10 +1326,11 @@ hhp_status run_direct64(Solver *s, bool merged) {
     const int nu = s->n_pad / 2;
     const int *stop = &s->sc->status;
     HHP_CUDA(cudaMemcpyAsync(s->sc, s->h_sc, kCtlBytes, cudaMemcpyHostToDevice, st));
-    HHP_TRY(launch_spmv64(A, st, EP_RESID, s->X, s->R, s->B, 1.0, 0.0));
-    HHP_CUDA(launch_k(k_init<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->R, s->R0, s->P, s->V, nu,
-                      parts_of(A->plan64), s->part_xr, s->part_s));
-    A->ctx->kernel_launches += 1;
+    HHP_TRY(launch_x0check(s, st));
+    HHP_TRY(launch_spmv64(A, st, EP_RESID, s->X, s->R, s->B, 1.0, 0.0, s->x0_nz));
+    HHP_CUDA(launch_k(k_init<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->R, s->B, s->R0, s->P, s->V, nu,
+                      parts_of(A->plan64), s->x0_nz, s->part_b, s->nblk, s->part_xr, s->part_s));
+    A->ctx->kernel_launches += 2;
     const PlanDev &pl = A->plan64;
     auto kp = [&](int first) -> hhp_status {
         HHP_CUDA(launch_k(k_p<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->P, s->V, s->R, nu, s->part_xr,
@@ -1318,8 +1373,8 @@ hhp_status run_direct64(Solver *s, bool merged) {
     return HHP_OK;
 }
 
-// FP64 solve graph (classic or merged loop): ctl copy, residual SpMV, init, WHILE{loop},
-// true-residual SpMV, finish.
+// FP64 solve graph (classic or merged loop): ctl copy, x0 check, residual SpMV (skipped for
+// x0 = 0), init, WHILE{loop}, true-residual SpMV, finish.
 hhp_status build_g64(Solver *s, bool merged) {
     hhp_mat *A = s->A;
     cudaStream_t st = A->ctx->stream;
@@ -1332,10 +1387,12 @@ hhp_status build_g64(Solver *s, bool merged) {
             rc = HHP_ERR_CUDA;
             break;
         }
-        rc = launch_spmv64(A, st, EP_RESID, s->X, s->R, s->B, 1.0, 0.0);
+        rc = launch_x0check(s, st);
         if (rc != HHP_OK) break;
-        HHP_CUDA(launch_k(k_init<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->R, s->R0, s->P, s->V, nu,
-                          parts_of(A->plan64), s->part_xr, s->part_s));
+        rc = launch_spmv64(A, st, EP_RESID, s->X, s->R, s->B, 1.0, 0.0, s->x0_nz);
+        if (rc != HHP_OK) break;
+        HHP_CUDA(launch_k(k_init<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->R, s->B, s->R0, s->P, s->V,
+                          nu, parts_of(A->plan64), s->x0_nz, s->part_b, s->nblk, s->part_xr, s->part_s));
         rc = capture_loop<double>(s, st, s->sc, s->X, s->R, s->R0, s->P, s->V, s->S, s->T, s->part_xr, s->part_s,
                                   false, merged);
         if (rc != HHP_OK) break;
@@ -1354,7 +1411,7 @@ hhp_status build_g64(Solver *s, bool merged) {
     cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
     cudaGraphDestroy(g);
     HHP_CUDA(ie);
-    s->g64_kernels_pro = 3;
+    s->g64_kernels_pro = 4;
     s->g64_kernels_epi = 2;
     // launch_spmv64 counted its captured launches; graph launches are counted when executed.
     A->ctx->kernel_launches -= 2 + 2 * s->unroll;
@@ -1377,10 +1434,13 @@ hhp_status build_gmix(Solver *s, bool merged) {
             rc = HHP_ERR_CUDA;
             break;
         }
-        rc = launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0);
+        rc = launch_x0check(s, st);
         if (rc != HHP_OK) break;
-        HHP_CUDA(launch_k(k_mix_init, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc32, s->Y, s->R32, s->R0_32, s->D32,
-                          s->P32, s->V32, nu4, parts_of(A->plan64), s->part_xr32, s->part_s32));
+        rc = launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0, s->x0_nz);
+        if (rc != HHP_OK) break;
+        HHP_CUDA(launch_k(k_mix_init, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc32, s->Y, s->B, s->R32, s->R0_32,
+                          s->D32, s->P32, s->V32, nu4, parts_of(A->plan64), s->x0_nz, s->part_b, s->nblk,
+                          s->part_xr32, s->part_s32));
         rc = capture_loop<float>(s, st, s->sc32, s->D32, s->R32, s->R0_32, s->P32, s->V32, s->S32, s->T32,
                                  s->part_xr32, s->part_s32, true, merged);
         if (rc != HHP_OK) break;
@@ -1401,7 +1461,7 @@ hhp_status build_gmix(Solver *s, bool merged) {
     cudaError_t ie = cudaGraphInstantiate(merged ? &s->gmixm : &s->gmix, g, 0);
     cudaGraphDestroy(g);
     HHP_CUDA(ie);
-    s->gmix_kernels_pro = 3;
+    s->gmix_kernels_pro = 4;
     s->gmix_kernels_epi = 3;
     // launch_spmv* counted their captured launches; graph launches are counted when executed.
     A->ctx->kernel_launches -= 2 + 3 * s->unroll;
@@ -1642,7 +1702,8 @@ void solver_release(Solver *s) {
     if (s->gmix) cudaGraphExecDestroy(s->gmix);
     if (s->gmixm) cudaGraphExecDestroy(s->gmixm);
     double *d[] = {s->X, s->B, s->R, s->R0, s->P, s->V, s->S, s->T, s->Y, s->part_xr, s->part_s, s->part_xr32,
-                   s->part_s32, s->hist};
+                   s->part_s32, s->part_b, s->hist};
+    cudaFree(s->x0_nz);
     for (double *p : d) cudaFree(p);
     float *f[] = {s->D32, s->R32, s->R0_32, s->P32, s->V32, s->S32, s->T32};
     for (float *p : f) cudaFree(p);

@@ -190,10 +190,10 @@ def test_merged_loop_is_four_kernels_per_iteration(ctx, cfg):
         n = ctx.kernel_launches - n0
         assert r.status == 0 and r.rel_res_true <= 1e-10 and r.err_vs_target <= 1e-6
         if r.outer_iters == 1:
-            # residual SpMV, init, first stop test; 2 iterations per loop body (a body that
-            # stops after its first iteration still launches its second, which returns at once);
-            # true-residual SpMV and finish
-            assert n == 3 + per_iter * 2 * math.ceil(r.iters / 2) + 2, (loop, n, r.iters)
+            # x0 check, residual SpMV (skipped for x0 = 0, still launched), init, first stop test;
+            # 2 iterations per loop body (a body that stops after its first iteration still
+            # launches its second, which returns at once); true-residual SpMV and finish
+            assert n == 4 + per_iter * 2 * math.ceil(r.iters / 2) + 2, (loop, n, r.iters)
     A.close()
 
 

@@ -52,9 +52,9 @@ def test_mixed_merged_and_classic_inner_loops(ctx, sysname):
         assert r.status == 0 and r.rel_res_true <= 1e-10 and not r.fp64_fallback, (loop, r)
         resid = s.b - orc.spmv(s.rowptr, s.col, s.val, x)
         assert np.sqrt(orc.dot(resid, resid) / orc.dot(s.b, s.b)) <= 1.0000001e-10
-        # residual SpMV, init, first stop test; bodies of 2 iterations; 3 per update; fold, true
-        # residual, finish
-        assert n == 3 + per_iter * 2 * math.ceil(r.iters / 2) + 3 * r.outer_iters + 3, (loop, n, r.iters,
+        # x0 check, residual SpMV, init, first stop test; bodies of 2 iterations; 3 per update;
+        # fold, true residual, finish
+        assert n == 4 + per_iter * 2 * math.ceil(r.iters / 2) + 3 * r.outer_iters + 3, (loop, n, r.iters,
                                                                                         r.outer_iters)
         res[loop] = (x, r)
     assert res["merged"][1].iters <= 1.1 * res["classic"][1].iters + 3
