@@ -259,3 +259,22 @@ def test_merged_and_classic_loops_on_long_rows(ctx):
     for key, x in xs.items():
         assert np.max(np.abs(x - xs["classic", "fp64"])) <= 1e-6 * scale, key
     A.close()
+
+
+def test_zero_start_shortcut_agrees_with_general_start(ctx):
+    """x0 = 0 (and -0) skips the initial residual SpMV (r = b); a single nonzero entry takes the
+    general path. All three reach the tolerance and the same solution."""
+    s = synth.config("c1")
+    A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
+    x_z, r_z = bicgstab(ctx, A, s.b, np.zeros(s.n), rtol=1e-10, maxit=3000)
+    x_m, r_m = bicgstab(ctx, A, s.b, np.full(s.n, -0.0), rtol=1e-10, maxit=3000)
+    assert r_m.iters == r_z.iters and np.array_equal(x_m, x_z)
+    x1 = np.zeros(s.n)
+    x1[s.n // 3] = 1e-3
+    x_g, r_g = bicgstab(ctx, A, s.b, x1, rtol=1e-10, maxit=3000)
+    for x, r in ((x_z, r_z), (x_g, r_g)):
+        assert r.status == 0 and r.rel_res_true <= 1e-10
+        res = s.b - orc.spmv(s.rowptr, s.col, s.val, x)
+        assert math.sqrt(orc.dot(res, res) / orc.dot(s.b, s.b)) <= 1.0000001e-10
+    assert np.max(np.abs(x_g - x_z)) <= 1e-6 * np.max(np.abs(x_z))
+    A.close()
