@@ -180,7 +180,7 @@ inline int pad4(int n) { return (n + 3) & ~3; }
 struct Tuning {
     // ctas_per_sm, spmv_unroll, rpl64: 0 = chosen per matrix at plan time; d16 0: never 16-bit offsets
     int cap = 2048, long_thr = 256, window = 8192, wpc = 8, ctas_per_sm = 0, vec_blocks_per_sm = 1,
-        unroll_iters = 2, spmv_unroll = 0, rpl64 = 0, rpl32 = 4, d16 = 1;
+        unroll_iters = 4, spmv_unroll = 0, rpl64 = 0, rpl32 = 4, d16 = 1;
 };
 const Tuning &tuning();
 

@@ -128,6 +128,14 @@ __device__ __forceinline__ double dunit4(double acc, float4 a, float4 b) {
 
 __device__ __forceinline__ bool b0t0() { return blockIdx.x == 0 && threadIdx.x == 0; }
 
+// A step after the loop's end (a body runs its remaining iterations once the stop test has
+// fired): the terminal status was written by an earlier launch, so every block sees it and the
+// kernel returns before any load or reduction. The kernel that ends an iteration still counts
+// the body and clears the loop condition.
+__device__ __forceinline__ bool dead_step(const DevScal *sc) {
+    return *reinterpret_cast<volatile const int *>(&sc->status) != ST_RUNNING;
+}
+
 struct SpmvParts {
     const double *cta_part;
     int n_cta;
@@ -245,6 +253,13 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
                                            const double *part_s, int nparts, double *hist, int hist_cap,
                                            cudaGraphConditionalHandle cond, int first_in_body, const int *dev_err,
                                            int use_cond) {
+    if (dead_step(sc)) {
+        if (b0t0()) {
+            if (first_in_body) sc->bodies += 1;
+            if (use_cond) cudaGraphSetConditional(cond, 0);
+        }
+        return;
+    }
     __shared__ double red[kRedScratch];
     __shared__ double bc[2];
     __shared__ int go;
@@ -328,6 +343,7 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
 template <typename T, bool M = false>
 __global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const T *V, const T *R0, int nu,
                                            SpmvParts sp, double *part_s) {
+    if (dead_step(sc)) return;
     __shared__ double red[kRedScratch];
     __shared__ double bc[1];
     __shared__ int go;
@@ -409,6 +425,7 @@ template <typename T>
 __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P, const T *S, const T *Tv,
                                             const T *R0, int nu, SpmvParts sp, const double *part_s, int nparts,
                                             double *part_xr) {
+    if (dead_step(sc)) return;
     __shared__ double red[kRedScratch];
     __shared__ double bc[2];
     __shared__ int go, hf;
@@ -517,6 +534,13 @@ __global__ void __launch_bounds__(512) k_xrp(DevScal *sc, T *X, T *R, T *P, cons
                                              int nu, SpmvParts sp, const double *part_s, int nparts, double *hist,
                                              int hist_cap, cudaGraphConditionalHandle cond, int first_in_body,
                                              const int *dev_err, int use_cond) {
+    if (dead_step(sc)) {
+        if (b0t0()) {
+            if (first_in_body) sc->bodies += 1;
+            if (use_cond) cudaGraphSetConditional(cond, 0);
+        }
+        return;
+    }
     __shared__ double red[kRedScratch];
     __shared__ double bc[3];
     __shared__ int go;  // 0: nothing to do, 1: full step and p, 2: half step, 3: full step, last
@@ -739,6 +763,14 @@ __global__ void __launch_bounds__(512) k_p_ru(DevScal *sc, double *X, float *D32
                                               const double *part_s, int nparts, double *hist, int hist_cap,
                                               cudaGraphConditionalHandle wcond, cudaGraphConditionalHandle icond,
                                               int first_in_body, const int *dev_err) {
+    if (dead_step(sc)) {
+        if (b0t0()) {
+            if (first_in_body) sc->bodies += 1;
+            cudaGraphSetConditional(icond, 0u);
+            cudaGraphSetConditional(wcond, 0);
+        }
+        return;
+    }
     __shared__ double red[kRedScratch];
     __shared__ float bc[2];
     __shared__ int go;  // 0: nothing, 1: p update, 2: fold d into x
@@ -833,6 +865,14 @@ __global__ void __launch_bounds__(512) k_xrp_ru(DevScal *sc, double *X, float *D
                                                 const double *part_s, int nparts, double *hist, int hist_cap,
                                                 cudaGraphConditionalHandle wcond, cudaGraphConditionalHandle icond,
                                                 int first_in_body, const int *dev_err) {
+    if (dead_step(sc)) {
+        if (b0t0()) {
+            if (first_in_body) sc->bodies += 1;
+            cudaGraphSetConditional(icond, 0u);
+            cudaGraphSetConditional(wcond, 0);
+        }
+        return;
+    }
     __shared__ double red[kRedScratch];
     __shared__ float bc[3];
     __shared__ int go;  // 0: nothing, 1: d, r, p updates, 2: fold d + alpha p + omega s into x

@@ -19,6 +19,7 @@ from hethyppar_gb300 import HHPError, Matrix, bicgstab, synth
 from oracle import oracle as orc
 
 pytestmark = pytest.mark.gpu
+BODY = 4  # iterations per loop-graph body (the library default; HHP_UNROLL_ITERS unset)
 SOLVE_CASES = [n for n in golden_names() if n not in ("crafted5",)]
 
 
@@ -191,9 +192,9 @@ def test_merged_loop_is_four_kernels_per_iteration(ctx, cfg):
         assert r.status == 0 and r.rel_res_true <= 1e-10 and r.err_vs_target <= 1e-6
         if r.outer_iters == 1:
             # x0 check, residual SpMV (skipped for x0 = 0, still launched), init, first stop test;
-            # 2 iterations per loop body (a body that stops after its first iteration still
-            # launches its second, which returns at once); true-residual SpMV and finish
-            assert n == 4 + per_iter * 2 * math.ceil(r.iters / 2) + 2, (loop, n, r.iters)
+            # BODY iterations per loop body (a body that stops early still launches its remaining
+            # iterations, which return at once); true-residual SpMV and finish
+            assert n == 4 + per_iter * BODY * math.ceil(r.iters / BODY) + 2, (loop, n, r.iters)
     A.close()
 
 

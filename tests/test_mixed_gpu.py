@@ -9,6 +9,7 @@ from hethyppar_gb300 import Matrix, bicgstab, synth
 from oracle import oracle as orc
 
 pytestmark = pytest.mark.gpu
+BODY = 4  # iterations per loop-graph body (the library default; HHP_UNROLL_ITERS unset)
 
 
 @pytest.mark.parametrize("sysname", ["c1", "cd3d_48", "banded"])
@@ -52,10 +53,10 @@ def test_mixed_merged_and_classic_inner_loops(ctx, sysname):
         assert r.status == 0 and r.rel_res_true <= 1e-10 and not r.fp64_fallback, (loop, r)
         resid = s.b - orc.spmv(s.rowptr, s.col, s.val, x)
         assert np.sqrt(orc.dot(resid, resid) / orc.dot(s.b, s.b)) <= 1.0000001e-10
-        # x0 check, residual SpMV, init, first stop test; bodies of 2 iterations; 3 per update;
-        # fold, true residual, finish
-        assert n == 4 + per_iter * 2 * math.ceil(r.iters / 2) + 3 * r.outer_iters + 3, (loop, n, r.iters,
-                                                                                        r.outer_iters)
+        # x0 check, residual SpMV, init, first stop test; bodies of BODY iterations; 3 per
+        # update; fold, true residual, finish
+        assert n == 4 + per_iter * BODY * math.ceil(r.iters / BODY) + 3 * r.outer_iters + 3, (
+            loop, n, r.iters, r.outer_iters)
         res[loop] = (x, r)
     assert res["merged"][1].iters <= 1.1 * res["classic"][1].iters + 3
     scale = np.max(np.abs(s.x_target))
