@@ -327,7 +327,26 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
             stu(P, u, p[k]);
         }
     }
-    for (int u = u0 + kPre * stride; u < nu; u += stride) {
+    // further units: whole batches of kPre with every load requested before the arithmetic (no
+    // per-unit guards: a multiply-add predicated off still takes an FP64 pipe slot), then the
+    // last few one at a time
+    int ub = u0 + kPre * stride;
+    for (; ub + (kPre - 1) * stride < nu; ub += kPre * stride) {
+        T pp[kPre][E], vx[kPre][E], rx[kPre][E];
+#pragma unroll
+        for (int k = 0; k < kPre; ++k) {
+            ldu(pp[k], P, ub + k * stride);
+            ldu(vx[k], V, ub + k * stride);
+            ldu(rx[k], R, ub + k * stride);
+        }
+#pragma unroll
+        for (int k = 0; k < kPre; ++k) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) pp[k][e] = tfma(tb, tfma(tw, vx[k][e], pp[k][e]), rx[k][e]);
+            stu(P, ub + k * stride, pp[k]);
+        }
+    }
+    for (int u = ub; u < nu; u += stride) {
         T pp[E], vx[E], rx[E];
         ldu(pp, P, u);
         ldu(vx, V, u);
@@ -397,7 +416,27 @@ __global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const 
             stu(S, u, sv);
         }
     }
-    for (int u = u0 + KP * stride; u < nu; u += stride) {
+    // whole batches of KP units, then the last few one at a time (see K_P)
+    int ub = u0 + KP * stride;
+    for (; ub + (KP - 1) * stride < nu; ub += KP * stride) {
+        T rx[KP][E], vx[KP][E], qx[M ? KP : 1][E];
+#pragma unroll
+        for (int k = 0; k < KP; ++k) {
+            ldu(rx[k], R, ub + k * stride);
+            ldu(vx[k], V, ub + k * stride);
+            if constexpr (M) ldu(qx[k], R0, ub + k * stride);
+        }
+#pragma unroll
+        for (int k = 0; k < KP; ++k) {
+            T sv[E];
+#pragma unroll
+            for (int e = 0; e < E; ++e) sv[e] = tfma(ta, vx[k][e], rx[k][e]);
+            acc[0] = dunit<E>(acc[0], sv, sv);
+            if constexpr (M) acc[M ? 1 : 0] = dunit<E>(acc[M ? 1 : 0], sv, qx[k]);
+            stu(S, ub + k * stride, sv);
+        }
+    }
+    for (int u = ub; u < nu; u += stride) {
         T rx[E], vx[E], sv[E];
         ldu(rx, R, u);
         ldu(vx, V, u);
@@ -500,7 +539,21 @@ __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P,
         const int u = u0 + k * stride;
         if (u < nu) unit(u, x[k], p[k], s[k], r0[k], t[k]);
     }
-    for (int u = u0 + kPre * stride; u < nu; u += stride) {
+    // whole batches of kPre units, then the last few one at a time (see K_P)
+    int ub = u0 + kPre * stride;
+    for (; ub + (kPre - 1) * stride < nu; ub += kPre * stride) {
+#pragma unroll
+        for (int k = 0; k < kPre; ++k) {
+            ldu(x[k], X, ub + k * stride);
+            ldu(p[k], P, ub + k * stride);
+            ldu(s[k], S, ub + k * stride);
+            ldu(r0[k], R0, ub + k * stride);
+            ldu(t[k], Tv, ub + k * stride);
+        }
+#pragma unroll
+        for (int k = 0; k < kPre; ++k) unit(ub + k * stride, x[k], p[k], s[k], r0[k], t[k]);
+    }
+    for (int u = ub; u < nu; u += stride) {
         T xx[E], pp[E], ss[E], rr0[E], tt[E];
         ldu(xx, X, u);
         ldu(pp, P, u);
@@ -654,7 +707,21 @@ __global__ void __launch_bounds__(512) k_xrp(DevScal *sc, T *X, T *R, T *P, cons
         const int u = u0 + k * stride;
         if (u < nu) unit(u, x[k], p[k], s[k], t[k], vv[k]);
     }
-    for (int u = u0 + kPreX * stride; u < nu; u += stride) {
+    // whole batches of kPreX units, then the last few one at a time (see K_P)
+    int ub = u0 + kPreX * stride;
+    for (; ub + (kPreX - 1) * stride < nu; ub += kPreX * stride) {
+#pragma unroll
+        for (int k = 0; k < kPreX; ++k) {
+            ldu(x[k], X, ub + k * stride);
+            ldu(p[k], P, ub + k * stride);
+            ldu(s[k], S, ub + k * stride);
+            ldu(t[k], Tv, ub + k * stride);
+            ldu(vv[k], V, ub + k * stride);
+        }
+#pragma unroll
+        for (int k = 0; k < kPreX; ++k) unit(ub + k * stride, x[k], p[k], s[k], t[k], vv[k]);
+    }
+    for (int u = ub; u < nu; u += stride) {
         T xx[E], pp[E], ss[E], tt[E], vx[E];
         ldu(xx, X, u);
         ldu(pp, P, u);
@@ -983,7 +1050,21 @@ __global__ void __launch_bounds__(512) k_xrp_ru(DevScal *sc, double *X, float *D
         const int u = u0 + k * stride;
         if (u < nu4) unit(u, d[k], p[k], s[k], t[k], vv[k]);
     }
-    for (int u = u0 + kPreX * stride; u < nu4; u += stride) {
+    // whole batches of kPreX units, then the last few one at a time (see K_P)
+    int ub = u0 + kPreX * stride;
+    for (; ub + (kPreX - 1) * stride < nu4; ub += kPreX * stride) {
+#pragma unroll
+        for (int k = 0; k < kPreX; ++k) {
+            ldu(d[k], D32, ub + k * stride);
+            ldu(p[k], P, ub + k * stride);
+            ldu(s[k], S, ub + k * stride);
+            ldu(t[k], Tv, ub + k * stride);
+            ldu(vv[k], V, ub + k * stride);
+        }
+#pragma unroll
+        for (int k = 0; k < kPreX; ++k) unit(ub + k * stride, d[k], p[k], s[k], t[k], vv[k]);
+    }
+    for (int u = ub; u < nu4; u += stride) {
         float dd[4], pp[4], ss[4], tt[4], vx[4];
         ldu(dd, D32, u);
         ldu(pp, P, u);
