@@ -309,9 +309,55 @@ def run_ours(args, rk):
                 e1.synchronize()
                 cus_ms.append(e0.elapsed_time(e1))
         cus_err = float((yc - ys).abs().max().item())
+        # library comparator for the whole solve: the reference's device-pointer loop
+        # (bicgstab_gpu_dp.c:163-196) restated with library calls -- cuSPARSE SpMV (torch.mv),
+        # cuBLAS dots (torch.dot), scalars kept on the device, elementwise updates as torch
+        # kernels -- run for our iteration count on the same system, L2 flushed first
+        bl = torch.as_tensor(s.b, device="cuda")
+
+        def lib_loop(k):
+            x = torch.zeros_like(bl)
+            r = bl - torch.mv(At, x)
+            r0 = r.clone()
+            p = torch.zeros_like(bl)
+            v = torch.zeros_like(bl)
+            one = torch.ones((), dtype=torch.float64, device="cuda")
+            rho, alpha, omega = one, one, one
+            for _ in range(k):
+                rho_new = torch.dot(r, r0)
+                beta = (rho_new / rho) * (alpha / omega)
+                p = (p - omega * v) * beta + r
+                v = torch.mv(At, p)
+                alpha = rho_new / torch.dot(r0, v)
+                rho = rho_new
+                sv = r - alpha * v
+                t = torch.mv(At, sv)
+                omega = torch.dot(t, sv) / torch.dot(t, t)
+                x = x + alpha * p + omega * sv
+                r = sv - omega * t
+            return x
+
+        with torch.cuda.stream(stream):
+            lib_loop(res.iters)
+            lib_ms = []
+            for _ in range(3):
+                torch.cuda.synchronize()
+                flush_l2(sync=False)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                xl = lib_loop(res.iters)
+                e1.record(stream)
+                e1.synchronize()
+                lib_ms.append(e0.elapsed_time(e1))
+        rl = bl - torch.mv(At, xl)
+        lib_loop_res = {"ms": statistics.mean(lib_ms), "iters": res.iters,
+                        "rel_res_true": float(torch.linalg.vector_norm(rl) / torch.linalg.vector_norm(bl)),
+                        "via": "reference dp-loop math on cuSPARSE SpMV (torch.mv) + cuBLAS dot (torch.dot) + "
+                               "torch elementwise kernels, scalars on the device, no graph"}
         del At
     except Exception as e:  # reported, not fatal
         cus_err = str(e)
+        lib_loop_res = {"error": str(e)}
     hbm, peak_kind = peaks()
     bsp = spmv_bytes(s.m, s.n, s.nnz)
     t_sp = statistics.mean(spmv_ms) * 1e-3  # mean: the event clock ticks in ~2 us steps
@@ -341,6 +387,7 @@ def run_ours(args, rk):
                               "gbs_l2_flushed": bsp / (statistics.mean(cus_ms) * 1e-3) / 1e9,
                               "max_abs_diff_vs_ours": cus_err, "via": "torch.mv on a sparse CSR tensor (cuSPARSE SpMV)"}
                              if cus_ms else {"error": cus_err}),
+           "solve_cusparse_cublas": lib_loop_res,
            "spmv": {"gbs_l2_flushed": achieved, "frac_of_hbm": achieved / hbm, "us_l2_flushed": t_sp * 1e6,
                     "gbs_effective_warm_l2": bsp / (warm_ms * 1e-3) / 1e9, "us_warm": warm_ms * 1e3},
            "clocks": clk, "gpu_launches": int(launches)}
