@@ -130,8 +130,9 @@ __device__ __forceinline__ bool b0t0() { return blockIdx.x == 0 && threadIdx.x =
 
 // A step after the loop's end (a body runs its remaining iterations once the stop test has
 // fired): the terminal status was written by an earlier launch, so every block sees it and the
-// kernel returns before any load or reduction. The kernel that ends an iteration still counts
-// the body and clears the loop condition.
+// kernel returns after its prologue (the status is read with the operand and record loads, so a
+// live step pays no extra memory latency for the test), before any store. The kernel that ends
+// an iteration still counts the body and clears the loop condition.
 __device__ __forceinline__ bool dead_step(const DevScal *sc) {
     return *reinterpret_cast<volatile const int *>(&sc->status) != ST_RUNNING;
 }
@@ -253,13 +254,7 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
                                            const double *part_s, int nparts, double *hist, int hist_cap,
                                            cudaGraphConditionalHandle cond, int first_in_body, const int *dev_err,
                                            int use_cond) {
-    if (dead_step(sc)) {
-        if (b0t0()) {
-            if (first_in_body) sc->bodies += 1;
-            if (use_cond) cudaGraphSetConditional(cond, 0);
-        }
-        return;
-    }
+    const bool dead = dead_step(sc);  // tested after the operand and record loads are in flight
     __shared__ double red[kRedScratch];
     __shared__ double bc[2];
     __shared__ int go;
@@ -279,6 +274,13 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
     }
     double q[4];  // r.r0, r.r (2-wide records), s.s (4-wide K_S records)
     reduce_two<2, 2, 1, 4, 4>(part_xr, nparts, nullptr, 0, part_s, nparts, q, red);
+    if (dead) {
+        if (b0t0()) {
+            if (first_in_body) sc->bodies += 1;
+            if (use_cond) cudaGraphSetConditional(cond, 0);
+        }
+        return;
+    }
     if (threadIdx.x == 0) {
         const double rho_new = q[0], rr = q[1], ss = q[2];
         const bool lead = blockIdx.x == 0;
@@ -362,7 +364,7 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
 template <typename T, bool M = false>
 __global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const T *V, const T *R0, int nu,
                                            SpmvParts sp, double *part_s) {
-    if (dead_step(sc)) return;
+    const bool dead = dead_step(sc);  // tested after the operand and record loads are in flight
     __shared__ double red[kRedScratch];
     __shared__ double bc[1];
     __shared__ int go;
@@ -381,6 +383,7 @@ __global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const 
     }
     double v[1];  // r0.v: the first component of the SpMV's 2-wide records
     reduce_partials<1, 2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
+    if (dead) return;
     if (threadIdx.x == 0) {
         int ok = sc->status == ST_RUNNING;
         if (ok) {
@@ -464,7 +467,7 @@ template <typename T>
 __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P, const T *S, const T *Tv,
                                             const T *R0, int nu, SpmvParts sp, const double *part_s, int nparts,
                                             double *part_xr) {
-    if (dead_step(sc)) return;
+    const bool dead = dead_step(sc);  // tested after the operand and record loads are in flight
     __shared__ double red[kRedScratch];
     __shared__ double bc[2];
     __shared__ int go, hf;
@@ -486,6 +489,7 @@ __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P,
     }
     double q[4];  // t.s, t.t (2-wide SpMV records), s.s (4-wide K_S records)
     reduce_two<2, 2, 1, 4, 4>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, part_s, nparts, q, red);
+    if (dead) return;
     if (threadIdx.x == 0) {
         int ok = sc->status == ST_RUNNING;
         int half = 0;
@@ -587,13 +591,7 @@ __global__ void __launch_bounds__(512) k_xrp(DevScal *sc, T *X, T *R, T *P, cons
                                              int nu, SpmvParts sp, const double *part_s, int nparts, double *hist,
                                              int hist_cap, cudaGraphConditionalHandle cond, int first_in_body,
                                              const int *dev_err, int use_cond) {
-    if (dead_step(sc)) {
-        if (b0t0()) {
-            if (first_in_body) sc->bodies += 1;
-            if (use_cond) cudaGraphSetConditional(cond, 0);
-        }
-        return;
-    }
+    const bool dead = dead_step(sc);  // tested after the operand and record loads are in flight
     __shared__ double red[kRedScratch];
     __shared__ double bc[3];
     __shared__ int go;  // 0: nothing to do, 1: full step and p, 2: half step, 3: full step, last
@@ -613,6 +611,13 @@ __global__ void __launch_bounds__(512) k_xrp(DevScal *sc, T *X, T *R, T *P, cons
     }
     double q[8];  // t.s, t.t, r0.t (4-wide SpMV records), s.s, r0.s (4-wide K_S records)
     reduce_two<3, 4, 2, 4, 8>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, part_s, nparts, q, red);
+    if (dead) {
+        if (b0t0()) {
+            if (first_in_body) sc->bodies += 1;
+            if (use_cond) cudaGraphSetConditional(cond, 0);
+        }
+        return;
+    }
     if (threadIdx.x == 0) {
         const bool lead = blockIdx.x == 0;
         int mode = 0, term = *reinterpret_cast<volatile const int *>(&sc->status);
@@ -932,14 +937,7 @@ __global__ void __launch_bounds__(512) k_xrp_ru(DevScal *sc, double *X, float *D
                                                 const double *part_s, int nparts, double *hist, int hist_cap,
                                                 cudaGraphConditionalHandle wcond, cudaGraphConditionalHandle icond,
                                                 int first_in_body, const int *dev_err) {
-    if (dead_step(sc)) {
-        if (b0t0()) {
-            if (first_in_body) sc->bodies += 1;
-            cudaGraphSetConditional(icond, 0u);
-            cudaGraphSetConditional(wcond, 0);
-        }
-        return;
-    }
+    const bool dead = dead_step(sc);  // tested after the operand and record loads are in flight
     __shared__ double red[kRedScratch];
     __shared__ float bc[3];
     __shared__ int go;  // 0: nothing, 1: d, r, p updates, 2: fold d + alpha p + omega s into x
@@ -958,6 +956,14 @@ __global__ void __launch_bounds__(512) k_xrp_ru(DevScal *sc, double *X, float *D
     }
     double q[8];  // t.s, t.t, r0.t (4-wide SpMV records), s.s, r0.s (4-wide K_S records)
     reduce_two<3, 4, 2, 4, 8>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, part_s, nparts, q, red);
+    if (dead) {
+        if (b0t0()) {
+            if (first_in_body) sc->bodies += 1;
+            cudaGraphSetConditional(icond, 0u);
+            cudaGraphSetConditional(wcond, 0);
+        }
+        return;
+    }
     if (threadIdx.x == 0) {
         const bool lead = blockIdx.x == 0;
         int what = 0, term = *reinterpret_cast<volatile const int *>(&sc->status);

@@ -326,10 +326,11 @@ struct MinCtas {
 
 template <typename VT, int R, int U, int EP, bool D16>
 __global__ void __launch_bounds__(256, MinCtas<R, U>::value) k_spmv(const SellArgs<VT> a) {
-    // After a recorded device error every later launch returns at once (uniform across the grid).
-    if (*reinterpret_cast<volatile const int *>(a.err) != DEV_OK) return;
-    if (a.gate && *a.gate == 0) return;
-    if (a.stop && *reinterpret_cast<volatile const int *>(a.stop) != 0) return;
+    // After a recorded device error, with the gate closed, or once the solver's status is
+    // terminal, the launch returns at once (uniform across the grid). The three words were
+    // written by earlier launches: read together (one memory latency, not three), through L2.
+    const int err = __ldcg(a.err), gate = a.gate ? __ldcg(a.gate) : 1, stop = a.stop ? __ldcg(a.stop) : 0;
+    if (err != DEV_OK || gate == 0 || stop != 0) return;
     __shared__ double red[32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int gw = blockIdx.x * nw + warp;
