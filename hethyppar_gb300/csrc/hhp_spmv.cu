@@ -144,7 +144,8 @@ __device__ __forceinline__ T comp(const V &v, int t) {
 // Row epilogue: stores y[r]; accumulates dot partials into (d0, d1, d2), in the value type (the
 // caller folds them into FP64 once per slice for FP32 data).
 template <typename VT, int EP, typename DT>
-__device__ __forceinline__ void row_epilogue(const SellArgs<VT> &a, int r, VT acc, DT &d0, DT &d1, DT &d2) {
+__device__ __forceinline__ void row_epilogue(const SellArgs<VT> &a, int r, VT acc, DT &d0, DT &d1, DT &d2,
+                                             VT w1r, VT w2r) {
     if (EP == EP_Y) {
         a.y[r] = acc;
     } else if (EP == EP_AXPBY) {
@@ -154,18 +155,18 @@ __device__ __forceinline__ void row_epilogue(const SellArgs<VT> &a, int r, VT ac
         a.y[r] = out;
     } else if (EP == EP_DOT1) {
         a.y[r] = acc;
-        d0 = vfma(static_cast<DT>(acc), static_cast<DT>(__ldg(a.w1 + r)), d0);
+        d0 = vfma(static_cast<DT>(acc), static_cast<DT>(w1r), d0);
     } else if (EP == EP_DOT2) {
         a.y[r] = acc;
-        d0 = vfma(static_cast<DT>(acc), static_cast<DT>(__ldg(a.w1 + r)), d0);
+        d0 = vfma(static_cast<DT>(acc), static_cast<DT>(w1r), d0);
         d1 = vfma(static_cast<DT>(acc), static_cast<DT>(acc), d1);
     } else if (EP == EP_DOT3) {
         a.y[r] = acc;
-        d0 = vfma(static_cast<DT>(acc), static_cast<DT>(__ldg(a.w1 + r)), d0);
+        d0 = vfma(static_cast<DT>(acc), static_cast<DT>(w1r), d0);
         d1 = vfma(static_cast<DT>(acc), static_cast<DT>(acc), d1);
-        d2 = vfma(static_cast<DT>(acc), static_cast<DT>(__ldg(a.w2 + r)), d2);
+        d2 = vfma(static_cast<DT>(acc), static_cast<DT>(w2r), d2);
     } else {  // EP_RESID
-        const VT b = __ldg(a.w1 + r);
+        const VT b = w1r;
         const VT res = b - acc;
         a.y[r] = res;
         d0 = vfma(static_cast<DT>(res), static_cast<DT>(res), d0);
@@ -201,6 +202,21 @@ __device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, int lane,
     auto colof = [&](const CW &w, int t) -> int {
         return D16 ? row[t] + static_cast<int>(comp<CW, CT>(w, t)) : static_cast<int>(comp<CW, CT>(w, t));
     };
+    // the epilogue's vector operands, requested before the slice's main loop so that their
+    // latency is hidden behind it
+    // (only where the registers allow: the wide-unroll instantiations)
+    constexpr bool W1 = EP == EP_DOT1 || EP == EP_DOT2 || EP == EP_DOT3 || EP == EP_RESID;
+    constexpr bool EARLY = R * U >= 8;
+    VT w1v[R], w2v[R];
+    auto load_w = [&]() {
+#pragma unroll
+        for (int t = 0; t < R; ++t) {
+            const bool ok = row[t] >= 0 && row[t] < a.m;
+            w1v[t] = (W1 && ok) ? __ldg(a.w1 + row[t]) : VT(0);
+            w2v[t] = (EP == EP_DOT3 && ok) ? __ldg(a.w2 + row[t]) : VT(0);
+        }
+    };
+    if constexpr (EARLY) load_w();
     const VV *vp = reinterpret_cast<const VV *>(a.sval + base) + lane;
     const CW *cp = D16 ? reinterpret_cast<const CW *>(a.scol16 + base) + lane
                        : reinterpret_cast<const CW *>(a.scol + base) + lane;
@@ -258,11 +274,12 @@ __device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, int lane,
         for (int t = 0; t < R; ++t)
             if (j < len[t]) acc[t] = vfma(comp<VV, VT>(vt, t), xt[t], acc[t]);
     }
+    if constexpr (!EARLY) load_w();
     VT e0 = VT(0), e1 = VT(0), e2 = VT(0);
 #pragma unroll
     for (int t = 0; t < R; ++t) {
         const int r = row[t];
-        if (r >= 0 && r < a.m) row_epilogue<VT, EP>(a, r, acc[t], e0, e1, e2);
+        if (r >= 0 && r < a.m) row_epilogue<VT, EP>(a, r, acc[t], e0, e1, e2, w1v[t], w2v[t]);
     }
     if (EP != EP_AXPBY && EP != EP_Y) {
         d0 += static_cast<double>(e0);
@@ -304,7 +321,9 @@ __device__ __forceinline__ void do_chunk(const SellArgs<VT> &a, int c, int lane)
             for (int q = 0; q < nch; ++q) tot += __ldcg(a.chunk_part + c_first + q);
             a.long_cnt[l] = 0u;  // ready for the next launch
             double e0 = 0.0, e1 = 0.0, e2 = 0.0;
-            row_epilogue<VT, EP, double>(a, d.x, static_cast<VT>(tot), e0, e1, e2);
+            constexpr bool W1 = EP == EP_DOT1 || EP == EP_DOT2 || EP == EP_DOT3 || EP == EP_RESID;
+            const VT w1r = W1 ? __ldg(a.w1 + d.x) : VT(0), w2r = EP == EP_DOT3 ? __ldg(a.w2 + d.x) : VT(0);
+            row_epilogue<VT, EP, double>(a, d.x, static_cast<VT>(tot), e0, e1, e2, w1r, w2r);
             if (EP == EP_DOT3) {
                 a.long_dot[4 * l] = e0;
                 a.long_dot[4 * l + 1] = e1;
