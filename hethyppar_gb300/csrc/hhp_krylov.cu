@@ -255,6 +255,10 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
                                            cudaGraphConditionalHandle cond, int first_in_body, const int *dev_err,
                                            int use_cond) {
     const bool dead = dead_step(sc);  // tested after the operand and record loads are in flight
+    // scalars written by earlier launches, read with the operand loads (off the critical path)
+    const int iter = sc->iter, it0 = sc->iter_start, maxit = sc->maxit,
+              dev_error = *reinterpret_cast<volatile const int *>(dev_err);
+    const double thr2 = sc->thr2_rec, rho_prev = sc->rho_prev, alpha = sc->alpha, omega = sc->omega;
     __shared__ double red[kRedScratch];
     __shared__ double bc[2];
     __shared__ int go;
@@ -284,21 +288,15 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
     if (threadIdx.x == 0) {
         const double rho_new = q[0], rr = q[1], ss = q[2];
         const bool lead = blockIdx.x == 0;
-        const int st = sc->status;
-        int term = ST_RUNNING;
+        int term = ST_RUNNING;  // the status was running at entry
         if (lead && first_in_body) sc->bodies += 1;  // bodies executed (kernel-launch accounting)
-        if (st != ST_RUNNING) {
-            if (lead && use_cond) cudaGraphSetConditional(cond, 0);
-            term = st;
-        } else {
-            const int iter = sc->iter, it0 = sc->iter_start;
-            const double thr2 = sc->thr2_rec;
+        {
             // raw ||r||^2: the host forms sqrt(rr / rr0), keeping FP64 sqrt and division off the
             // loop's critical path
             if (lead && iter > it0 && iter - 1 < hist_cap) hist[iter - 1] = rr;
             double beta = 0.0;
-            term = step_p(st, iter, it0, sc->maxit, thr2, rho_new, rr, ss, sc->rho_prev, sc->alpha, sc->omega,
-                          *reinterpret_cast<volatile const int *>(dev_err) != DEV_OK, beta);
+            term = step_p(ST_RUNNING, iter, it0, maxit, thr2, rho_new, rr, ss, rho_prev, alpha, omega,
+                          dev_error != DEV_OK, beta);
             if (term != ST_RUNNING) {
                 if (lead) {
                     sc->status = term;
@@ -307,7 +305,7 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
                 }
             } else {
                 bc[0] = beta;
-                bc[1] = -sc->omega;
+                bc[1] = -omega;
                 if (lead) {
                     sc->rho_cur = rho_new;
                     sc->beta = beta;
@@ -365,6 +363,9 @@ template <typename T, bool M = false>
 __global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const T *V, const T *R0, int nu,
                                            SpmvParts sp, double *part_s) {
     const bool dead = dead_step(sc);  // tested after the operand and record loads are in flight
+    // scalars written by earlier launches, read with the operand loads (off the critical path)
+    const double rho_cur = sc->rho_cur;
+    const int iter0 = sc->iter;
     __shared__ double red[kRedScratch];
     __shared__ double bc[1];
     __shared__ int go;
@@ -385,20 +386,18 @@ __global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const 
     reduce_partials<1, 2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
     if (dead) return;
     if (threadIdx.x == 0) {
-        int ok = sc->status == ST_RUNNING;
-        if (ok) {
-            const double rv = v[0];
-            const double alpha = sc->rho_cur / rv;
-            if (!finite_nonzero(rv) || !isfinite(alpha)) {
-                if (blockIdx.x == 0) sc->status = ST_BREAKDOWN;
-                ok = 0;
-            } else {
-                bc[0] = -alpha;
-                if (blockIdx.x == 0) {
-                    sc->alpha = alpha;
-                    sc->rho_prev = sc->rho_cur;
-                    sc->iter = sc->iter + 1;
-                }
+        int ok = 1;  // the status was running at entry
+        const double rv = v[0];
+        const double alpha = rho_cur / rv;
+        if (!finite_nonzero(rv) || !isfinite(alpha)) {
+            if (blockIdx.x == 0) sc->status = ST_BREAKDOWN;
+            ok = 0;
+        } else {
+            bc[0] = -alpha;
+            if (blockIdx.x == 0) {
+                sc->alpha = alpha;
+                sc->rho_prev = rho_cur;
+                sc->iter = iter0 + 1;
             }
         }
         go = ok;
@@ -468,6 +467,7 @@ __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P,
                                             const T *R0, int nu, SpmvParts sp, const double *part_s, int nparts,
                                             double *part_xr) {
     const bool dead = dead_step(sc);  // tested after the operand and record loads are in flight
+    const double thr2 = sc->thr2_rec, alpha = sc->alpha;  // read with the operand loads
     __shared__ double red[kRedScratch];
     __shared__ double bc[2];
     __shared__ int go, hf;
@@ -491,12 +491,11 @@ __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P,
     reduce_two<2, 2, 1, 4, 4>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, part_s, nparts, q, red);
     if (dead) return;
     if (threadIdx.x == 0) {
-        int ok = sc->status == ST_RUNNING;
+        int ok = 1;  // the status was running at entry
         int half = 0;
-        if (ok) {
-            const double thr2 = sc->thr2_rec;
+        {
             half = thr2 >= 0.0 && q[2] <= thr2;
-            bc[0] = sc->alpha;
+            bc[0] = alpha;
             bc[1] = 0.0;
             if (!half) {
                 const double omega = q[0] / q[1];
@@ -592,6 +591,9 @@ __global__ void __launch_bounds__(512) k_xrp(DevScal *sc, T *X, T *R, T *P, cons
                                              int hist_cap, cudaGraphConditionalHandle cond, int first_in_body,
                                              const int *dev_err, int use_cond) {
     const bool dead = dead_step(sc);  // tested after the operand and record loads are in flight
+    // scalars written by earlier launches, read with the operand loads (off the critical path)
+    const double thr2 = sc->thr2_rec, alpha = sc->alpha, rho_prev = sc->rho_prev;
+    const int iter = sc->iter, maxit = sc->maxit, dev_error = *reinterpret_cast<volatile const int *>(dev_err);
     __shared__ double red[kRedScratch];
     __shared__ double bc[3];
     __shared__ int go;  // 0: nothing to do, 1: full step and p, 2: half step, 3: full step, last
@@ -620,16 +622,14 @@ __global__ void __launch_bounds__(512) k_xrp(DevScal *sc, T *X, T *R, T *P, cons
     }
     if (threadIdx.x == 0) {
         const bool lead = blockIdx.x == 0;
-        int mode = 0, term = *reinterpret_cast<volatile const int *>(&sc->status);
+        int mode = 0, term = ST_RUNNING;  // the status was running at entry
         if (lead && first_in_body) sc->bodies += 1;  // bodies executed (kernel-launch accounting)
-        if (term == ST_RUNNING) {
+        {
             const double ts = q[0], tt = q[1], r0t = q[2], ss = q[3], r0s = q[4];
-            const double thr2 = sc->thr2_rec, alpha = sc->alpha;
-            const int iter = sc->iter;  // this iteration (K_S counted it)
-            double rr = ss;
+            double rr = ss;  // iter: this iteration (K_S counted it)
             bc[0] = alpha;
             bc[1] = 0.0;
-            if (*reinterpret_cast<volatile const int *>(dev_err) != DEV_OK) {
+            if (dev_error != DEV_OK) {
                 term = ST_DEVICE_ERROR;
             } else if (thr2 >= 0.0 && ss <= thr2) {
                 mode = 2;
@@ -644,14 +644,14 @@ __global__ void __launch_bounds__(512) k_xrp(DevScal *sc, T *X, T *R, T *P, cons
                     mode = 3;
                     if (thr2 >= 0.0 && fmax(rr, kCancel * ss) <= thr2) {
                         term = ST_CONVERGED;
-                    } else if (iter >= sc->maxit) {
+                    } else if (iter >= maxit) {
                         term = ST_MAXIT;
                     } else {
                         const double rho_new = r0s - omega * r0t;
                         if (!finite_nonzero(rho_new) || !isfinite(rr)) {
                             term = ST_BREAKDOWN;
                         } else {
-                            const double beta = (rho_new / sc->rho_prev) * (alpha / omega);
+                            const double beta = (rho_new / rho_prev) * (alpha / omega);
                             bc[2] = beta;
                             mode = 1;
                             if (lead) {
@@ -938,6 +938,11 @@ __global__ void __launch_bounds__(512) k_xrp_ru(DevScal *sc, double *X, float *D
                                                 cudaGraphConditionalHandle wcond, cudaGraphConditionalHandle icond,
                                                 int first_in_body, const int *dev_err) {
     const bool dead = dead_step(sc);  // tested after the operand and record loads are in flight
+    // scalars written by earlier launches, read with the operand loads (off the critical path)
+    const int it = sc->iter, it0 = sc->iter_start, maxit = sc->maxit,
+              dev_error = *reinterpret_cast<volatile const int *>(dev_err);
+    const double alpha = sc->alpha, rho_prev = sc->rho_prev, true_rr = sc->true_rr, thr2 = sc->thr2,
+                 inner2 = sc->inner_rtol2, mx_even = sc->rr_max[0], mx_odd = sc->rr_max[1];
     __shared__ double red[kRedScratch];
     __shared__ float bc[3];
     __shared__ int go;  // 0: nothing, 1: d, r, p updates, 2: fold d + alpha p + omega s into x
@@ -966,25 +971,24 @@ __global__ void __launch_bounds__(512) k_xrp_ru(DevScal *sc, double *X, float *D
     }
     if (threadIdx.x == 0) {
         const bool lead = blockIdx.x == 0;
-        int what = 0, term = *reinterpret_cast<volatile const int *>(&sc->status);
+        int what = 0, term = ST_RUNNING;  // the status was running at entry
         if (lead && first_in_body) sc->bodies += 1;
         if (term == ST_RUNNING) {
             const double ts = q[0], tt = q[1], r0t = q[2], ss = q[3], r0s = q[4];
-            const double omega = ts / tt, alpha = sc->alpha;
-            const int it = sc->iter;
-            if (*reinterpret_cast<volatile const int *>(dev_err) != DEV_OK) {
+            const double omega = ts / tt;
+            if (dev_error != DEV_OK) {
                 term = ST_DEVICE_ERROR;
             } else if (!finite_nonzero(tt) || !isfinite(omega)) {
                 term = ST_BREAKDOWN;
             } else {
                 const double rr = fmax(ss - omega * ts, 0.0);
-                const double mx = sc->rr_max[it & 1];
+                const double mx = (it & 1) ? mx_odd : mx_even;
                 bc[0] = static_cast<float>(alpha);
                 bc[1] = static_cast<float>(omega);
                 if (lead) sc->omega = omega;
-                if (!isfinite(rr) || rr > kDivergence2 * sc->true_rr) {
+                if (!isfinite(rr) || rr > kDivergence2 * true_rr) {
                     term = ST_BREAKDOWN;  // d is not folded into x
-                } else if (rr <= sc->thr2 || rr < sc->inner_rtol2 * mx || it >= sc->maxit) {
+                } else if (rr <= thr2 || rr < inner2 * mx || it >= maxit) {
                     if (lead) {
                         sc->rr_max[(it + 1) & 1] = mx;
                         sc->ru_flag = 1;
@@ -992,12 +996,12 @@ __global__ void __launch_bounds__(512) k_xrp_ru(DevScal *sc, double *X, float *D
                     what = 2;
                 } else {
                     if (lead) sc->rr_max[(it + 1) & 1] = fmax(mx, rr);
-                    if (lead && it > sc->iter_start && it - 1 < hist_cap) hist[it - 1] = rr;
+                    if (lead && it > it0 && it - 1 < hist_cap) hist[it - 1] = rr;
                     const double rho_new = r0s - omega * r0t;
                     if (!finite_nonzero(rho_new)) {
                         term = ST_BREAKDOWN;
                     } else {
-                        const double beta = (rho_new / sc->rho_prev) * (alpha / omega);
+                        const double beta = (rho_new / rho_prev) * (alpha / omega);
                         bc[2] = static_cast<float>(beta);
                         if (lead) {
                             sc->rho_cur = rho_new;
