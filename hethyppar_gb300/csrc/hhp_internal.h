@@ -61,6 +61,9 @@ struct PlanDev {
     int *pos_len = nullptr;           // n_slices * H
     int *warp_ptr = nullptr;          // n_warps + 1
     int *warp_units = nullptr;        // unit ids (slice s < n_slices, else chunk n_slices + c)
+    int4 *unit_rec = nullptr;         // per entry of warp_units: {unit, slice steps, slice start
+                                      // (low, high 32 bits)}, so a warp starts a slice's streams
+                                      // one dependent load after its unit id
     double imbalance = 1.0;           // max warp cost / mean warp cost
     void *sval = nullptr;             // total values (double or float), padding zero
     int *scol = nullptr;              // total column indices (when !d16)

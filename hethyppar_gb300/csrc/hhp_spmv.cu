@@ -108,6 +108,7 @@ struct SellArgs {
     const int *pos_len;
     const int *warp_ptr;
     const int *warp_units;
+    const int4 *unit_rec;
     const VT *sval;
     const int *scol;       // int32 columns, or
     const short *scol16;   // 16-bit offsets col - row (plans whose every |col - row| < 2^15)
@@ -175,16 +176,15 @@ __device__ __forceinline__ void row_epilogue(const SellArgs<VT> &a, int r, VT ac
 }
 
 template <typename VT, int R, int U, int EP, bool D16>
-__device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, int lane, double &d0, double &d1,
-                                         double &d2) {
+__device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, long long base, int wmax, int lane,
+                                         double &d0, double &d1, double &d2) {
     using VV = typename Vec<VT, R>::V;
     using IV = typename Vec<VT, R>::I;
     using CW = typename std::conditional<D16, typename Vec<VT, R>::I16, IV>::type;  // index word
     using CT = typename std::conditional<D16, short, int>::type;
     constexpr int H = 32 * R;
-    const long long base = a.slice_ptr[s];
-    // the slice's longest row: every lane walks this many steps (uniform across the warp)
-    const int wmax = static_cast<int>((a.slice_ptr[s + 1] - base) / H);
+    // base: the slice's first stored word; wmax: its longest row, every lane walks this many
+    // steps (uniform across the warp)
     const int q0 = s * H + lane * R;
     const IV lv = *reinterpret_cast<const IV *>(a.pos_len + q0);
     int len[R], row[R];
@@ -348,18 +348,27 @@ __global__ void __launch_bounds__(256, MinCtas<R, U>::value) k_spmv(const SellAr
     // After a recorded device error, with the gate closed, or once the solver's status is
     // terminal, the launch returns at once (uniform across the grid). The three words were
     // written by earlier launches: read together (one memory latency, not three), through L2.
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int gw = blockIdx.x * nw + warp;
+    // this warp's units, balanced at plan time (fixed order: reductions are reproducible); read
+    // with the skip words, on which they do not depend
+    const int ub = __ldg(a.warp_ptr + gw), ue = __ldg(a.warp_ptr + gw + 1);
     const int err = __ldcg(a.err), gate = a.gate ? __ldcg(a.gate) : 1, stop = a.stop ? __ldcg(a.stop) : 0;
     if (err != DEV_OK || gate == 0 || stop != 0) return;
     __shared__ double red[32];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int gw = blockIdx.x * nw + warp;
     double d0 = 0.0, d1 = 0.0, d2 = 0.0;
-    // this warp's units, balanced at plan time (fixed order: reductions are reproducible)
-    const int ub = a.warp_ptr[gw], ue = a.warp_ptr[gw + 1];
     for (int i = ub; i < ue; ++i) {
-        const int u = __ldg(a.warp_units + i);
-        if (u < a.n_slices) do_slice<VT, R, U, EP, D16>(a, u, lane, d0, d1, d2);
-        else do_chunk<VT, EP>(a, u - a.n_slices, lane);
+        const int4 rec = __ldg(a.unit_rec + i);
+        // the next record is pulled into L1 while this unit runs (no registers held for it)
+        if (i + 1 < ue) asm volatile("prefetch.global.L1 [%0];" ::"l"(a.unit_rec + i + 1));
+        const int u = rec.x;
+        if (u < a.n_slices) {
+            const long long base = static_cast<long long>(static_cast<unsigned>(rec.z)) |
+                                   (static_cast<long long>(rec.w) << 32);
+            do_slice<VT, R, U, EP, D16>(a, u, base, rec.y, lane, d0, d1, d2);
+        } else {
+            do_chunk<VT, EP>(a, u - a.n_slices, lane);
+        }
     }
     if (EP == EP_DOT3) {
         // records of 4: (d0, d1, d2, 0); each warp's transposed butterfly leaves quantity q in
@@ -531,6 +540,21 @@ hhp_status build_plan_dev(hhp_mat *A, PlanDev &p) {
     assign_units(h, p.ctas * p.warps_per_cta, wptr, wunits, &p.imbalance);
     HHP_TRY(upload(&p.warp_ptr, wptr));
     HHP_TRY(upload(&p.warp_units, wunits));
+    {
+        std::vector<int4> rec(wunits.size());
+        for (size_t i = 0; i < wunits.size(); ++i) {
+            const int u = wunits[i];
+            if (u < h.n_slices) {
+                const long long b = h.slice_ptr[static_cast<size_t>(u)];
+                const int steps = static_cast<int>((h.slice_ptr[static_cast<size_t>(u) + 1] - b) / h.H);
+                rec[i] = make_int4(u, steps, static_cast<int>(static_cast<unsigned>(b & 0xffffffffLL)),
+                                   static_cast<int>(b >> 32));
+            } else {
+                rec[i] = make_int4(u, 0, 0, 0);
+            }
+        }
+        HHP_TRY(upload(&p.unit_rec, rec));
+    }
     HHP_TRY(upload(&p.slice_ptr, h.slice_ptr));
     HHP_TRY(upload(&p.pos_row, h.pos_row, 4));
     HHP_TRY(upload(&p.pos_len, h.pos_len, 4));
@@ -584,6 +608,7 @@ SellArgs<VT> make_args(hhp_mat *A, const PlanDev &p, const VT *csr_val, const VT
     a.pos_len = p.pos_len;
     a.warp_ptr = p.warp_ptr;
     a.warp_units = p.warp_units;
+    a.unit_rec = p.unit_rec;
     a.sval = static_cast<const VT *>(p.sval);
     a.scol = p.scol;
     a.scol16 = p.scol16;
@@ -622,6 +647,7 @@ void PlanDev::release() {
     cudaFree(pos_len);
     cudaFree(warp_ptr);
     cudaFree(warp_units);
+    cudaFree(unit_rec);
     cudaFree(sval);
     cudaFree(scol);
     cudaFree(scol16);
