@@ -106,6 +106,24 @@ def cpu_reference_time(s, nthreads, k_ref):
     return time.perf_counter() - t0, rr
 
 
+def host_cpu() -> dict:
+    """The host the CPU baseline ran on: logical CPUs and the processor model (or architecture)."""
+    import platform
+    model = ""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                key = line.split(":")[0].strip().lower()
+                if key in ("model name", "cpu part", "hardware") and ":" in line:
+                    model = line.split(":", 1)[1].strip()
+                    if key == "model name":
+                        break
+    except OSError:
+        pass
+    return {"nproc": os.cpu_count() or 1, "cpu": model or platform.processor() or platform.machine(),
+            "arch": platform.machine()}
+
+
 def cpu_baseline(s, budget_s=20.0):
     """Reference iteration count to 1e-10 (serial reference loop with a true-residual check per
     iteration), then the multi-threaded reference form timed at that count, and a serial sample."""
@@ -125,7 +143,8 @@ def cpu_baseline(s, budget_s=20.0):
                       f"({k_ref}, found by a serial run with per-iteration true residual in {t_find:.1f} s); "
                       f"relres {rr:.2e}",
             "iters_ref": k_ref, "relres_ref": rr_ref,
-            "serial_1core_s": t_ser, "serial_sample": f"{k_ser} iterations of bicgstab_cpu.c's loop, scaled to {k_ref}"}
+            "serial_1core_s": t_ser, "serial_sample": f"{k_ser} iterations of bicgstab_cpu.c's loop, scaled to {k_ref}",
+            "host": host_cpu()}
 
 
 def run_reference_arm(args, rk):
@@ -150,7 +169,8 @@ def run_reference_arm(args, rk):
             "iters": k_ref, "rel_res_true": rr,
             "cpu_baseline": {"value": v, "unit": "s", "cores": nthreads, "kind": "port",
                              "sample": f"full solve per step: the reference's BiCGStab loop in its MPI-rank form "
-                                       f"(ranks as {nthreads} threads) for its own iteration count to 1e-10 ({k_ref})"},
+                                       f"(ranks as {nthreads} threads) for its own iteration count to 1e-10 ({k_ref})",
+                             "host": host_cpu()},
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
