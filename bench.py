@@ -137,7 +137,20 @@ def cpu_baseline(s, budget_s=20.0):
     t0 = time.perf_counter()
     orc.bicgstab_fixed(s.rowptr, s.col, s.val, s.b, s.x0, k_ser)
     t_ser = (time.perf_counter() - t0) / k_ser * max(k_ref, 1)
-    return {"value": t_mt, "unit": "s", "cores": nthreads, "kind": "port",
+    # the reference's SpMV benchmarks on the host: spmv-cpu (CSR_spmxv_seq, one core) and
+    # spmv-cpu-mt (CSR_spmxv_omp, every core), best of 3 after one warm-up
+    xs = np.random.default_rng(0).standard_normal(s.n)
+    spmv_t = {}
+    for key, fn in (("spmv_1core_ms", lambda: orc.spmv(s.rowptr, s.col, s.val, xs)),
+                    ("spmv_mt_ms", lambda: orc.spmv_omp(s.rowptr, s.col, s.val, xs, nthreads))):
+        fn()
+        best = float("inf")
+        for _ in range(3):
+            t0 = time.perf_counter()
+            fn()
+            best = min(best, time.perf_counter() - t0)
+        spmv_t[key] = best * 1e3
+    return {"value": t_mt, "unit": "s", "cores": nthreads, "kind": "port", **spmv_t,
             "sample": f"full solve of the same system: reference BiCGStab loop (bicgstab_mpi.c decomposition, "
                       f"{nthreads} threads as ranks) run for the reference's own iteration count to 1e-10 "
                       f"({k_ref}, found by a serial run with per-iteration true residual in {t_find:.1f} s); "
