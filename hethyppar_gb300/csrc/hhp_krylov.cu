@@ -49,6 +49,7 @@ struct DevScal {
                           // double-buffered by iteration parity (read one, write the other)
     int iter, iter_start, status, bodies, outer_conv, ru_flag, updates;
     int arrivals;         // K_XRP blocks that have read the status this launch (0 between launches)
+    int stalls;           // mixed form: consecutive FP64 updates that did not lower ||b - A x||
 };
 constexpr size_t kCtlBytes = offsetof(DevScal, rho_prev);
 
@@ -812,6 +813,7 @@ __global__ void __launch_bounds__(512) k_mix_init(DevScal *sc, const double *Yd,
         sc->omega = 1.0;
         sc->bodies = 0;
         sc->rr_max[0] = sc->rr_max[1] = rd2;
+        sc->stalls = 0;
         sc->true_rr = rd2;
         sc->rr_last = rd2;
         sc->ru_flag = 0;
@@ -822,6 +824,10 @@ __global__ void __launch_bounds__(512) k_mix_init(DevScal *sc, const double *Yd,
 // Growth of the FP32 recursive ||r||^2 over the last true ||b - A x||^2 taken as divergence
 // (a factor 1e5 in the norm: BiCGStab's residual peaks stay far below it when it converges).
 constexpr double kDivergence2 = 1e10;
+// Mixed form, stagnation: an FP64 update whose true ||b - A x||^2 is above kStall2 times the last
+// one's (the norm fell by less than 10%), kStallUpdates times in a row.
+constexpr double kStall2 = 0.81;
+constexpr int kStallUpdates = 3;
 
 // Mixed form, after K_XR: the reliable-update test fused with K_P. The FP32 residual triggers an
 // FP64 update when it has dropped by delta since the last one (or looks converged, or the budget
@@ -1114,9 +1120,15 @@ __global__ void __launch_bounds__(512) k_ru_apply(DevScal *sc, const double *Rd,
         const int it = sc->iter;
         sc->rr_max[(it + 1) & 1] = rd2;
         sc->updates = sc->updates + 1;
+        // stagnation: the FP32 recurrences keep reaching their reduction while the true residual
+        // no longer falls (by 10% per update, kStallUpdates updates in a row): they have hit what
+        // FP32 can resolve for this system, and the pass ends as a breakdown (x holds every folded
+        // increment) so that the host restarts it, then hands the solve to FP64
+        const int stalls = rd2 > kStall2 * sc->true_rr ? sc->stalls + 1 : 0;
+        sc->stalls = stalls;
         sc->true_rr = rd2;
         if (rd2 <= sc->thr2) sc->status = ST_CONVERGED;
-        else if (!isfinite(rd2)) sc->status = ST_BREAKDOWN;
+        else if (!isfinite(rd2) || stalls >= kStallUpdates) sc->status = ST_BREAKDOWN;
         else if (it >= sc->maxit) sc->status = ST_MAXIT;
     }
 }
