@@ -11,7 +11,13 @@
 // threshold = rtol ||r0||, stop after the s-step if ||s|| < threshold (x += alpha p only), or
 // after a full step if ||r|| < threshold.
 //
-// One iteration = 5 kernels, 3 reduction points:
+// The merged schedule (the default for solves) runs one iteration as 4 kernels, 2 reduction points:
+//   SpMV   v = A p, epilogue r0.v
+//   K_S    alpha = rho/(r0.v), s = r - alpha v, epilogue (s.s, r0.s)
+//   SpMV   t = A s, epilogue (t.s, t.t, r0.t)
+//   K_XRP  omega, x and r updates, the stop tests on ||r||^2 = s.s - omega t.s, beta from
+//          r0.r = r0.s - omega r0.t, p = r + beta (p - omega v)
+// The classic schedule (the reference's dot products; fixed-iteration runs and adjoints) runs 5:
 //   K_P    reduces (r.r0, r.r) of the previous step, tests convergence, forms beta, updates p
 //   SpMV   v = A p, epilogue r0.v
 //   K_S    alpha = rho/(r0.v), s = r - alpha v, epilogue s.s
@@ -20,7 +26,7 @@
 // Reductions: each producer writes one partial per block; each consumer block re-reduces all
 // partials in a fixed order (so every block gets the same scalar, bit for bit, and runs are
 // reproducible). No host synchronisation inside the loop: kernels read the scalars from device
-// memory and the K_P kernel ends the WHILE loop with cudaGraphSetConditional.
+// memory and the kernel with the stop tests ends the WHILE loop with cudaGraphSetConditional.
 #include <algorithm>
 #include <cmath>
 #include <cstddef>

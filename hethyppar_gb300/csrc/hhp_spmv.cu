@@ -5,7 +5,8 @@
 //
 // Design (GB300):
 //  * Layout: the CSR handed to the library is re-laid out once on the device into slices of
-//    H = 32*RPL rows (RPL = 2 rows per lane for FP64, 4 for FP32). Within a slice the j-th
+//    H = 32*RPL rows (RPL rows per lane, chosen per matrix: 1-2 for FP64, 2-4 for FP32; column
+//    indices as 16-bit offsets from the row where they fit, else int32). Within a slice the j-th
 //    nonzero of every row sits next to the j-th nonzero of its slice-mates, so at each step a
 //    lane loads the values / column indices of its RPL rows with ONE 128-bit load and the warp's
 //    load is one contiguous 512-byte request: the value and index streams are read from HBM
@@ -22,7 +23,9 @@
 //    fixed butterfly); chunk sums are combined in chunk order by the warp finishing a row's last
 //    chunk. Work units (slices and chunks) are dealt to warps at plan time, longest first to the
 //    least-loaded warp, so power-law matrices stay balanced; every warp walks a fixed list, so
-//    every reduction has a fixed order and results are reproducible run to run.
+//    every reduction has a fixed order and results are reproducible run to run. Each list entry
+//    carries its slice's start and length, so a slice's streams are requested one dependent load
+//    after the warp reads the entry.
 //  * Epilogues fuse the BiCGStab dot products (r0.v, t.s, t.t, and r0.t for the merged loop) and
 //    the residual r = b - A x into the store of y; one partial per CTA, summed in a fixed order by
 //    the consumer.
