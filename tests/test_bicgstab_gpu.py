@@ -279,3 +279,42 @@ def test_zero_start_shortcut_agrees_with_general_start(ctx):
         assert math.sqrt(orc.dot(res, res) / orc.dot(s.b, s.b)) <= 1.0000001e-10
     assert np.max(np.abs(x_g - x_z)) <= 1e-6 * np.max(np.abs(x_z))
     A.close()
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_random_systems_all_schedules(ctx, seed):
+    """Seeded random diagonally dominant systems of assorted sizes and row-length spreads (some
+    rows long enough to be chunked, some with only the diagonal): every schedule and precision
+    reaches the tolerance, with the oracle's independent residual, and the FP64 schedules stay
+    within the reference's iteration bar."""
+    rng = np.random.default_rng(100 + seed)
+    m = int(rng.integers(1, 6000))
+    lens = np.minimum(rng.zipf(1.8, size=m) - 1, m - 1)
+    if m > 300:
+        lens[rng.choice(m, size=2, replace=False)] = min(m - 1, 600)
+    rows, cols = [], []
+    for i in range(m):
+        c = rng.choice(m - 1, size=int(lens[i]), replace=False) if lens[i] else np.array([], np.int64)
+        c = c + (c >= i)  # never the diagonal
+        rows.append(np.full(c.size + 1, i))
+        cols.append(np.concatenate([c, [i]]))
+    rows, cols = np.concatenate(rows), np.concatenate(cols)
+    order = np.lexsort((cols, rows))
+    rows, cols = rows[order], cols[order]
+    val = rng.standard_normal(rows.size) / np.maximum(lens[rows], 1)
+    diag = rows == cols
+    val[diag] = 2.0 + rng.random(int(diag.sum()))
+    rp = np.concatenate([[0], np.cumsum(np.bincount(rows, minlength=m))]).astype(np.int32)
+    col = cols.astype(np.int32)
+    xt = rng.standard_normal(m)
+    b = orc.spmv(rp, col, val, xt)
+    k_ref, _, _ = orc.iters_to_tol(rp, col, val, b, np.zeros(m), 1e-10, 500)
+    A = Matrix.from_csr(ctx, rp, col, val)
+    for loop, prec in (("merged", "fp64"), ("classic", "fp64"), ("merged", "mixed")):
+        x, r = bicgstab(ctx, A, b, None, rtol=1e-10, maxit=1000, loop=loop, precision=prec)
+        assert r.status == 0, (loop, prec, r)
+        res = b - orc.spmv(rp, col, val, x)
+        assert math.sqrt(orc.dot(res, res) / orc.dot(b, b)) <= 1.0000001e-10, (loop, prec)
+        if prec == "fp64" and k_ref > 0:
+            assert _within_5pct(r.iters, k_ref) or r.iters <= k_ref + 2, (loop, r.iters, k_ref)
+    A.close()
