@@ -1,4 +1,4 @@
-// hhp_api.cpp -- the C ABI (include/hhp_gpu.h): errors, contexts, matrices, host-buffer wrappers.
+// hhp_api.cu -- the C ABI (include/hhp_gpu.h): errors, contexts, matrices, host-buffer wrappers.
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
@@ -35,7 +35,8 @@ int env_int(const char *name, int dflt) {
     if (!v || !*v) return dflt;
     char *end = nullptr;
     const long x = std::strtol(v, &end, 10);
-    return (end && *end == '\0') ? static_cast<int>(x) : dflt;
+    if (!end || *end != '\0') return dflt;
+    return static_cast<int>(std::min<long>(std::max<long>(x, -(1L << 30)), 1L << 30));
 }
 
 const Tuning &tuning() {
@@ -52,6 +53,21 @@ const Tuning &tuning() {
         d.rpl64 = env_int("HHP_SPMV_RPL64", d.rpl64);
         d.rpl32 = env_int("HHP_SPMV_RPL32", d.rpl32);
         d.d16 = env_int("HHP_SPMV_D16", d.d16);
+        // out-of-range overrides fall back to the defaults' valid ranges (a zero window or chunk
+        // cap would never advance the plan builder's loops)
+        const Tuning def;
+        auto clamp = [](int v, int lo, int hi) { return std::min(std::max(v, lo), hi); };
+        d.cap = clamp(d.cap, 32, 1 << 24);
+        d.long_thr = clamp(d.long_thr, 1, 1 << 24);
+        d.window = clamp(d.window, 1, 1 << 30);
+        d.wpc = clamp(d.wpc, 1, 8);
+        d.ctas_per_sm = clamp(d.ctas_per_sm, 0, 32);
+        d.vec_blocks_per_sm = clamp(d.vec_blocks_per_sm, 1, 32);
+        d.unroll_iters = clamp(d.unroll_iters, 1, 16);
+        if (d.spmv_unroll != 0 && d.spmv_unroll != 2 && d.spmv_unroll != 4) d.spmv_unroll = def.spmv_unroll;
+        if (d.rpl64 != 0 && d.rpl64 != 1 && d.rpl64 != 2) d.rpl64 = def.rpl64;
+        if (d.rpl32 != 2 && d.rpl32 != 4) d.rpl32 = def.rpl32;
+        d.d16 = d.d16 != 0 ? 1 : 0;
         return d;
     }();
     return t;

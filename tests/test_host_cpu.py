@@ -4,6 +4,7 @@ argument handling."""
 import os
 import re
 import subprocess
+import sys
 import tempfile
 
 import numpy as np
@@ -260,6 +261,28 @@ def test_work_plan_layout_choices():
     rp = synth.powerlaw(200000, seed=6).rowptr
     st = hhp.plan_stats(rp, 2, 2048)
     assert st["long_rows"] > 0 and st["chunks"] >= st["long_rows"] and st["sorted"] and st["padding"] < 1.5
+
+
+def test_tuning_overrides_out_of_range_are_clamped():
+    # a zero sort window or long-row threshold from the environment must not stall the plan
+    # builder: the library clamps every override to its valid range
+    code = ("import numpy as np, hethyppar_gb300 as h\n"
+            "from hethyppar_gb300 import synth\n"
+            "rp = synth.powerlaw(5000, max_len=3000, n_dense=2, dense_lo=1000, dense_hi=2000, seed=1).rowptr\n"
+            "st = h.plan_stats(rp, 2, 2048)\n"
+            "rows, ch = h.plan_dump(rp, 2, 2048)\n"
+            "placed = np.zeros(rp.size - 1, np.int64)\n"
+            "np.add.at(placed, rows[rows >= 0], 1)\n"
+            "np.add.at(placed, np.unique(ch[:, 0]) if ch.size else np.zeros(0, np.int64), 1)\n"
+            "assert np.all(placed == 1)\n"
+            "print(st['long_rows'], st['slices'])\n")
+    env = dict(os.environ, HHP_SPMV_WINDOW="0", HHP_SPMV_LONG="-5", HHP_SPMV_CHUNK="0", HHP_SPMV_WPC="99",
+               HHP_SPMV_RPL32="3", HHP_UNROLL_ITERS="99999999999")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, env=env, stdout=subprocess.PIPE,
+                       stderr=subprocess.PIPE, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr[-2000:]
+    long_rows, slices = map(int, r.stdout.split())
+    assert long_rows > 0 and slices >= 0  # threshold clamped to 1: every row with 2+ entries is long
 
 
 def test_cli_rejects_missing_arguments():
