@@ -154,6 +154,14 @@ void assign_units(const SellHost &P, int n_warps, std::vector<int> &warp_ptr, st
     }
 }
 
+namespace {
+bool rows_ascending(int m, const int *rowptr) {
+    for (int i = 0; i < m; ++i)
+        if (rowptr[i + 1] < rowptr[i]) return false;
+    return true;
+}
+}  // namespace
+
 }  // namespace hhp
 
 extern "C" hhp_status hhp_plan_stats(int m, int nnz, const int *rowptr, int rows_per_lane, int cap, int *n_slices,
@@ -163,8 +171,8 @@ extern "C" hhp_status hhp_plan_stats(int m, int nnz, const int *rowptr, int rows
         hhp::set_error("hhp_plan_stats: invalid arguments");
         return HHP_ERR_ARG;
     }
-    if (rowptr[0] != 0 || rowptr[m] != nnz) {
-        hhp::set_error("hhp_plan_stats: rowptr[0] must be 0 and rowptr[m] must equal nnz");
+    if (rowptr[0] != 0 || rowptr[m] != nnz || !hhp::rows_ascending(m, rowptr)) {
+        hhp::set_error("hhp_plan_stats: rowptr must rise from 0 to nnz");
         return HHP_ERR_ARG;
     }
     hhp::SellHost P;
@@ -185,8 +193,8 @@ extern "C" hhp_status hhp_plan_dump(int m, int nnz, const int *rowptr, int rows_
         hhp::set_error("hhp_plan_dump: invalid arguments");
         return HHP_ERR_ARG;
     }
-    if (rowptr[0] != 0 || rowptr[m] != nnz) {
-        hhp::set_error("hhp_plan_dump: rowptr[0] must be 0 and rowptr[m] must equal nnz");
+    if (rowptr[0] != 0 || rowptr[m] != nnz || !hhp::rows_ascending(m, rowptr)) {
+        hhp::set_error("hhp_plan_dump: rowptr must rise from 0 to nnz");
         return HHP_ERR_ARG;
     }
     hhp::SellHost P;
