@@ -21,6 +21,10 @@
  *   --reorder rcm     reverse Cuthill-McKee row/column order (instead of a --perm file)
  *   --loop L          auto (default: merged) | merged (4 kernels per iteration) | classic (the
  *                     reference's dot products; --fixed always runs it)
+ *
+ * Environment: HHP_PROFILE=1 adds "profile_* : seconds" lines (context, matrix to device,
+ * vectors, reorder, the solve call and its device time, and a second, warm solve that
+ * separates one-time setup from the steady state).
  */
 #include <argp.h>
 #include <math.h>
@@ -169,6 +173,12 @@ int main(int argc, char **argv) {
     if (a.n_iters < 0) FAIL("-n must be >= 0");
     if (a.rcm && a.perm) FAIL("--reorder rcm and --perm are exclusive");
 
+    /* HHP_PROFILE (set, not "0"): phase times as extra "profile_* : value" lines, and a second,
+     * warm solve from the same start that separates one-time setup (slice layout, graph capture)
+     * from the steady state; the reference's switch of the same name fences its GPU loop into
+     * dot / SpMV / vector buckets (src/entry/bicgstab_gpu.c:92-101) */
+    const char *prof_env = getenv("HHP_PROFILE");
+    const int prof = prof_env && *prof_env && strcmp(prof_env, "0") != 0;
     const double t_begin = now_s();
     hhp_ctx *ctx = NULL;
     CHECK(hhp_ctx_create(a.device, &ctx));
@@ -176,6 +186,7 @@ int main(int argc, char **argv) {
     const double t_read0 = now_s();
     hhp_mat *A = NULL;
     CHECK(hhp_mat_from_mtx(ctx, a.input_matrix, &A));
+    const double t_mat = now_s();
     int m = 0, n = 0, nnz = 0;
     CHECK(hhp_mat_shape(A, &m, &n, &nnz));
     printf("Matrix name : %s\n", a.input_matrix);
@@ -196,6 +207,7 @@ int main(int argc, char **argv) {
         XT = malloc(sizeof(double) * (size_t)n);
         CHECK(hhp_vector_read(a.x_target, n, XT));
     }
+    const double t_vec = now_s();
     if (a.perm || a.rcm) {
         perm = malloc(sizeof(int) * (size_t)m);
         if (a.perm && read_part(a.perm, m, perm) != 0)
@@ -234,9 +246,29 @@ int main(int argc, char **argv) {
     o.cb = a.print_every > 0 ? print_iter : NULL;
     hhp_solve_info info;
     memset(&info, 0, sizeof info);
+    double *X0 = NULL;
+    if (prof) {
+        X0 = malloc(sizeof(double) * (size_t)n);
+        memcpy(X0, X, sizeof(double) * (size_t)n);
+    }
+    const double t_solve0 = now_s();
     hhp_status st = hhp_bicgstab(ctx, A, B, X, XT, &o, &info);
+    const double t_solve1 = now_s();
     if (st != HHP_OK && st != HHP_ERR_MAXIT)
         FAIL("hhp_bicgstab: %s (%s)", hhp_status_str(st), hhp_last_error());
+    double t_warm = 0.0, t_warm_dev = 0.0;
+    if (prof) {
+        hhp_solve_info info2;
+        memset(&info2, 0, sizeof info2);
+        o.cb = NULL;
+        o.print_every = 0;
+        const double t0 = now_s();
+        const hhp_status st2 = hhp_bicgstab(ctx, A, B, X0, XT, &o, &info2);
+        t_warm = now_s() - t0;
+        t_warm_dev = info2.t_solve_s;
+        if (st2 != st || info2.iters != info.iters) FAIL("HHP_PROFILE: the warm solve differs from the first");
+        free(X0);
+    }
 
     if (perm) {
         double *tmp = malloc(sizeof(double) * (size_t)m);
@@ -253,6 +285,18 @@ int main(int argc, char **argv) {
     printf("outer_iters : %d\n", info.outer_iters);
     printf("precision : %s\n", a.mixed ? (info.fp64_fallback ? "mixed (finished in fp64)" : "mixed") : "fp64");
     printf("status : %s\n", hhp_status_str(st));
+    if (prof) {
+        printf("profile_ctx_create : %lf\n", t_read0 - t_begin);
+        printf("profile_matrix_to_device : %lf\n", t_mat - t_read0);
+        printf("profile_vectors_read : %lf\n", t_vec - t_mat);
+        printf("profile_reorder : %lf\n", t_read1 - t_vec);
+        printf("profile_solve_call : %lf\n", t_solve1 - t_solve0);
+        printf("profile_solve_device : %lf\n", info.t_solve_s);
+        printf("profile_solve_call_warm : %lf\n", t_warm);
+        printf("profile_solve_device_warm : %lf\n", t_warm_dev);
+        printf("profile_setup_once : %lf\n", (t_solve1 - t_solve0) - t_warm);
+        printf("profile_us_per_iter : %lf\n", info.iters > 0 ? 1e6 * t_warm_dev / info.iters : 0.0);
+    }
     printf("everything_total : %lf\n", now_s() - t_begin);
     printf("\n----------------------------------------------------------------------\n");
     CHECK(hhp_vector_write(a.output_x, n, X, a.exact));

@@ -49,6 +49,29 @@ def test_cli_solves_sample_to_tolerance():
         assert np.max(np.abs(x - np.arange(1, 17))) < 1e-8
 
 
+def test_cli_profile_phases():
+    g = load_golden("sample320")
+    with tempfile.TemporaryDirectory() as td:
+        p = _files(td, g)
+        out = os.path.join(td, "X.txt")
+        args = ["-m", p["A"], "-x", p["x0"], "-y", p["b"], "-o", out, "-n", "500", "--out-format", "exact"]
+        plain, _ = _run(args)
+        assert not any(k.startswith("profile_") for k in plain)
+        x_plain = open(out).read()
+        r = subprocess.run([EXE] + args, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True,
+                           env=dict(os.environ, HHP_PROFILE="1"))
+        assert r.returncode == 0, r.stderr
+        kv = dict(re.findall(r"^(\w+)\s*:\s*(\S+)", r.stdout, re.M))
+        keys = ("ctx_create", "matrix_to_device", "vectors_read", "reorder", "solve_call", "solve_device",
+                "solve_call_warm", "solve_device_warm", "setup_once", "us_per_iter")
+        v = {k: float(kv["profile_" + k]) for k in keys}
+        assert all(val >= 0 for key, val in v.items() if key != "setup_once")
+        assert 0 < v["solve_device"] <= v["solve_call"] and 0 < v["solve_device_warm"] <= v["solve_call_warm"]
+        assert v["us_per_iter"] > 0
+        # the same answer and the same keys as without the switch
+        assert kv["n_iters"] == plain["n_iters"] and open(out).read() == x_plain
+
+
 def test_cli_fixed_iterations_like_reference():
     g = load_golden("sample16")
     with tempfile.TemporaryDirectory() as td:
