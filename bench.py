@@ -54,21 +54,98 @@ def peaks():
 
 
 class Clocks:
-    """nvidia-smi sampled every 200 ms while the timed region runs."""
+    """SM clock, power and clock-event reasons while the timed region runs, read through NVML
+    (libnvidia-ml, every 2 ms from a sampling thread: the timed region is tens of milliseconds) or,
+    where NVML cannot be loaded, from nvidia-smi every 200 ms. Read-only queries."""
     Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
+    # clock-event reason bits of nvmlDeviceGetCurrentClocksEventReasons (nvml.h)
+    BITS = {"hw_slowdown": 0x8, "hw_thermal_slowdown": 0x40, "sw_thermal_slowdown": 0x20, "sw_power_cap": 0x4}
 
     def __init__(self, index: int):
-        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+        self.rows = []
+        self.nvml = self._start_nvml(index)
+        if self.nvml is None:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            try:
+                self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), f"--query-gpu={self.Q}",
+                                           "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                          stderr=subprocess.DEVNULL)
+            except OSError:
+                self.p = None
+
+    def _start_nvml(self, index):
+        import ctypes
+        import threading
         try:
-            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), f"--query-gpu={self.Q}",
-                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
-                                      stderr=subprocess.DEVNULL)
-        except OSError:
-            self.p = None
+            lib = ctypes.CDLL("libnvidia-ml.so.1")
+            get_clock, get_reasons = lib.nvmlDeviceGetClockInfo, lib.nvmlDeviceGetCurrentClocksEventReasons
+            get_power = lib.nvmlDeviceGetPowerUsage
+            if lib.nvmlInit_v2() != 0:
+                return None
+            h = self._nvml_handle(lib, index)
+            if h is None:
+                return None
+            mx = ctypes.c_uint(0)
+            lib.nvmlDeviceGetMaxClockInfo(h, ctypes.c_int(1), ctypes.byref(mx))  # NVML_CLOCK_SM
+        except (OSError, AttributeError):
+            return None
+        self.sm_max = float(mx.value)
+        self.stop_evt = threading.Event()
+        first = threading.Event()
+
+        def run():
+            mhz, mask, mw = ctypes.c_uint(0), ctypes.c_ulonglong(0), ctypes.c_uint(0)
+            while not self.stop_evt.is_set():
+                ok = get_clock(h, ctypes.c_int(1), ctypes.byref(mhz)) == 0
+                ok = ok and get_reasons(h, ctypes.byref(mask)) == 0
+                if get_power(h, ctypes.byref(mw)) != 0:
+                    mw.value = 0
+                if ok:
+                    self.rows.append((float(mhz.value), int(mask.value), mw.value / 1000.0))
+                first.set()
+                time.sleep(0.002)
+        self.thread = threading.Thread(target=run, daemon=True)
+        self.thread.start()
+        first.wait(timeout=2.0)  # the first sample is taken before the timed region starts
+        return lib
+
+    @staticmethod
+    def _nvml_handle(lib, index):
+        """The NVML device whose UUID is the CUDA device's (NVML numbers every GPU of the host,
+        CUDA only the visible ones); by index when the UUIDs cannot be compared."""
+        import ctypes
+        h = ctypes.c_void_p()
+        try:
+            import torch
+            want = str(torch.cuda.get_device_properties(index).uuid).lower()
+        except Exception:
+            want = None
+        n = ctypes.c_uint(0)
+        if want and lib.nvmlDeviceGetCount_v2(ctypes.byref(n)) == 0:
+            buf = ctypes.create_string_buffer(96)
+            for i in range(n.value):
+                if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(i), ctypes.byref(h)) != 0:
+                    continue
+                if lib.nvmlDeviceGetUUID(h, buf, ctypes.c_uint(96)) == 0 and \
+                        buf.value.decode(errors="replace").lower().endswith(want):
+                    return h
+        if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(index), ctypes.byref(h)) == 0:
+            return h
+        return None
 
     def stop(self):
+        if self.nvml is not None:
+            self.stop_evt.set()
+            self.thread.join(timeout=5)
+            if not self.rows:
+                return {"sm_mhz": None, "sm_max_mhz": self.sm_max, "reasons": ["no samples"], "source": "nvml"}
+            reasons = sorted({k for _, m, _ in self.rows for k, bit in self.BITS.items() if m & bit})
+            return {"sm_mhz": statistics.median(r[0] for r in self.rows), "sm_max_mhz": self.sm_max,
+                    "power_w_max": max(r[2] for r in self.rows), "samples": len(self.rows), "reasons": reasons,
+                    "source": "nvml, every 2 ms"}
         if self.p is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.p.terminate()
@@ -95,7 +172,8 @@ class Clocks:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in rows for i in range(4) if r[4 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(num(r[1]) for r in rows),
-                "power_w_max": max(num(r[2]) for r in rows), "samples": len(rows), "reasons": reasons}
+                "power_w_max": max(num(r[2]) for r in rows), "samples": len(rows), "reasons": reasons,
+                "source": "nvidia-smi, every 200 ms"}
 
 
 def cpu_reference_time(s, nthreads, k_ref):
