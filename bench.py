@@ -66,6 +66,7 @@ class Clocks:
     def __init__(self, index: int):
         self.p = None
         self.rows = []
+        self.t0 = time.perf_counter()
         self.nvml = self._start_nvml(index)
         if self.nvml is None:
             self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
@@ -137,6 +138,7 @@ class Clocks:
         return None
 
     def stop(self):
+        window = time.perf_counter() - self.t0
         if self.nvml is not None:
             self.stop_evt.set()
             self.thread.join(timeout=5)
@@ -145,7 +147,7 @@ class Clocks:
             reasons = sorted({k for _, m, _ in self.rows for k, bit in self.BITS.items() if m & bit})
             return {"sm_mhz": statistics.median(r[0] for r in self.rows), "sm_max_mhz": self.sm_max,
                     "power_w_max": max(r[2] for r in self.rows), "samples": len(self.rows), "reasons": reasons,
-                    "source": "nvml, every 2 ms"}
+                    "window_s": window, "source": "nvml, every 2 ms"}
         if self.p is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.p.terminate()
@@ -173,7 +175,7 @@ class Clocks:
         reasons = sorted({names[i] for r in rows for i in range(4) if r[4 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(num(r[1]) for r in rows),
                 "power_w_max": max(num(r[2]) for r in rows), "samples": len(rows), "reasons": reasons,
-                "source": "nvidia-smi, every 200 ms"}
+                "window_s": window, "source": "nvidia-smi, every 200 ms"}
 
 
 def cpu_reference_time(s, nthreads, k_ref):
