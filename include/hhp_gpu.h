@@ -132,8 +132,9 @@ hhp_status hhp_mat_set_values(hhp_mat *mat, const double *val);
 hhp_status hhp_mat_set_values_dev(hhp_mat *mat, const double *val_dev);
 /* Copy the device CSR back to host arrays (m+1, nnz, nnz; any may be NULL). */
 hhp_status hhp_mat_get_csr(const hhp_mat *mat, int *rowptr, int *col, double *val);
-/* Host CSR of A^T built on the device (count, scan, scatter; within a row of A^T entries are in
- * increasing row order of A, as CSR_to_CSC src/util/hhp_matrix.c:1476-1535). Arrays n+1, nnz, nnz. */
+/* Host CSR of A^T built on the device (a stable radix sort of A's entries by column; within a row
+ * of A^T entries are in increasing row order of A, as CSR_to_CSC src/util/hhp_matrix.c:1476-1535).
+ * Arrays n+1, nnz, nnz. */
 hhp_status hhp_mat_get_transpose(hhp_mat *mat, int *t_rowptr, int *t_col, double *t_val);
 
 /* ---- SpMV: replaces device_csr_spmv (src/util/hhp_cuda.c:226-236): y = alpha*A*x + beta*y ---- */
