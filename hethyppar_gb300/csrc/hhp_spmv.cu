@@ -8,12 +8,13 @@
 //    H = 32*RPL rows (RPL rows per lane, chosen per matrix: 1-2 for FP64, 2-4 for FP32; column
 //    indices as 16-bit offsets from the row where they fit, else int32). Within a slice the j-th
 //    nonzero of every row sits next to the j-th nonzero of its slice-mates, so at each step a
-//    lane loads the values / column indices of its RPL rows with ONE 128-bit load and the warp's
-//    load is one contiguous 512-byte request: the value and index streams are read from HBM
-//    exactly once, fully coalesced, with no shared-memory staging.
-//  * Occupancy instead of staging: with no shared memory in use the kernel runs at full
-//    occupancy; every lane keeps UNROLL steps of loads (values, indices, then x gathers through
-//    the read-only L1/L2 path) in flight. HBM latency is hidden by warps, not by buffers.
+//    lane loads the values / column indices of its RPL rows with one vector load (up to 128
+//    bits) and the warp's load is one contiguous request: the value and index streams are read
+//    from HBM exactly once, fully coalesced, with no shared-memory staging.
+//  * Registers instead of staging: every lane keeps UNROLL steps of loads (values, indices, then
+//    x gathers through the read-only L1/L2 path) in flight, and the register budget that takes
+//    sets the occupancy (3-6 CTAs of 8 warps per SM by instantiation). HBM latency is hidden by
+//    warps, not by buffers (shared-memory rings filled by cp.async or TMA measured slower).
 //  * Arithmetic: each lane sums each of its rows sequentially in CSR order with fused
 //    multiply-adds -- one FP64 FMA per nonzero, the minimum on GB300 whose FP64 rate (~2
 //    FMA/clk/SM) is as much a limit as HBM here -- and the RPL independent chains per lane give
