@@ -9,7 +9,8 @@
 //   '%' comment lines, then "M N nz", then nz triplets "i j v", 1-based;
 //   rows in order, entries of a row in file order, duplicates kept (SpMV sums them).
 // Unlike the reference (fscanf, unchecked), short files and out-of-range indices are errors.
-// Parsing reads the whole file and converts with std::from_chars; large files are parsed by one
+// Parsing maps the whole file (reads it where it cannot be mapped) and converts with
+// std::from_chars; large files are parsed by one
 // thread per core on line-aligned chunks, joined in file order (so the CSR is identical to the
 // serial parse), and any irregularity (a malformed entry, a count mismatch) re-parses serially
 // for the exact error message.

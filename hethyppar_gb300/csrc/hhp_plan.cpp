@@ -5,7 +5,7 @@
 //   len <= long_thr  -> "slice rows": placed in slices of H = 32*RPL rows (RPL rows per lane).
 //                       Inside a slice the j-th nonzero of all H rows are stored next to each
 //                       other (step-major), so at every step a warp loads its lanes' values and
-//                       column indices with one coalesced 128-bit load per lane; each lane sums
+//                       column indices with one coalesced vector load per lane; each lane sums
 //                       its rows sequentially in CSR order (the order of CSR_spmxv_seq,
 //                       src/util/hhp_cpu.c:445-455), one fused multiply-add per nonzero.
 //                       Rows keep their natural order unless that would pad the slices by more
