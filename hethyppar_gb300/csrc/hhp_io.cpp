@@ -10,10 +10,9 @@
 //   rows in order, entries of a row in file order, duplicates kept (SpMV sums them).
 // Unlike the reference (fscanf, unchecked), short files and out-of-range indices are errors.
 // Parsing maps the whole file (reads it where it cannot be mapped) and converts with
-// std::from_chars; large files are parsed by one
-// thread per core on line-aligned chunks, joined in file order (so the CSR is identical to the
-// serial parse), and any irregularity (a malformed entry, a count mismatch) re-parses serially
-// for the exact error message.
+// std::from_chars; large files are parsed by one thread per core on line-aligned chunks, joined
+// in file order (so the CSR is identical to the serial parse), and any irregularity (a malformed
+// entry, a count mismatch) re-parses serially for the exact error message.
 //
 // Binary CSR files ("HHPCSR01" magic, then int64 m, n, nnz, then rowptr[m+1] and col[nnz] as
 // int32 and val[nnz] as FP64, little-endian) skip text parsing altogether: hhp_csr_file_write
