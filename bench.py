@@ -230,6 +230,24 @@ def cpu_baseline(s, budget_s=20.0):
             fn()
             best = min(best, time.perf_counter() - t0)
         spmv_t[key] = best * 1e3
+    # spmv-cpu-mt at 1, 2, 4, ... threads and every core: the best thread count
+    sweep = {}
+    nt = 1
+    while True:
+        fn = (lambda k: (lambda: orc.spmv_omp(s.rowptr, s.col, s.val, xs, k)))(nt)
+        fn()
+        best = float("inf")
+        for _ in range(3):
+            t0 = time.perf_counter()
+            fn()
+            best = min(best, time.perf_counter() - t0)
+        sweep[str(nt)] = best * 1e3
+        if nt >= nthreads:
+            break
+        nt = min(2 * nt, nthreads)
+    best_nt = min(sweep, key=sweep.get)
+    spmv_t["spmv_mt_threads_ms"] = sweep
+    spmv_t["spmv_mt_best"] = {"threads": int(best_nt), "ms": sweep[best_nt]}
     return {"value": t_mt, "unit": "s", "cores": nthreads, "kind": "port", **spmv_t,
             "sample": f"full solve of the same system: reference BiCGStab loop (bicgstab_mpi.c decomposition, "
                       f"{nthreads} threads as ranks) run for the reference's own iteration count to 1e-10 "
