@@ -46,8 +46,10 @@ def test_spmv_golden(ctx, name):
             assert np.all(np.abs(y - g[yk]) <= spmv_tolerance(g["rowptr"], g["col"], g["val"], g[xk]))
 
 
-@pytest.mark.parametrize("cfg", ["c1", "c2"])
+@pytest.mark.parametrize("cfg", ["c1", "c2", "c4", "c5"])
 def test_spmv_full_size_configs(ctx, cfg):
+    # c4 and c5 take the 16-bit-offset layout and the stencil plan (2 rows x 2 steps per lane);
+    # c3 (3.5M-row power law, ~45 s to generate) is covered by the 300k-row power-law case below
     s = synth.config(cfg)
     x = np.random.default_rng(7).standard_normal(s.n)
     _check(ctx, s.rowptr, s.col, s.val, x)
@@ -100,8 +102,9 @@ def test_spmv_alpha_beta(ctx):
     assert np.max(np.abs(y - ref)) <= 1e-13 * np.max(np.abs(ref))
 
 
-def test_spmv_fp32(ctx):
-    s = synth.config("c1")
+@pytest.mark.parametrize("cfg", ["c1", "c4"])
+def test_spmv_fp32(ctx, cfg):
+    s = synth.config(cfg)
     x = np.random.default_rng(2).uniform(-1, 1, s.n)
     A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
     y = torch.empty(s.m, dtype=torch.float32, device="cuda")
