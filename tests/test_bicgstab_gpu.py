@@ -85,6 +85,42 @@ def test_device_and_host_entry_points_agree_and_repeat(ctx):
     assert r_h.iters == r_d.iters and r_d.err_vs_target <= 1e-6
 
 
+def test_contexts_on_concurrent_host_threads(ctx):
+    """One context per host thread: solves running at the same time on separate contexts (each
+    with its own stream, graphs and scratch) give the bits a lone solve gives."""
+    import threading
+    from hethyppar_gb300 import Context
+    systems = [synth.config("c1"), synth.convdiff2d(200, 20.0, seed=11)]
+    expect = []
+    for s in systems:
+        A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
+        expect.append(bicgstab(ctx, A, s.b, s.x0, rtol=1e-10, maxit=3000))
+        A.close()
+    out, errors = [None] * 4, []
+
+    def worker(i):
+        try:
+            s = systems[i % 2]
+            with Context(0) as c:
+                A = Matrix.from_csr(c, s.rowptr, s.col, s.val)
+                res = [bicgstab(c, A, s.b, s.x0, rtol=1e-10, maxit=3000) for _ in range(3)]
+                A.close()
+            out[i] = res
+        except Exception as e:  # reported on the main thread
+            errors.append(repr(e))
+
+    threads = [threading.Thread(target=worker, args=(i,)) for i in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join(timeout=300)
+    assert not errors, errors
+    for i in range(4):
+        x_ref, r_ref = expect[i % 2]
+        for x, r in out[i]:
+            assert r.iters == r_ref.iters and np.array_equal(x, x_ref)
+
+
 def test_history_callback(ctx):
     g = load_golden("convdiff2d_32")
     A = Matrix.from_csr(ctx, g["rowptr"], g["col"], g["val"])
