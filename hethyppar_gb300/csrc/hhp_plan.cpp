@@ -18,10 +18,37 @@
 #include <cmath>
 #include <numeric>
 #include <queue>
+#include <thread>
 
 #include "hhp_internal.h"
 
 namespace hhp {
+
+namespace {
+
+// fn(begin, end) over [0, n) split into contiguous ranges, one per host thread (serial for small
+// n). Every range is processed exactly as the serial loop would process it, so the result does
+// not depend on the thread count.
+template <typename Fn>
+void parallel_ranges(size_t n, size_t min_per_thread, Fn fn) {
+    const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t nt = std::min({hw, size_t{32}, std::max<size_t>(1, n / std::max<size_t>(min_per_thread, 1))});
+    if (nt <= 1) {
+        fn(size_t{0}, n);
+        return;
+    }
+    std::vector<std::thread> pool;
+    pool.reserve(nt - 1);
+    const size_t step = (n + nt - 1) / nt;
+    for (size_t t = 1; t < nt; ++t) {
+        const size_t b = std::min(n, t * step), e = std::min(n, b + step);
+        pool.emplace_back([=, &fn] { fn(b, e); });
+    }
+    fn(size_t{0}, std::min(n, step));
+    for (auto &th : pool) th.join();
+}
+
+}  // namespace
 
 void build_plan(int m, const int *rowptr, int rpl, int long_thr, int cap, int window, SellHost &P) {
     P = SellHost();
@@ -30,13 +57,44 @@ void build_plan(int m, const int *rowptr, int rpl, int long_thr, int cap, int wi
     P.long_thr = long_thr;
     P.cap = cap;
     const int H = P.H;
-    std::vector<int> order;
-    order.reserve(static_cast<size_t>(m));
+    // rows up to long_thr go to slices in row order, longer ones to chunks: counted per range of
+    // rows, then placed at each range's offset
+    const size_t nr = static_cast<size_t>(m), kRange = 1 << 16;
+    const size_t nrange = (nr + kRange - 1) / kRange;
+    std::vector<size_t> n_short(nrange + 1, 0);
+    std::vector<long long> nnz_short(nrange, 0);
+    parallel_ranges(nrange, 4, [&](size_t gb, size_t ge) {
+        for (size_t g = gb; g < ge; ++g) {
+            size_t c = 0;
+            long long z = 0;
+            for (size_t r = g * kRange; r < std::min(nr, (g + 1) * kRange); ++r) {
+                const int len = rowptr[r + 1] - rowptr[r];
+                if (len <= long_thr) {
+                    ++c;
+                    z += len;
+                }
+            }
+            n_short[g + 1] = c;
+            nnz_short[g] = z;
+        }
+    });
     long long short_nnz = 0;
+    for (size_t g = 0; g < nrange; ++g) {
+        n_short[g + 1] += n_short[g];
+        short_nnz += nnz_short[g];
+    }
+    std::vector<int> order(n_short[nrange]);
+    parallel_ranges(nrange, 4, [&](size_t gb, size_t ge) {
+        for (size_t g = gb; g < ge; ++g) {
+            size_t o = n_short[g];
+            for (size_t r = g * kRange; r < std::min(nr, (g + 1) * kRange); ++r)
+                if (rowptr[r + 1] - rowptr[r] <= long_thr) order[o++] = static_cast<int>(r);
+        }
+    });
     int n_chunks = 0;
-    for (int r = 0; r < m; ++r) {
-        const int len = rowptr[r + 1] - rowptr[r];
-        if (len > long_thr) {
+    if (order.size() < nr)
+        for (int r = 0; r < m; ++r) {
+            if (rowptr[r + 1] - rowptr[r] <= long_thr) continue;
             const int l = static_cast<int>(P.long_rows.size());
             P.long_rows.push_back(r);
             P.long_first.push_back(n_chunks);
@@ -46,32 +104,43 @@ void build_plan(int m, const int *rowptr, int rpl, int long_thr, int cap, int wi
                 P.chunk_long.push_back(l);
                 ++n_chunks;
             }
-        } else {
-            order.push_back(r);
-            short_nnz += len;
         }
-    }
     P.long_first.push_back(n_chunks);
+    // slice widths of an order (H rows per slice, the longest row sets the width), in parallel
+    auto widths = [&](const std::vector<int> &ord, std::vector<int> &w) {
+        const size_t ns = (ord.size() + static_cast<size_t>(H) - 1) / static_cast<size_t>(H);
+        w.assign(ns, 0);
+        parallel_ranges(ns, 2048, [&](size_t b, size_t e) {
+            for (size_t s = b; s < e; ++s) {
+                int mx = 0;
+                const size_t q1 = std::min(ord.size(), (s + 1) * static_cast<size_t>(H));
+                for (size_t q = s * static_cast<size_t>(H); q < q1; ++q)
+                    mx = std::max(mx, rowptr[ord[q] + 1] - rowptr[ord[q]]);
+                w[s] = mx;
+            }
+        });
+    };
+    std::vector<int> width;
     auto padded = [&](const std::vector<int> &ord) {
+        widths(ord, width);
         long long tot = 0;
-        for (size_t s0 = 0; s0 < ord.size(); s0 += static_cast<size_t>(H)) {
-            int mx = 0;
-            for (size_t q = s0; q < std::min(ord.size(), s0 + static_cast<size_t>(H)); ++q)
-                mx = std::max(mx, rowptr[ord[q] + 1] - rowptr[ord[q]]);
-            tot += static_cast<long long>(mx) * H;
-        }
+        for (int x : width) tot += static_cast<long long>(x) * H;
         return tot;
     };
     long long tot = padded(order);
     P.sorted = false;
     if (short_nnz > 0 && static_cast<double>(tot) > 1.15 * static_cast<double>(short_nnz)) {
-        for (size_t w0 = 0; w0 < order.size(); w0 += static_cast<size_t>(window)) {
-            const auto b = order.begin() + static_cast<long>(w0);
-            const auto e = order.begin() + static_cast<long>(std::min(order.size(), w0 + static_cast<size_t>(window)));
-            std::stable_sort(b, e, [&](int x, int y) {
-                return (rowptr[x + 1] - rowptr[x]) > (rowptr[y + 1] - rowptr[y]);
-            });
-        }
+        const size_t nwin = (order.size() + static_cast<size_t>(window) - 1) / static_cast<size_t>(window);
+        parallel_ranges(nwin, 4, [&](size_t wb, size_t we) {
+            for (size_t wi = wb; wi < we; ++wi) {
+                const size_t w0 = wi * static_cast<size_t>(window);
+                const auto b = order.begin() + static_cast<long>(w0);
+                const auto e = order.begin() + static_cast<long>(std::min(order.size(), w0 + static_cast<size_t>(window)));
+                std::stable_sort(b, e, [&](int x, int y) {
+                    return (rowptr[x + 1] - rowptr[x]) > (rowptr[y + 1] - rowptr[y]);
+                });
+            }
+        });
         tot = padded(order);
         P.sorted = true;
     }
@@ -79,24 +148,27 @@ void build_plan(int m, const int *rowptr, int rpl, int long_thr, int cap, int wi
     const size_t ms = order.size();
     P.n_slices = static_cast<int>((ms + static_cast<size_t>(H) - 1) / static_cast<size_t>(H));
     const size_t npos = static_cast<size_t>(P.n_slices) * static_cast<size_t>(H);
-    P.pos_row.assign(npos, -1);
-    P.pos_len.assign(npos, 0);
+    P.pos_row.resize(npos);
+    P.pos_len.resize(npos);
     P.slice_ptr.assign(static_cast<size_t>(P.n_slices) + 1, 0);
+    // `width` holds the widths of the final order (padded() ran last on it)
     long long off = 0;
     for (int s = 0; s < P.n_slices; ++s) {
-        int mx = 0;
-        for (int q = 0; q < H; ++q) {
-            const size_t p = static_cast<size_t>(s) * H + static_cast<size_t>(q);
+        P.slice_ptr[static_cast<size_t>(s)] = off;
+        off += static_cast<long long>(width[static_cast<size_t>(s)]) * H;
+    }
+    parallel_ranges(npos, 65536, [&](size_t b, size_t e) {
+        for (size_t p = b; p < e; ++p) {
             if (p < ms) {
                 const int r = order[p];
                 P.pos_row[p] = r;
                 P.pos_len[p] = rowptr[r + 1] - rowptr[r];
-                mx = std::max(mx, P.pos_len[p]);
+            } else {
+                P.pos_row[p] = -1;
+                P.pos_len[p] = 0;
             }
         }
-        P.slice_ptr[static_cast<size_t>(s)] = off;
-        off += static_cast<long long>(mx) * H;
-    }
+    });
     P.slice_ptr[static_cast<size_t>(P.n_slices)] = off;
     P.total = off;
     P.short_nnz = short_nnz;

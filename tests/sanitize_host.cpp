@@ -226,6 +226,14 @@ void work_plan() {
         l[5] = 70000;  // one very long row
         cases.push_back(l);
     }
+    {
+        // large enough for the plan builder's threaded passes (row classification, length-sorted
+        // windows, slice widths and positions)
+        std::vector<int> l(1200000);
+        for (auto &x : l) x = static_cast<int>(rng() % 5 == 0 ? rng() % 300 : 1 + rng() % 6);
+        for (int i = 0; i < 40; ++i) l[static_cast<size_t>(i) * 29989] = 3000 + i;
+        cases.push_back(l);
+    }
     for (const auto &lens : cases) {
         const std::vector<int> rp = rowptr_of(lens);
         const int m = static_cast<int>(lens.size()), nnz = rp.back();
