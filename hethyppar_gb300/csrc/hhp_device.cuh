@@ -10,7 +10,7 @@
 
 namespace hhp {
 
-// Device error codes for the context's error word. No kernel of this build waits on another
+// Device error codes for the context's error word. No kernel of this library waits on another
 // (the long-row combine is a last-arriver atomic count, every other ordering is a kernel
 // boundary), so nothing sets it today; SpMV launches and the solve loop check it, so a future
 // bounded wait that gives up stops every later launch and the solve returns HHP_ERR_TIMEOUT.

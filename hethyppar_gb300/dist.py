@@ -1,6 +1,6 @@
 """Process-group plumbing for running independent replicas of the solve on several GPUs.
 
-The solve does not shard across GPUs in this build (one partition per GPU, no halo exchange):
+The solve does not shard across GPUs in this library (one partition per GPU, no halo exchange):
 N ranks run N independent replicas. The only cross-rank operations are a barrier around the
 timed region and a max over ranks of the measured times (the slowest replica sets the job time).
 """

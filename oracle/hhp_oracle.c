@@ -2,7 +2,7 @@
  * hhp_oracle.c -- CPU oracle for the BiCGStab / CSR-SpMV path (TEST INFRASTRUCTURE ONLY).
  *
  * A plain-C restatement of HetHypPar's CPU path, used by the tests, the smoke check and the
- * benchmark's CPU-baseline leg as the checker. The product never links or calls this file.
+ * benchmark's CPU-baseline leg, to compare against. The product never links or calls this file.
  * Compile with -ffp-contract=off (the build does): every multiply and add then rounds on its
  * own, in the order the reference's loops use, so results match the reference bit for bit on
  * the golden vectors in tests/golden/ (made from the reference's own compiled functions).

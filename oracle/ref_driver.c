@@ -5,7 +5,7 @@
  * hhp_wrap_bora.c, hhp_dp_helpers.c, mmio, bora matrix.c) into oracle/_ref/libhhpref.so by
  * oracle/Makefile. tests/golden/make_golden.py calls these wrappers through ctypes to record the
  * reference's results at full double precision (its executables print only %E and %lf).
- * Every numerical step below is a call into the reference; the driver only marshals arrays.
+ * Every numerical step below is a call into the reference; this file only marshals arrays.
  */
 #include <math.h>
 #include <stdlib.h>
