@@ -102,9 +102,11 @@ def test_spmv_alpha_beta(ctx):
     assert np.max(np.abs(y - ref)) <= 1e-13 * np.max(np.abs(ref))
 
 
-@pytest.mark.parametrize("cfg", ["c1", "c4"])
+@pytest.mark.parametrize("cfg", ["c1", "c4", "powerlaw"])
 def test_spmv_fp32(ctx, cfg):
-    s = synth.config(cfg)
+    # powerlaw: FP32 slices sorted by length plus rows of 20k-60k entries summed in chunks
+    s = (synth.powerlaw(300_000, max_len=60_000, n_dense=5, dense_lo=20_000, dense_hi=60_000, seed=9)
+         if cfg == "powerlaw" else synth.config(cfg))
     x = np.random.default_rng(2).uniform(-1, 1, s.n)
     A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
     y = torch.empty(s.m, dtype=torch.float32, device="cuda")
