@@ -24,6 +24,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -154,6 +155,21 @@ void parse_chunk(const char *p, const char *e, long long M, long long N, EntryCh
 
 // Parallel parse of the entry section [p, e) into CSR; false if the serial path must run (a
 // malformed or out-of-range entry, or a count other than nnz).
+// fn(t) for t in [0, T) on T threads; a share whose thread cannot be created runs on this one.
+template <typename Fn>
+void run_threads(int T, Fn fn) {
+    std::vector<std::thread> th;
+    th.reserve(static_cast<size_t>(T));
+    for (int t = 0; t < T; ++t) {
+        try {
+            th.emplace_back(fn, t);
+        } catch (const std::system_error &) {
+            fn(t);
+        }
+    }
+    for (auto &x : th) x.join();
+}
+
 bool parse_entries_parallel(const char *p, const char *e, long long M, long long N, int nnz, int m,
                             std::vector<int> &rowptr, std::vector<int> &col, std::vector<double> &val) {
     const size_t bytes = static_cast<size_t>(e - p);
@@ -169,12 +185,11 @@ bool parse_entries_parallel(const char *p, const char *e, long long M, long long
         cut[static_cast<size_t>(t)] = nl ? nl + 1 : e;
     }
     std::vector<EntryChunk> ch(static_cast<size_t>(T));
-    std::vector<std::thread> th;
-    for (int t = 0; t < T; ++t)
-        th.emplace_back(parse_chunk, std::max(cut[static_cast<size_t>(t)], cut[0]),
-                        std::max(cut[static_cast<size_t>(t) + 1], cut[static_cast<size_t>(t)]), M, N,
-                        std::ref(ch[static_cast<size_t>(t)]));
-    for (auto &x : th) x.join();
+    run_threads(T, [&](int t) {
+        parse_chunk(std::max(cut[static_cast<size_t>(t)], cut[0]),
+                    std::max(cut[static_cast<size_t>(t) + 1], cut[static_cast<size_t>(t)]), M, N,
+                    ch[static_cast<size_t>(t)]);
+    });
     long long total = 0;
     bool sorted = true;
     int prev_last = -1;
@@ -191,10 +206,8 @@ bool parse_entries_parallel(const char *p, const char *e, long long M, long long
     if (sorted) {
         // row counts: each chunk's rows form a range that meets its neighbours' only at the ends,
         // so the chunks count their own rows in parallel and only boundary rows are merged
-        std::vector<std::thread> cnt;
         std::vector<std::vector<int>> edge(static_cast<size_t>(T));  // {first row, its count, last row, its count}
-        for (int t = 0; t < T; ++t)
-            cnt.emplace_back([&, t] {
+        run_threads(T, [&](int t) {
                 const EntryChunk &c = ch[static_cast<size_t>(t)];
                 if (c.ri.empty()) return;
                 const int first = c.ri.front(), last = c.ri.back();
@@ -206,7 +219,6 @@ bool parse_entries_parallel(const char *p, const char *e, long long M, long long
                 }
                 edge[static_cast<size_t>(t)] = {first, nf, last, nl};
             });
-        for (auto &x : cnt) x.join();
         for (const auto &eg : edge) {
             if (eg.empty()) continue;
             rowptr[static_cast<size_t>(eg[0]) + 1] += eg[1];
@@ -216,15 +228,12 @@ bool parse_entries_parallel(const char *p, const char *e, long long M, long long
         // rows in file order already: the CSR is the chunks' concatenation
         std::vector<size_t> off(static_cast<size_t>(T) + 1, 0);
         for (int t = 0; t < T; ++t) off[static_cast<size_t>(t) + 1] = off[static_cast<size_t>(t)] + ch[static_cast<size_t>(t)].ri.size();
-        std::vector<std::thread> cp;
-        for (int t = 0; t < T; ++t)
-            cp.emplace_back([&, t] {
+        run_threads(T, [&](int t) {
                 const EntryChunk &c = ch[static_cast<size_t>(t)];
                 if (c.ci.empty()) return;
                 std::memcpy(col.data() + off[static_cast<size_t>(t)], c.ci.data(), sizeof(int) * c.ci.size());
                 std::memcpy(val.data() + off[static_cast<size_t>(t)], c.vv.data(), sizeof(double) * c.vv.size());
             });
-        for (auto &x : cp) x.join();
     } else {
         // stable counting sort by row, chunks in file order: entries of a row keep file order
         for (const auto &c : ch)

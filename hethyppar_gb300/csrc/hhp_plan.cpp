@@ -18,6 +18,7 @@
 #include <cmath>
 #include <numeric>
 #include <queue>
+#include <system_error>
 #include <thread>
 
 #include "hhp_internal.h"
@@ -42,7 +43,11 @@ void parallel_ranges(size_t n, size_t min_per_thread, Fn fn) {
     const size_t step = (n + nt - 1) / nt;
     for (size_t t = 1; t < nt; ++t) {
         const size_t b = std::min(n, t * step), e = std::min(n, b + step);
-        pool.emplace_back([=, &fn] { fn(b, e); });
+        try {
+            pool.emplace_back([=, &fn] { fn(b, e); });
+        } catch (const std::system_error &) {
+            fn(b, e);  // no thread to be had: this range runs here
+        }
     }
     fn(size_t{0}, std::min(n, step));
     for (auto &th : pool) th.join();
