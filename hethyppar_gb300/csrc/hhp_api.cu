@@ -168,6 +168,7 @@ const char *hhp_status_str(hhp_status s) {
 const char *hhp_last_error(void) { return g_last_error.c_str(); }
 
 hhp_status hhp_ctx_create(int device, hhp_ctx **out) {
+    HHP_API_BEGIN
     if (!out) {
         set_error("hhp_ctx_create: out is NULL");
         return HHP_ERR_ARG;
@@ -200,6 +201,7 @@ hhp_status hhp_ctx_create(int device, hhp_ctx **out) {
     }
     *out = c;
     return HHP_OK;
+    HHP_API_END
 }
 
 void hhp_ctx_destroy(hhp_ctx *c) {
@@ -225,6 +227,7 @@ long long hhp_ctx_kernel_launches(const hhp_ctx *c) { return c ? c->kernel_launc
 
 hhp_status hhp_mat_from_csr(hhp_ctx *ctx, int m, int n, int nnz, const int *rowptr, const int *col, const double *val,
                             const int *perm, hhp_mat **out) {
+    HHP_API_BEGIN
     if (!ctx || !out || (nnz > 0 && !val)) {
         set_error("hhp_mat_from_csr: null argument");
         return HHP_ERR_ARG;
@@ -273,10 +276,12 @@ hhp_status hhp_mat_from_csr(hhp_ctx *ctx, int m, int n, int nnz, const int *rowp
     }
     *out = A;
     return HHP_OK;
+    HHP_API_END
 }
 
 hhp_status hhp_mat_from_csr_dev(hhp_ctx *ctx, int m, int n, int nnz, const int *rowptr_dev, const int *col_dev,
                                 const double *val_dev, hhp_mat **out) {
+    HHP_API_BEGIN
     if (!ctx || !out || m < 0 || n < 0 || nnz < 0 || !rowptr_dev || (nnz > 0 && (!col_dev || !val_dev))) {
         set_error("hhp_mat_from_csr_dev: invalid arguments");
         return HHP_ERR_ARG;
@@ -318,9 +323,11 @@ hhp_status hhp_mat_from_csr_dev(hhp_ctx *ctx, int m, int n, int nnz, const int *
     }
     *out = A;
     return HHP_OK;
+    HHP_API_END
 }
 
 hhp_status hhp_mat_from_mtx(hhp_ctx *ctx, const char *path, hhp_mat **out) {
+    HHP_API_BEGIN
     if (!ctx || !out) {
         set_error("hhp_mat_from_mtx: null argument");
         return HHP_ERR_ARG;
@@ -330,6 +337,7 @@ hhp_status hhp_mat_from_mtx(hhp_ctx *ctx, const char *path, hhp_mat **out) {
     std::vector<double> val;
     HHP_TRY(read_mtx(path, m, n, nnz, rp, col, val));
     return hhp_mat_from_csr(ctx, m, n, nnz, rp.data(), col.data(), val.data(), nullptr, out);
+    HHP_API_END
 }
 
 void hhp_mat_destroy(hhp_mat *A) {
@@ -374,30 +382,41 @@ hhp_status hhp_mat_set_values(hhp_mat *A, const double *val) { return set_values
 hhp_status hhp_mat_set_values_dev(hhp_mat *A, const double *val) { return set_values(A, val, cudaMemcpyDeviceToDevice); }
 
 hhp_status hhp_mat_get_csr(const hhp_mat *A, int *rowptr, int *col, double *val) {
+    HHP_API_BEGIN
+    HHP_API_BEGIN
+    HHP_API_BEGIN
     if (!A) return HHP_ERR_ARG;
     HHP_CUDA(cudaStreamSynchronize(A->ctx->stream));
     if (rowptr) HHP_CUDA(cudaMemcpy(rowptr, A->rowptr, sizeof(int) * (static_cast<size_t>(A->m) + 1), cudaMemcpyDeviceToHost));
     if (col && A->nnz) HHP_CUDA(cudaMemcpy(col, A->col, sizeof(int) * static_cast<size_t>(A->nnz), cudaMemcpyDeviceToHost));
     if (val && A->nnz) HHP_CUDA(cudaMemcpy(val, A->val, sizeof(double) * static_cast<size_t>(A->nnz), cudaMemcpyDeviceToHost));
     return HHP_OK;
+    HHP_API_END
+    HHP_API_END
+    HHP_API_END
 }
 
 hhp_status hhp_mat_get_transpose(hhp_mat *A, int *t_rowptr, int *t_col, double *t_val) {
+    HHP_API_BEGIN
     if (!A) return HHP_ERR_ARG;
     HHP_TRY(ensure_transpose(A));
     return hhp_mat_get_csr(A->t, t_rowptr, t_col, t_val);
+    HHP_API_END
 }
 
 hhp_status hhp_spmv_dev(hhp_ctx *ctx, hhp_mat *A, double alpha, const double *x, double beta, double *y) {
+    HHP_API_BEGIN
     if (!ctx || !A || A->ctx != ctx || (A->n > 0 && !x) || (A->m > 0 && !y)) {
         set_error("hhp_spmv_dev: invalid arguments");
         return HHP_ERR_ARG;
     }
     if (A->m == 0) return HHP_OK;
     return launch_spmv64(A, ctx->stream, EP_AXPBY, x, y, nullptr, alpha, beta);
+    HHP_API_END
 }
 
 hhp_status hhp_spmv_f32_dev(hhp_ctx *ctx, hhp_mat *A, const float *x, float *y) {
+    HHP_API_BEGIN
     if (!ctx || !A || A->ctx != ctx || (A->n > 0 && !x) || (A->m > 0 && !y)) {
         set_error("hhp_spmv_f32_dev: invalid arguments");
         return HHP_ERR_ARG;
@@ -405,9 +424,11 @@ hhp_status hhp_spmv_f32_dev(hhp_ctx *ctx, hhp_mat *A, const float *x, float *y) 
     if (!A->val32) HHP_TRY(mat_refresh_derived(A));
     if (A->m == 0) return HHP_OK;
     return launch_spmv32(A, ctx->stream, EP_AXPBY, x, y, nullptr);
+    HHP_API_END
 }
 
 hhp_status hhp_spmv_t_dev(hhp_ctx *ctx, hhp_mat *A, const double *x, double *y) {
+    HHP_API_BEGIN
     if (!ctx || !A || A->ctx != ctx || (A->m > 0 && !x) || (A->n > 0 && !y)) {
         set_error("hhp_spmv_t_dev: invalid arguments");
         return HHP_ERR_ARG;
@@ -415,9 +436,11 @@ hhp_status hhp_spmv_t_dev(hhp_ctx *ctx, hhp_mat *A, const double *x, double *y) 
     HHP_TRY(ensure_transpose(A));
     if (A->n == 0) return HHP_OK;
     return launch_spmv64(A->t, ctx->stream, EP_AXPBY, x, y, nullptr, 1.0, 0.0);
+    HHP_API_END
 }
 
 hhp_status hhp_spmv(hhp_ctx *ctx, hhp_mat *A, const double *x, double *y) {
+    HHP_API_BEGIN
     if (!ctx || !A || A->ctx != ctx || (A->n > 0 && !x) || (A->m > 0 && !y)) {
         set_error("hhp_spmv: invalid arguments");
         return HHP_ERR_ARG;
@@ -441,6 +464,7 @@ hhp_status hhp_spmv(hhp_ctx *ctx, hhp_mat *A, const double *x, double *y) {
     cudaFree(dx);
     cudaFree(dy);
     return rc;
+    HHP_API_END
 }
 
 static hhp_solve_opts default_opts() {
@@ -475,22 +499,27 @@ static hhp_status check_solve(hhp_ctx *ctx, hhp_mat *A, const void *b, const voi
 
 hhp_status hhp_bicgstab(hhp_ctx *ctx, hhp_mat *A, const double *b, double *x, const double *xt,
                         const hhp_solve_opts *opts, hhp_solve_info *info) {
+    HHP_API_BEGIN
     HHP_TRY(check_solve(ctx, A, b, x, opts));
     const hhp_solve_opts o = opts ? *opts : default_opts();
     if (o.precond == HHP_PRECOND_JACOBI) return solve_jacobi(A, b, x, xt, &o, info, true);
     return solve_any(A, b, x, xt, &o, info, true);
+    HHP_API_END
 }
 
 hhp_status hhp_bicgstab_dev(hhp_ctx *ctx, hhp_mat *A, const double *b, double *x, const double *xt,
                             const hhp_solve_opts *opts, hhp_solve_info *info) {
+    HHP_API_BEGIN
     HHP_TRY(check_solve(ctx, A, b, x, opts));
     const hhp_solve_opts o = opts ? *opts : default_opts();
     if (o.precond == HHP_PRECOND_JACOBI) return solve_jacobi(A, b, x, xt, &o, info, false);
     return solve_any(A, b, x, xt, &o, info, false);
+    HHP_API_END
 }
 
 hhp_status hhp_bicgstab_backward_dev(hhp_ctx *ctx, hhp_mat *A, const double *x, const double *dldx, double *dldb,
                                      double *dlda, const hhp_solve_opts *opts, hhp_solve_info *info) {
+    HHP_API_BEGIN
     HHP_TRY(check_solve(ctx, A, dldx, x, opts));
     if (!dldb) {
         set_error("bicgstab_backward: dldb is NULL");
@@ -499,10 +528,12 @@ hhp_status hhp_bicgstab_backward_dev(hhp_ctx *ctx, hhp_mat *A, const double *x, 
     hhp_solve_opts o = opts ? *opts : default_opts();
     o.fixed_iters = 0;
     return backward_dev(A, x, dldx, dldb, dlda, &o, info);
+    HHP_API_END
 }
 
 hhp_status hhp_bicgstab_backward(hhp_ctx *ctx, hhp_mat *A, const double *x, const double *dldx, double *dldb,
                                  double *dlda, const hhp_solve_opts *opts, hhp_solve_info *info) {
+    HHP_API_BEGIN
     HHP_TRY(check_solve(ctx, A, dldx, x, opts));
     if (!dldb) {
         set_error("bicgstab_backward: dldb is NULL");
@@ -532,6 +563,7 @@ hhp_status hhp_bicgstab_backward(hhp_ctx *ctx, hhp_mat *A, const double *x, cons
     }
     cudaFree(d);
     return rc;
+    HHP_API_END
 }
 
 }  // extern "C"

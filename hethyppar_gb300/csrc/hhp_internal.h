@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <exception>
+#include <new>
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -15,6 +17,30 @@ namespace hhp {
 // ---- error plumbing ----------------------------------------------------------------------------
 void set_error(const char *fmt, ...);
 hhp_status cuda_fail(cudaError_t e, const char *what, const char *file, int line);
+
+// No C++ exception crosses the C ABI: every entry point that allocates host memory or starts
+// threads runs its body inside HHP_API_BEGIN / HHP_API_END, which turn an exception into a status
+// (std::bad_alloc -> HHP_ERR_OOM, anything else -> HHP_ERR_STATE) with the message recorded.
+inline hhp_status api_exception() {
+    try {
+        throw;
+    } catch (const std::bad_alloc &) {
+        set_error("out of host memory");
+        return HHP_ERR_OOM;
+    } catch (const std::exception &e) {
+        set_error("internal error: %s", e.what());
+        return HHP_ERR_STATE;
+    } catch (...) {
+        set_error("internal error");
+        return HHP_ERR_STATE;
+    }
+}
+#define HHP_API_BEGIN try {
+#define HHP_API_END                          \
+    }                                        \
+    catch (...) {                            \
+        return ::hhp::api_exception();       \
+    }
 
 #define HHP_CUDA(call)                                                          \
     do {                                                                        \

@@ -387,6 +387,7 @@ hhp_status read_mtx(const char *path, int &m, int &n, int &nnz, std::vector<int>
 }  // namespace hhp
 
 extern "C" hhp_status hhp_vector_read(const char *path, int size, double *out) {
+    HHP_API_BEGIN
     if (!path || size < 0 || (size > 0 && !out)) {
         hhp::set_error("hhp_vector_read: invalid arguments");
         return HHP_ERR_ARG;
@@ -404,9 +405,11 @@ extern "C" hhp_status hhp_vector_read(const char *path, int size, double *out) {
         }
     }
     return HHP_OK;
+    HHP_API_END
 }
 
 extern "C" hhp_status hhp_vector_write(const char *path, int size, const double *v, int exact) {
+    HHP_API_BEGIN
     if (!path || size < 0 || (size > 0 && !v)) {
         hhp::set_error("hhp_vector_write: invalid arguments");
         return HHP_ERR_ARG;
@@ -428,10 +431,12 @@ extern "C" hhp_status hhp_vector_write(const char *path, int size, const double 
         return HHP_ERR_IO;
     }
     return HHP_OK;
+    HHP_API_END
 }
 
 extern "C" hhp_status hhp_mtx_read(const char *path, int *m, int *n, int *nnz, int **rowptr, int **col,
                                    double **val) {
+    HHP_API_BEGIN
     if (!m || !n || !nnz || !rowptr || !col || !val) {
         hhp::set_error("hhp_mtx_read: null output pointer");
         return HHP_ERR_ARG;
@@ -461,12 +466,14 @@ extern "C" hhp_status hhp_mtx_read(const char *path, int *m, int *n, int *nnz, i
     *col = b;
     *val = d;
     return HHP_OK;
+    HHP_API_END
 }
 
 extern "C" void hhp_free(void *p) { std::free(p); }
 
 extern "C" hhp_status hhp_csr_file_write(const char *path, int m, int n, int nnz, const int *rowptr, const int *col,
                                          const double *val) {
+    HHP_API_BEGIN
     if (!path || m < 0 || n < 0 || nnz < 0 || !rowptr || (nnz > 0 && (!col || !val))) {
         hhp::set_error("hhp_csr_file_write: invalid arguments");
         return HHP_ERR_ARG;
@@ -493,4 +500,5 @@ extern "C" hhp_status hhp_csr_file_write(const char *path, int m, int n, int nnz
         return HHP_ERR_IO;
     }
     return HHP_OK;
+    HHP_API_END
 }

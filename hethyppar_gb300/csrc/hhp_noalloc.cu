@@ -142,6 +142,7 @@ hhp_status scratch_for_current_device(Scratch &out) {
 extern "C" hhp_status hhp_spmv_csr_noalloc(int m, int n, int nnz, const int *rowptr_dev, const int *col_dev,
                                            const double *val_dev, double alpha, const double *x_dev, double beta,
                                            double *y_dev, void *stream) {
+    HHP_API_BEGIN
     if (m < 0 || n < 0 || nnz < 0 || !rowptr_dev || (nnz > 0 && (!col_dev || !val_dev)) || (m > 0 && !y_dev) ||
         (nnz > 0 && !x_dev)) {
         hhp::set_error("hhp_spmv_csr_noalloc: invalid sizes or null pointers");
@@ -166,4 +167,5 @@ extern "C" hhp_status hhp_spmv_csr_noalloc(int m, int n, int nnz, const int *row
                                                                       sc.row);
     HHP_CUDA(cudaGetLastError());
     return HHP_OK;
+    HHP_API_END
 }

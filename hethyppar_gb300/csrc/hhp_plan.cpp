@@ -243,6 +243,7 @@ bool rows_ascending(int m, const int *rowptr) {
 
 extern "C" hhp_status hhp_plan_stats(int m, int nnz, const int *rowptr, int rows_per_lane, int cap, int *n_slices,
                                      int *n_long_rows, int *n_chunks, int *sorted, double *padding) {
+    HHP_API_BEGIN
     if (m < 0 || nnz < 0 || !rowptr || (rows_per_lane != 1 && rows_per_lane != 2 && rows_per_lane != 4) ||
         cap < 32) {
         hhp::set_error("hhp_plan_stats: invalid arguments");
@@ -261,10 +262,12 @@ extern "C" hhp_status hhp_plan_stats(int m, int nnz, const int *rowptr, int rows
     if (sorted) *sorted = P.sorted ? 1 : 0;
     if (padding) *padding = P.padding;
     return HHP_OK;
+    HHP_API_END
 }
 
 extern "C" hhp_status hhp_plan_dump(int m, int nnz, const int *rowptr, int rows_per_lane, int cap, int capacity,
                                     int *slice_rows, int *chunks, int *n_slices, int *n_chunks) {
+    HHP_API_BEGIN
     if (m < 0 || nnz < 0 || !rowptr || (rows_per_lane != 1 && rows_per_lane != 2 && rows_per_lane != 4) ||
         cap < 32 || !n_slices || !n_chunks) {
         hhp::set_error("hhp_plan_dump: invalid arguments");
@@ -292,4 +295,5 @@ extern "C" hhp_status hhp_plan_dump(int m, int nnz, const int *rowptr, int rows_
         chunks[4 * c + 3] = P.chunks[c].w;
     }
     return HHP_OK;
+    HHP_API_END
 }

@@ -107,6 +107,7 @@ int lowest_degree(const Graph &g, const std::vector<int> &nodes) {
 using namespace hhp;
 
 hhp_status hhp_reorder_rcm(int m, const int *rowptr, const int *col, int *perm) {
+    HHP_API_BEGIN
     if (m < 0 || (m > 0 && (!rowptr || !perm)) || (m > 0 && rowptr[m] > 0 && !col)) {
         set_error("reorder_rcm: null argument or negative size");
         return HHP_ERR_ARG;
@@ -171,4 +172,5 @@ hhp_status hhp_reorder_rcm(int m, const int *rowptr, const int *col, int *perm) 
     }
     for (int i = 0; i < m; ++i) perm[i] = order[static_cast<size_t>(m - 1 - i)];
     return HHP_OK;
+    HHP_API_END
 }

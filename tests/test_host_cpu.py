@@ -285,6 +285,28 @@ def test_tuning_overrides_out_of_range_are_clamped():
     assert long_rows > 0 and slices >= 0  # threshold clamped to 1: every row with 2+ entries is long
 
 
+def test_host_allocation_failure_is_a_status_not_a_crash():
+    # with the address space capped just above what the process already maps, building the work
+    # plan of a 60M-row pattern cannot get its ~750 MB: the C ABI returns HHP_ERR_OOM (an
+    # exception never crosses it) and the process carries on
+    code = ("import os, resource, sys, numpy as np, hethyppar_gb300 as h\n"
+            "rp = np.arange(60_000_001, dtype=np.int32) * 3\n"
+            "vm = [l for l in open('/proc/self/status') if l.startswith('VmSize:')][0].split()[1]\n"
+            "cap = (int(vm) << 10) + (256 << 20)\n"
+            "resource.setrlimit(resource.RLIMIT_AS, (cap, cap))\n"
+            "try:\n"
+            "    h.plan_stats(rp, 2, 2048)\n"
+            "    print('no error')\n"
+            "except h.HHPError as e:\n"
+            "    print('status', e.status)\n"
+            "print(h.plan_stats(np.array([0, 1, 2], np.int32), 2, 2048)['slices'])\n")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, stdout=subprocess.PIPE, stderr=subprocess.PIPE,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    out = r.stdout.split()
+    assert out[:2] == ["status", "4"] and out[2] == "1", r.stdout
+
+
 def test_cli_rejects_missing_arguments():
     exe = os.path.join(ROOT, "hethyppar_gb300", "bin", "hhp-bicgstab")
     r = subprocess.run([exe, "-m", "/nonexistent.mtx"], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
