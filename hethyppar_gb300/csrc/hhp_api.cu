@@ -121,9 +121,11 @@ hhp_status mat_create_dev(hhp_ctx *ctx, int m, int n, int nnz, hhp_mat **out) {
         set_error("out of device memory for a %d x %d matrix with %d nonzeros", m, n, nnz);
         return HHP_ERR_OOM;
     }
-    HHP_CUDA(cudaMemset(A->rowptr, 0, rp * sizeof(int)));
-    HHP_CUDA(cudaMemset(A->col, 0, nz * sizeof(int)));
-    HHP_CUDA(cudaMemset(A->val, 0, nz * sizeof(double)));
+    // on the context's stream: it is non-blocking, so work on the legacy default stream would not
+    // be ordered before the kernels that later read these arrays
+    HHP_CUDA(cudaMemsetAsync(A->rowptr, 0, rp * sizeof(int), ctx->stream));
+    HHP_CUDA(cudaMemsetAsync(A->col, 0, nz * sizeof(int), ctx->stream));
+    HHP_CUDA(cudaMemsetAsync(A->val, 0, nz * sizeof(double), ctx->stream));
     *out = A;
     return HHP_OK;
 }
@@ -131,10 +133,10 @@ hhp_status mat_create_dev(hhp_ctx *ctx, int m, int n, int nnz, hhp_mat **out) {
 hhp_status mat_refresh_derived(hhp_mat *A) {
     if (!A->val32) {
         HHP_CUDA(cudaMalloc(&A->val32, (static_cast<size_t>(A->nnz) + 4) * sizeof(float)));
-        HHP_CUDA(cudaMemset(A->val32, 0, (static_cast<size_t>(A->nnz) + 4) * sizeof(float)));
+        HHP_CUDA(cudaMemsetAsync(A->val32, 0, (static_cast<size_t>(A->nnz) + 4) * sizeof(float), A->ctx->stream));
     }
     if (A->nnz > 0) {
-        const int grid = std::max(1, std::min((A->nnz + 255) / 256, 8 * A->ctx->num_sms));
+        const int grid = static_cast<int>(std::max(1LL, std::min((A->nnz + 255LL) / 256, 8LL * A->ctx->num_sms)));
         k_to_f32<<<grid, 256, 0, A->ctx->stream>>>(A->val, A->val32, A->nnz);
         HHP_CUDA(cudaGetLastError());
     }
@@ -194,7 +196,9 @@ hhp_status hhp_ctx_create(int device, hhp_ctx **out) {
     c->smem_optin = prop.sharedMemPerBlockOptin;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
-        cudaMalloc(&c->dev_err, sizeof(int)) != cudaSuccess || cudaMemset(c->dev_err, 0, sizeof(int)) != cudaSuccess) {
+        cudaMalloc(&c->dev_err, sizeof(int)) != cudaSuccess ||
+        cudaMemsetAsync(c->dev_err, 0, sizeof(int), c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess) {
         hhp_ctx_destroy(c);
         set_error("hhp_ctx_create: CUDA setup failed: %s", cudaGetErrorString(cudaGetLastError()));
         return HHP_ERR_CUDA;
@@ -267,9 +271,13 @@ hhp_status hhp_mat_from_csr(hhp_ctx *ctx, int m, int n, int nnz, const int *rowp
     hhp_mat *A = nullptr;
     HHP_TRY(mat_create_dev(ctx, m, n, nnz, &A));
     A->rowptr_host.assign(rowptr, rowptr + m + 1);
-    if (cudaMemcpy(A->rowptr, rowptr, sizeof(int) * (static_cast<size_t>(m) + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
-        (nnz > 0 && cudaMemcpy(A->col, col, sizeof(int) * static_cast<size_t>(nnz), cudaMemcpyHostToDevice) != cudaSuccess) ||
-        (nnz > 0 && cudaMemcpy(A->val, val, sizeof(double) * static_cast<size_t>(nnz), cudaMemcpyHostToDevice) != cudaSuccess)) {
+    const cudaStream_t st = ctx->stream;
+    // ordered after the zero fill on the same stream; the wait keeps the (possibly temporary) host
+    // arrays alive until the copies have landed
+    if (cudaMemcpyAsync(A->rowptr, rowptr, sizeof(int) * (static_cast<size_t>(m) + 1), cudaMemcpyHostToDevice, st) ||
+        (nnz > 0 && cudaMemcpyAsync(A->col, col, sizeof(int) * static_cast<size_t>(nnz), cudaMemcpyHostToDevice, st)) ||
+        (nnz > 0 && cudaMemcpyAsync(A->val, val, sizeof(double) * static_cast<size_t>(nnz), cudaMemcpyHostToDevice, st)) ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
         hhp_mat_destroy(A);
         set_error("hhp_mat_from_csr: upload failed");
         return HHP_ERR_CUDA;
@@ -287,6 +295,8 @@ hhp_status hhp_mat_from_csr_dev(hhp_ctx *ctx, int m, int n, int nnz, const int *
         return HHP_ERR_ARG;
     }
     std::vector<int> rp(static_cast<size_t>(m) + 1);
+    // the caller's arrays may have been written by work on this context's stream
+    HHP_CUDA(cudaStreamSynchronize(ctx->stream));
     HHP_CUDA(cudaMemcpy(rp.data(), rowptr_dev, sizeof(int) * rp.size(), cudaMemcpyDeviceToHost));
     if (rp[0] != 0 || rp[static_cast<size_t>(m)] != nnz) {
         set_error("hhp_mat_from_csr_dev: rowptr[0] must be 0 and rowptr[m] must equal nnz");
@@ -302,20 +312,28 @@ hhp_status hhp_mat_from_csr_dev(hhp_ctx *ctx, int m, int n, int nnz, const int *
     A->rowptr_host = std::move(rp);
     int *bad = nullptr;
     int hbad = 0;
-    if (cudaMemcpy(A->rowptr, rowptr_dev, sizeof(int) * (static_cast<size_t>(m) + 1), cudaMemcpyDeviceToDevice) ||
-        (nnz > 0 && cudaMemcpy(A->col, col_dev, sizeof(int) * static_cast<size_t>(nnz), cudaMemcpyDeviceToDevice)) ||
-        (nnz > 0 && cudaMemcpy(A->val, val_dev, sizeof(double) * static_cast<size_t>(nnz), cudaMemcpyDeviceToDevice)) ||
-        cudaMalloc(&bad, sizeof(int)) || cudaMemset(bad, 0, sizeof(int))) {
+    const cudaStream_t st = ctx->stream;
+    if (cudaMalloc(&bad, sizeof(int)) ||
+        cudaMemcpyAsync(A->rowptr, rowptr_dev, sizeof(int) * (static_cast<size_t>(m) + 1), cudaMemcpyDeviceToDevice, st) ||
+        (nnz > 0 && cudaMemcpyAsync(A->col, col_dev, sizeof(int) * static_cast<size_t>(nnz), cudaMemcpyDeviceToDevice, st)) ||
+        (nnz > 0 && cudaMemcpyAsync(A->val, val_dev, sizeof(double) * static_cast<size_t>(nnz), cudaMemcpyDeviceToDevice, st)) ||
+        cudaMemsetAsync(bad, 0, sizeof(int), st)) {
         cudaFree(bad);
         hhp_mat_destroy(A);
         set_error("hhp_mat_from_csr_dev: copy failed");
         return HHP_ERR_CUDA;
     }
     if (nnz > 0) {
-        k_check_cols<<<std::max(1, std::min((nnz + 255) / 256, 8 * ctx->num_sms)), 256>>>(A->col, nnz, n, bad);
-        cudaMemcpy(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost);
+        k_check_cols<<<static_cast<int>(std::max(1LL, std::min((nnz + 255LL) / 256, 8LL * ctx->num_sms))), 256, 0,
+                       st>>>(A->col, nnz, n, bad);
+        cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st);
     }
+    const cudaError_t e_sync = cudaStreamSynchronize(st);
     cudaFree(bad);
+    if (e_sync != cudaSuccess) {
+        hhp_mat_destroy(A);
+        return cuda_fail(e_sync, "hhp_mat_from_csr_dev: copy", __FILE__, __LINE__);
+    }
     if (hbad != 0) {
         hhp_mat_destroy(A);
         set_error("hhp_mat_from_csr_dev: %d column indices outside [0, %d)", hbad, n);
@@ -383,16 +401,12 @@ hhp_status hhp_mat_set_values_dev(hhp_mat *A, const double *val) { return set_va
 
 hhp_status hhp_mat_get_csr(const hhp_mat *A, int *rowptr, int *col, double *val) {
     HHP_API_BEGIN
-    HHP_API_BEGIN
-    HHP_API_BEGIN
     if (!A) return HHP_ERR_ARG;
     HHP_CUDA(cudaStreamSynchronize(A->ctx->stream));
     if (rowptr) HHP_CUDA(cudaMemcpy(rowptr, A->rowptr, sizeof(int) * (static_cast<size_t>(A->m) + 1), cudaMemcpyDeviceToHost));
     if (col && A->nnz) HHP_CUDA(cudaMemcpy(col, A->col, sizeof(int) * static_cast<size_t>(A->nnz), cudaMemcpyDeviceToHost));
     if (val && A->nnz) HHP_CUDA(cudaMemcpy(val, A->val, sizeof(double) * static_cast<size_t>(A->nnz), cudaMemcpyDeviceToHost));
     return HHP_OK;
-    HHP_API_END
-    HHP_API_END
     HHP_API_END
 }
 
@@ -544,8 +558,8 @@ hhp_status hhp_bicgstab_backward(hhp_ctx *ctx, hhp_mat *A, const double *x, cons
     HHP_CUDA(cudaMalloc(&d, sizeof(double) * (3 * n + nz + 1)));
     double *dx = d, *dg = d + n, *db = d + 2 * n, *da = d + 3 * n;
     hhp_status rc = HHP_OK;
-    if (cudaMemcpy(dx, x, sizeof(double) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(dg, dldx, sizeof(double) * n, cudaMemcpyHostToDevice) != cudaSuccess) {
+    if (cudaMemcpyAsync(dx, x, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
+        cudaMemcpyAsync(dg, dldx, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess) {
         set_error("bicgstab_backward: upload failed");
         rc = HHP_ERR_CUDA;
     }
@@ -555,8 +569,10 @@ hhp_status hhp_bicgstab_backward(hhp_ctx *ctx, hhp_mat *A, const double *x, cons
         rc = backward_dev(A, dx, dg, db, dlda ? da : nullptr, &o, info);
     }
     if (rc == HHP_OK || rc == HHP_ERR_MAXIT) {
-        if (cudaMemcpy(dldb, db, sizeof(double) * n, cudaMemcpyDeviceToHost) != cudaSuccess ||
-            (dlda && nz && cudaMemcpy(dlda, da, sizeof(double) * nz, cudaMemcpyDeviceToHost) != cudaSuccess)) {
+        if (cudaMemcpyAsync(dldb, db, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+            (dlda && nz &&
+             cudaMemcpyAsync(dlda, da, sizeof(double) * nz, cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess) ||
+            cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
             set_error("bicgstab_backward: download failed");
             rc = HHP_ERR_CUDA;
         }

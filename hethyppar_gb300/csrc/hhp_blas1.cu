@@ -73,7 +73,7 @@ hhp_status ensure_dot_scratch(hhp_ctx *ctx) {
     if (ctx->dot_part) return HHP_OK;
     if (cudaMalloc(&ctx->dot_part, sizeof(double) * kDotMaxBlocks) != cudaSuccess ||
         cudaMalloc(&ctx->dot_count, sizeof(unsigned)) != cudaSuccess ||
-        cudaMemset(ctx->dot_count, 0, sizeof(unsigned)) != cudaSuccess) {
+        cudaMemsetAsync(ctx->dot_count, 0, sizeof(unsigned), ctx->stream) != cudaSuccess) {
         set_error("dot: out of device memory for the partials");
         return HHP_ERR_OOM;
     }

@@ -92,10 +92,10 @@ __global__ void k_XR(double *X, double *R, const double *P, const double *S, con
 
 inline bool a16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 inline int grid_of(int n) {
-    int dev = 0, sms = 148;
+    int dev = 0, sms = 152;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int want = (n + 511) / 512;
-    return want < 1 ? 1 : (want < 4 * sms ? want : 4 * sms);
+    const long long want = (n + 511LL) / 512;
+    return want < 1 ? 1 : static_cast<int>(want < 4LL * sms ? want : 4LL * sms);
 }
 
 }  // namespace

@@ -1162,7 +1162,7 @@ __global__ void __launch_bounds__(512) k_mix_final(const DevScal *sc, double *X,
 
 // ---------------------------------------------------------------------------------------------
 template <typename T>
-T *dalloc(size_t n, hhp_status &st) {
+T *dalloc(size_t n, hhp_status &st, cudaStream_t stream) {
     T *p = nullptr;
     if (st != HHP_OK) return nullptr;
     if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) {
@@ -1170,7 +1170,9 @@ T *dalloc(size_t n, hhp_status &st) {
         st = HHP_ERR_OOM;
         return nullptr;
     }
-    cudaMemset(p, 0, n * sizeof(T));
+    // zeroed on the context's stream, ahead of every kernel that uses the buffer (the legacy
+    // default stream is not ordered with the library's non-blocking streams)
+    cudaMemsetAsync(p, 0, n * sizeof(T), stream);
     return p;
 }
 
@@ -1187,23 +1189,23 @@ hhp_status ensure_solver(hhp_mat *A, Solver **out, int maxit) {
         s->unroll = std::max(1, std::min(tuning().unroll_iters, 16));
         hhp_status st = HHP_OK;
         const size_t np = static_cast<size_t>(s->n_pad);
-        s->X = dalloc<double>(np, st);
-        s->B = dalloc<double>(np, st);
-        s->R = dalloc<double>(np, st);
-        s->R0 = dalloc<double>(np, st);
-        s->P = dalloc<double>(np, st);
-        s->V = dalloc<double>(np, st);
-        s->S = dalloc<double>(np, st);
-        s->T = dalloc<double>(np, st);
-        s->Y = dalloc<double>(np, st);
-        s->part_xr = dalloc<double>(2 * s->nblk, st);
-        s->part_s = dalloc<double>(4 * s->nblk, st);  // K_S records are 4 wide
-        s->part_b = dalloc<double>(s->nblk, st);
-        s->x0_nz = dalloc<int>(1, st);
-        s->part_xr32 = dalloc<double>(2 * s->nblk, st);
-        s->part_s32 = dalloc<double>(4 * s->nblk, st);
-        s->sc = dalloc<DevScal>(1, st);
-        s->sc32 = dalloc<DevScal>(1, st);
+        s->X = dalloc<double>(np, st, A->ctx->stream);
+        s->B = dalloc<double>(np, st, A->ctx->stream);
+        s->R = dalloc<double>(np, st, A->ctx->stream);
+        s->R0 = dalloc<double>(np, st, A->ctx->stream);
+        s->P = dalloc<double>(np, st, A->ctx->stream);
+        s->V = dalloc<double>(np, st, A->ctx->stream);
+        s->S = dalloc<double>(np, st, A->ctx->stream);
+        s->T = dalloc<double>(np, st, A->ctx->stream);
+        s->Y = dalloc<double>(np, st, A->ctx->stream);
+        s->part_xr = dalloc<double>(2 * s->nblk, st, A->ctx->stream);
+        s->part_s = dalloc<double>(4 * s->nblk, st, A->ctx->stream);  // K_S records are 4 wide
+        s->part_b = dalloc<double>(s->nblk, st, A->ctx->stream);
+        s->x0_nz = dalloc<int>(1, st, A->ctx->stream);
+        s->part_xr32 = dalloc<double>(2 * s->nblk, st, A->ctx->stream);
+        s->part_s32 = dalloc<double>(4 * s->nblk, st, A->ctx->stream);
+        s->sc = dalloc<DevScal>(1, st, A->ctx->stream);
+        s->sc32 = dalloc<DevScal>(1, st, A->ctx->stream);
         if (st == HHP_OK && cudaMallocHost(&s->h_sc, sizeof(DevScal)) != cudaSuccess) st = HHP_ERR_OOM;
         if (st == HHP_OK && cudaMallocHost(&s->h_sc32, sizeof(DevScal)) != cudaSuccess) st = HHP_ERR_OOM;
         if (st == HHP_OK && (cudaStreamCreateWithFlags(&s->s2, cudaStreamNonBlocking) != cudaSuccess ||
@@ -1237,13 +1239,13 @@ hhp_status ensure_fp32_inner(hhp_mat *A, Solver *s) {
     if (!s->D32) {
         hhp_status st = HHP_OK;
         const size_t np = static_cast<size_t>(s->n_pad);
-        s->D32 = dalloc<float>(np, st);
-        s->R32 = dalloc<float>(np, st);
-        s->R0_32 = dalloc<float>(np, st);
-        s->P32 = dalloc<float>(np, st);
-        s->V32 = dalloc<float>(np, st);
-        s->S32 = dalloc<float>(np, st);
-        s->T32 = dalloc<float>(np, st);
+        s->D32 = dalloc<float>(np, st, A->ctx->stream);
+        s->R32 = dalloc<float>(np, st, A->ctx->stream);
+        s->R0_32 = dalloc<float>(np, st, A->ctx->stream);
+        s->P32 = dalloc<float>(np, st, A->ctx->stream);
+        s->V32 = dalloc<float>(np, st, A->ctx->stream);
+        s->S32 = dalloc<float>(np, st, A->ctx->stream);
+        s->T32 = dalloc<float>(np, st, A->ctx->stream);
         if (st != HHP_OK) return st;
     }
     return HHP_OK;

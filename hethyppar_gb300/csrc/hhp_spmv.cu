@@ -477,12 +477,15 @@ __global__ void k_offsets_fit(const int *__restrict__ rowptr, const int *__restr
     }
 }
 
+// Device copy of a host vector (zero-padded to min_elems), ordered on `st`: the library's streams
+// are non-blocking, so zero fills or copies on the legacy default stream would not be ordered
+// before the kernels that read these arrays.
 template <typename T>
-hhp_status upload(T **dst, const std::vector<T> &src, size_t min_elems = 1) {
+hhp_status upload(T **dst, const std::vector<T> &src, cudaStream_t st, size_t min_elems = 1) {
     const size_t n = std::max(src.size(), min_elems);
     HHP_CUDA(cudaMalloc(reinterpret_cast<void **>(dst), n * sizeof(T)));
-    HHP_CUDA(cudaMemset(*dst, 0, n * sizeof(T)));
-    if (!src.empty()) HHP_CUDA(cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
+    HHP_CUDA(cudaMemsetAsync(*dst, 0, n * sizeof(T), st));
+    if (!src.empty()) HHP_CUDA(cudaMemcpyAsync(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, st));
     return HHP_OK;
 }
 
@@ -542,8 +545,8 @@ hhp_status build_plan_dev(hhp_mat *A, PlanDev &p) {
     p.ctas = ctx->num_sms * std::min(std::max(cps, 1), 8);
     std::vector<int> wptr, wunits;
     assign_units(h, p.ctas * p.warps_per_cta, wptr, wunits, &p.imbalance);
-    HHP_TRY(upload(&p.warp_ptr, wptr));
-    HHP_TRY(upload(&p.warp_units, wunits));
+    HHP_TRY(upload(&p.warp_ptr, wptr, ctx->stream));
+    HHP_TRY(upload(&p.warp_units, wunits, ctx->stream));
     {
         std::vector<int4> rec(wunits.size());
         for (size_t i = 0; i < wunits.size(); ++i) {
@@ -557,17 +560,17 @@ hhp_status build_plan_dev(hhp_mat *A, PlanDev &p) {
                 rec[i] = make_int4(u, 0, 0, 0);
             }
         }
-        HHP_TRY(upload(&p.unit_rec, rec));
+        HHP_TRY(upload(&p.unit_rec, rec, ctx->stream));
     }
-    HHP_TRY(upload(&p.slice_ptr, h.slice_ptr));
-    HHP_TRY(upload(&p.pos_row, h.pos_row, 4));
-    HHP_TRY(upload(&p.pos_len, h.pos_len, 4));
-    HHP_TRY(upload(&p.chunks, h.chunks));
-    HHP_TRY(upload(&p.long_first, h.long_first));
-    HHP_TRY(upload(&p.chunk_long, h.chunk_long));
+    HHP_TRY(upload(&p.slice_ptr, h.slice_ptr, ctx->stream));
+    HHP_TRY(upload(&p.pos_row, h.pos_row, ctx->stream, 4));
+    HHP_TRY(upload(&p.pos_len, h.pos_len, ctx->stream, 4));
+    HHP_TRY(upload(&p.chunks, h.chunks, ctx->stream));
+    HHP_TRY(upload(&p.long_first, h.long_first, ctx->stream));
+    HHP_TRY(upload(&p.chunk_long, h.chunk_long, ctx->stream));
     const size_t tot = static_cast<size_t>(std::max<long long>(h.total, 1));
     HHP_CUDA(cudaMalloc(&p.sval, tot * sizeof(VT)));
-    HHP_CUDA(cudaMemset(p.sval, 0, tot * sizeof(VT)));
+    HHP_CUDA(cudaMemsetAsync(p.sval, 0, tot * sizeof(VT), ctx->stream));
     // Index words: 16-bit offsets col - row when every slice row's entries lie within 2^15 of
     // the diagonal (stencils: 2 bytes per nonzero instead of 4), else int32 columns.
     p.d16 = false;
@@ -586,18 +589,18 @@ hhp_status build_plan_dev(hhp_mat *A, PlanDev &p) {
     }
     if (p.d16) {
         HHP_CUDA(cudaMalloc(&p.scol16, tot * sizeof(short)));
-        HHP_CUDA(cudaMemset(p.scol16, 0, tot * sizeof(short)));
+        HHP_CUDA(cudaMemsetAsync(p.scol16, 0, tot * sizeof(short), ctx->stream));
     } else {
         HHP_CUDA(cudaMalloc(&p.scol, tot * sizeof(int)));
-        HHP_CUDA(cudaMemset(p.scol, 0, tot * sizeof(int)));
+        HHP_CUDA(cudaMemsetAsync(p.scol, 0, tot * sizeof(int), ctx->stream));
     }
     HHP_CUDA(cudaMalloc(&p.chunk_part, sizeof(double) * std::max(1, p.n_chunks)));
     HHP_CUDA(cudaMalloc(&p.long_cnt, sizeof(unsigned) * std::max(1, p.n_long)));
-    HHP_CUDA(cudaMemset(p.long_cnt, 0, sizeof(unsigned) * std::max(1, p.n_long)));
+    HHP_CUDA(cudaMemsetAsync(p.long_cnt, 0, sizeof(unsigned) * std::max(1, p.n_long), ctx->stream));
     HHP_CUDA(cudaMalloc(&p.long_dot, sizeof(double) * 4 * std::max(1, p.n_long)));
-    HHP_CUDA(cudaMemset(p.long_dot, 0, sizeof(double) * 4 * std::max(1, p.n_long)));
+    HHP_CUDA(cudaMemsetAsync(p.long_dot, 0, sizeof(double) * 4 * std::max(1, p.n_long), ctx->stream));
     HHP_CUDA(cudaMalloc(&p.cta_part, sizeof(double) * 4 * p.ctas));
-    HHP_CUDA(cudaMemset(p.cta_part, 0, sizeof(double) * 4 * p.ctas));
+    HHP_CUDA(cudaMemsetAsync(p.cta_part, 0, sizeof(double) * 4 * p.ctas, ctx->stream));
     HHP_TRY(fill_values<VT>(A, p, true));
     HHP_CUDA(cudaStreamSynchronize(ctx->stream));
     return HHP_OK;
