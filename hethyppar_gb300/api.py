@@ -27,6 +27,29 @@ def _ptr(a) -> ctypes.c_void_p:
     return a.ctypes.data_as(ctypes.c_void_p)
 
 
+class _Ordered:
+    """Orders a library call on device tensors with torch's current stream: the context's stream
+    waits for the work torch has queued (the inputs), and torch's stream waits for the call's work
+    (the outputs). Event waits on the device, no host synchronisation."""
+
+    def __init__(self, ctx, *tensors):
+        self.on = any(hasattr(t, "data_ptr") for t in tensors)
+        self.ctx = ctx
+
+    def __enter__(self):
+        if self.on:
+            import torch
+            self.ext = torch.cuda.ExternalStream(self.ctx.stream)
+            self.cur = torch.cuda.current_stream()
+            self.ext.wait_stream(self.cur)
+        return self
+
+    def __exit__(self, *exc):
+        if self.on:
+            self.cur.wait_stream(self.ext)
+        return False
+
+
 def _host(a, dtype) -> np.ndarray:
     return np.ascontiguousarray(a, dtype=dtype)
 
@@ -69,23 +92,27 @@ class Context:
     def dot(self, x, y, out=None):
         """sum x*y: a Python float, or written into the 1-element CUDA tensor `out` (no sync)."""
         n = int(x.numel())
-        if out is not None:
-            check(lib().hhp_dot_dev(self._h, n, _ptr(x), _ptr(y), _ptr(out)), "hhp_dot_dev")
-            return out
-        r = ctypes.c_double()
-        check(lib().hhp_dot(self._h, n, _ptr(x), _ptr(y), ctypes.byref(r)), "hhp_dot")
+        with _Ordered(self, x, y):
+            if out is not None:
+                check(lib().hhp_dot_dev(self._h, n, _ptr(x), _ptr(y), _ptr(out)), "hhp_dot_dev")
+                return out
+            r = ctypes.c_double()
+            check(lib().hhp_dot(self._h, n, _ptr(x), _ptr(y), ctypes.byref(r)), "hhp_dot")
         return r.value
 
     def axpy(self, alpha: float, x, y):
-        check(lib().hhp_axpy_dev(self._h, int(x.numel()), float(alpha), _ptr(x), _ptr(y)), "hhp_axpy_dev")
+        with _Ordered(self, x, y):
+            check(lib().hhp_axpy_dev(self._h, int(x.numel()), float(alpha), _ptr(x), _ptr(y)), "hhp_axpy_dev")
         return y
 
     def scal(self, alpha: float, x):
-        check(lib().hhp_scal_dev(self._h, int(x.numel()), float(alpha), _ptr(x)), "hhp_scal_dev")
+        with _Ordered(self, x):
+            check(lib().hhp_scal_dev(self._h, int(x.numel()), float(alpha), _ptr(x)), "hhp_scal_dev")
         return x
 
     def copy(self, src, dst):
-        check(lib().hhp_copy_dev(self._h, int(src.numel()), _ptr(src), _ptr(dst)), "hhp_copy_dev")
+        with _Ordered(self, src, dst):
+            check(lib().hhp_copy_dev(self._h, int(src.numel()), _ptr(src), _ptr(dst)), "hhp_copy_dev")
         return dst
 
     def close(self):
@@ -190,13 +217,16 @@ class Matrix:
 
     def spmv_dev(self, x, y, alpha: float = 1.0, beta: float = 0.0):
         """y = alpha A x + beta y on device tensors, on the context's stream (asynchronous)."""
-        check(lib().hhp_spmv_dev(self.ctx.handle, self._h, alpha, _ptr(x), beta, _ptr(y)), "hhp_spmv_dev")
+        with _Ordered(self.ctx, x, y):
+            check(lib().hhp_spmv_dev(self.ctx.handle, self._h, alpha, _ptr(x), beta, _ptr(y)), "hhp_spmv_dev")
 
     def spmv_f32_dev(self, x, y):
-        check(lib().hhp_spmv_f32_dev(self.ctx.handle, self._h, _ptr(x), _ptr(y)), "hhp_spmv_f32_dev")
+        with _Ordered(self.ctx, x, y):
+            check(lib().hhp_spmv_f32_dev(self.ctx.handle, self._h, _ptr(x), _ptr(y)), "hhp_spmv_f32_dev")
 
     def spmv_t_dev(self, x, y):
-        check(lib().hhp_spmv_t_dev(self.ctx.handle, self._h, _ptr(x), _ptr(y)), "hhp_spmv_t_dev")
+        with _Ordered(self.ctx, x, y):
+            check(lib().hhp_spmv_t_dev(self.ctx.handle, self._h, _ptr(x), _ptr(y)), "hhp_spmv_t_dev")
 
 
 @dataclass
@@ -267,8 +297,9 @@ def bicgstab(ctx: Context, A: Matrix, b, x=None, x_target=None, *, rtol: float =
         import torch
         if x is None:
             x = torch.zeros_like(b)
-        st = lib().hhp_bicgstab_dev(ctx.handle, A.handle, _ptr(b), _ptr(x), _ptr(x_target), ctypes.byref(o),
-                                    ctypes.byref(info))
+        with _Ordered(ctx, b, x):
+            st = lib().hhp_bicgstab_dev(ctx.handle, A.handle, _ptr(b), _ptr(x), _ptr(x_target), ctypes.byref(o),
+                                        ctypes.byref(info))
         out = x
     else:
         bv = _host(b, np.float64)
@@ -298,8 +329,9 @@ def bicgstab_backward(ctx: Context, A: Matrix, x, dldx, *, rtol: float = 1e-12, 
         import torch
         dldb = torch.empty_like(x)
         dlda = torch.empty(A.nnz, dtype=torch.float64, device=x.device) if want_dlda else None
-        st = lib().hhp_bicgstab_backward_dev(ctx.handle, A.handle, _ptr(x), _ptr(dldx), _ptr(dldb), _ptr(dlda),
-                                             ctypes.byref(o), ctypes.byref(info))
+        with _Ordered(ctx, x, dldx):
+            st = lib().hhp_bicgstab_backward_dev(ctx.handle, A.handle, _ptr(x), _ptr(dldx), _ptr(dldb), _ptr(dlda),
+                                                 ctypes.byref(o), ctypes.byref(info))
     else:
         xv, gv = _host(x, np.float64), _host(dldx, np.float64)
         dldb = np.empty(A.shape[0], np.float64)

@@ -110,6 +110,8 @@ int main(int argc, char **argv) {
     CHECK_CUDA(cudaMalloc((void **)&yd, sizeof(double) * (size_t)(m > 0 ? m : 1)));
     CHECK_CUDA(cudaMemcpy(xd, xh, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice));
     CHECK_CUDA(cudaMemset(yd, 0, sizeof(double) * (size_t)(m > 0 ? m : 1)));
+    /* the library works on its own non-blocking stream: the copies above must have landed */
+    CHECK_CUDA(cudaDeviceSynchronize());
     const double t_read1 = now_s();
     printf("Matrix name : %s\n", a.input_matrix);
 
