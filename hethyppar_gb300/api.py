@@ -157,8 +157,9 @@ class Matrix:
     @classmethod
     def from_csr_dev(cls, ctx: Context, m: int, n: int, rowptr, col, val) -> "Matrix":
         h = ctypes.c_void_p()
-        check(lib().hhp_mat_from_csr_dev(ctx.handle, m, n, int(col.numel()), _ptr(rowptr), _ptr(col), _ptr(val),
-                                         ctypes.byref(h)), "hhp_mat_from_csr_dev")
+        with _Ordered(ctx, rowptr, col, val):  # the arrays torch is still writing are complete first
+            check(lib().hhp_mat_from_csr_dev(ctx.handle, m, n, int(col.numel()), _ptr(rowptr), _ptr(col),
+                                             _ptr(val), ctypes.byref(h)), "hhp_mat_from_csr_dev")
         return cls(ctx, h)
 
     @classmethod
@@ -186,7 +187,8 @@ class Matrix:
 
     def set_values(self, val):
         if _is_dev(val):
-            check(lib().hhp_mat_set_values_dev(self._h, _ptr(val)), "hhp_mat_set_values_dev")
+            with _Ordered(self.ctx, val):  # values torch is still writing are complete first
+                check(lib().hhp_mat_set_values_dev(self._h, _ptr(val)), "hhp_mat_set_values_dev")
         else:
             v = _host(val, np.float64)
             check(lib().hhp_mat_set_values(self._h, _ptr(v)), "hhp_mat_set_values")

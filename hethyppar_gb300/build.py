@@ -22,7 +22,9 @@ CLI_BIN = os.path.join(PKG, "bin", "hhp-bicgstab")
 SPMV_CLI_SRC = os.path.join(PKG, "cli", "hhp_spmv.c")
 SPMV_CLI_BIN = os.path.join(PKG, "bin", "hhp-spmv")
 ORACLE_DIR = os.path.join(ROOT, "oracle")
-REFERENCE_DIR = "/root/reference"
+# A HetHypPar source tree to build the reference itself from (oracle/_ref): named by the
+# HHP_REFERENCE_DIR environment variable; without it only the C restatement is built.
+REFERENCE_DIR = os.environ.get("HHP_REFERENCE_DIR", "")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-pthread", "-I" + INCLUDE]
@@ -118,7 +120,7 @@ def build_oracle() -> str:
     """The oracle (test infrastructure): the C restatement everywhere, and the reference built
     from its own sources into oracle/_ref where those sources exist."""
     _run(["make", "-s", "-B", "-C", ORACLE_DIR, "liboracle.so", f"CUDA_HOME={_cuda_home()}"])
-    if os.path.isdir(os.path.join(REFERENCE_DIR, "src")):
+    if REFERENCE_DIR and os.path.isdir(os.path.join(REFERENCE_DIR, "src")):
         _run(["make", "-s", "-C", ORACLE_DIR, "ref", f"REF={REFERENCE_DIR}", f"CUDA_HOME={_cuda_home()}"])
     return os.path.join(ORACLE_DIR, "liboracle.so")
 

@@ -39,9 +39,12 @@ int env_int(const char *name, int dflt) {
     return static_cast<int>(std::min<long>(std::max<long>(x, -(1L << 30)), 1L << 30));
 }
 
+// The per-matrix choices below are the library's; the environment overrides exist for kernel
+// sweeps and are read only when HHP_TUNING=1 (otherwise the environment is ignored).
 const Tuning &tuning() {
     static const Tuning t = [] {
         Tuning d;
+        if (env_int("HHP_TUNING", 0) != 1) return d;
         d.cap = env_int("HHP_SPMV_CHUNK", d.cap);
         d.long_thr = env_int("HHP_SPMV_LONG", d.long_thr);
         d.window = env_int("HHP_SPMV_WINDOW", d.window);

@@ -171,32 +171,57 @@ def powerlaw(m: int = 3_500_000, a: float = 2.1, max_len: int = 100_000, n_dense
              dense_lo: int = 50_000, dense_hi: int = 100_000, dom: float = 1.1, seed: int = 2) -> System:
     """Off-diagonal row lengths ~ Zipf(a) clipped to [1, max_len]; n_dense rows get
     U[dense_lo, dense_hi] entries; distinct uniform random columns (never the diagonal);
-    off-diagonals ~ N(0,1); diagonal = dom * sum|off|; b = A 1."""
+    off-diagonals ~ N(0,1); diagonal = dom * sum|off|; b = A 1.
+
+    Columns are drawn per row, sorted, and every duplicate or diagonal column is redrawn (in
+    position order) until none is left; after the first pass only the rows that had a redraw are
+    sorted again. The diagonal is then inserted at its sorted place in each row."""
     rng = np.random.default_rng(seed)
     lens = np.minimum(rng.zipf(a, size=m), max_len).astype(np.int64)
     dense_rows = rng.choice(m, size=n_dense, replace=False)
     lens[dense_rows] = rng.integers(dense_lo, dense_hi + 1, size=n_dense)
     lens = np.minimum(lens, m - 1)
+    start = np.zeros(m + 1, np.int64)
+    np.cumsum(lens, out=start[1:])
+    nnz = int(start[-1])
     rows = np.repeat(np.arange(m, dtype=np.int64), lens)
-    cols = rng.integers(0, m, size=rows.size, dtype=np.int64)
+    cols = rng.integers(0, m, size=nnz, dtype=np.int64)
+    seg = None  # positions of the rows that can still hold a bad column (None: every position)
     for _ in range(100):
-        order = np.lexsort((cols, rows))
-        rows, cols = rows[order], cols[order]
-        dup = np.zeros(rows.size, bool)
-        dup[1:] = (rows[1:] == rows[:-1]) & (cols[1:] == cols[:-1])
-        bad = dup | (cols == rows)
+        # stable sort by (row, column); rows are already in order, so only columns move
+        if seg is None:
+            cols = cols[np.argsort(rows * m + cols, kind="stable")]
+            r, c = rows, cols
+        else:
+            cols[seg] = cols[seg][np.argsort(rows[seg] * m + cols[seg], kind="stable")]
+            r, c = rows[seg], cols[seg]
+        dup = np.zeros(r.size, bool)
+        dup[1:] = (r[1:] == r[:-1]) & (c[1:] == c[:-1])
+        bad = dup | (c == r)
         nb = int(bad.sum())
         if nb == 0:
             break
-        cols[bad] = rng.integers(0, m, size=nb, dtype=np.int64)
+        pos = np.nonzero(bad)[0] if seg is None else seg[bad]
+        cols[pos] = rng.integers(0, m, size=nb, dtype=np.int64)
+        aff = np.unique(rows[pos])
+        ln = lens[aff]
+        seg = np.repeat(start[aff] - np.concatenate([[0], np.cumsum(ln)[:-1]]), ln) + np.arange(int(ln.sum()))
     else:
         raise RuntimeError("powerlaw: could not draw distinct columns")
-    vals = rng.standard_normal(rows.size)
+    vals = rng.standard_normal(nnz)
     offsum = np.bincount(rows, weights=np.abs(vals), minlength=m)
-    rows = np.concatenate([rows, np.arange(m, dtype=np.int64)])
-    cols = np.concatenate([cols, np.arange(m, dtype=np.int64)])
-    vals = np.concatenate([vals, dom * offsum])
-    rp, col, val = _from_coo_sorted(m, rows, cols, vals)
+    # CSR with the diagonal in its sorted place: off-diagonal k of row r moves r places right
+    # (one diagonal per earlier row), one more if it lies right of the diagonal
+    below = np.bincount(rows, weights=(cols < rows), minlength=m).astype(np.int64)
+    dst = np.arange(nnz, dtype=np.int64) + rows + (cols > rows)
+    dpos = start[:-1] + np.arange(m, dtype=np.int64) + below
+    col = np.empty(nnz + m, np.int32)
+    val = np.empty(nnz + m, np.float64)
+    col[dst] = cols
+    val[dst] = vals
+    col[dpos] = np.arange(m, dtype=np.int32)
+    val[dpos] = dom * offsum
+    rp = (start + np.arange(m + 1, dtype=np.int64)).astype(np.int32)
     ones = np.ones(m)
     b = csr_matvec(rp, col, val, ones)
     return System(f"powerlaw_{m}", rp, col, val, b, np.zeros(m), ones)

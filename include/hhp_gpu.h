@@ -242,7 +242,10 @@ void hhp_dp_update_omega(double *omega, double *neg_omega, const double *ts, con
  * stream) of the current device. The first call on a device looks up the scratch array's address
  * there: make it before any stream capture. Calls share that array, so calls that overlap on one
  * GPU race and give wrong results; serialise them. Rows split between CTAs are summed in another
- * order than hhp_spmv_dev, so results agree to rounding, not bit for bit. */
+ * order than hhp_spmv_dev, so results agree to rounding, not bit for bit.
+ * Preconditions, NOT checked (checking them would need a device-to-host copy): rowptr[0] == 0,
+ * rowptr[m] == nnz, rowptr non-decreasing, and 0 <= col[k] < n for every k. A CSR that breaks
+ * them gives wrong results (a row past the end is never finished) or out-of-range reads. */
 hhp_status hhp_spmv_csr_noalloc(int m, int n, int nnz, const int *rowptr_dev, const int *col_dev,
                                 const double *val_dev, double alpha, const double *x_dev, double beta,
                                 double *y_dev, void *stream);

@@ -1,9 +1,9 @@
 """Generates the golden fixtures in tests/golden/ from the REFERENCE ITSELF.
 
-Run in the container that holds the HetHypPar sources (default /root/reference), after
-``make -C oracle ref`` has compiled them into oracle/_ref:
+Run where the HetHypPar sources are, after ``make -C oracle ref REF=<source tree>`` has compiled
+them into oracle/_ref:
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <source tree>     (or HHP_REFERENCE_DIR=<source tree>)
 
 Sources of truth, all executed here from the reference's own code:
   * oracle/_ref/libhhpref.so -- the reference's CPU functions (buReadSparseMatrix, CSR_spmxv_seq,
@@ -227,8 +227,11 @@ def crafted_case():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("HHP_REFERENCE_DIR", ""),
+                    help="the HetHypPar source tree (default: $HHP_REFERENCE_DIR)")
     a = ap.parse_args()
+    if not a.ref or not os.path.isdir(os.path.join(a.ref, "data")):
+        sys.exit("name the HetHypPar source tree with --ref or HHP_REFERENCE_DIR")
     if not orc.ref_available():
         sys.exit("oracle/_ref/libhhpref.so missing: run `make -C oracle ref` first")
     crafted_case()

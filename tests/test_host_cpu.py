@@ -276,13 +276,20 @@ def test_tuning_overrides_out_of_range_are_clamped():
             "np.add.at(placed, np.unique(ch[:, 0]) if ch.size else np.zeros(0, np.int64), 1)\n"
             "assert np.all(placed == 1)\n"
             "print(st['long_rows'], st['slices'])\n")
-    env = dict(os.environ, HHP_SPMV_WINDOW="0", HHP_SPMV_LONG="-5", HHP_SPMV_CHUNK="0", HHP_SPMV_WPC="99",
-               HHP_SPMV_RPL32="3", HHP_UNROLL_ITERS="99999999999")
+    env = dict(os.environ, HHP_TUNING="1", HHP_SPMV_WINDOW="0", HHP_SPMV_LONG="-5", HHP_SPMV_CHUNK="0",
+               HHP_SPMV_WPC="99", HHP_SPMV_RPL32="3", HHP_UNROLL_ITERS="99999999999")
     r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, env=env, stdout=subprocess.PIPE,
                        stderr=subprocess.PIPE, text=True, timeout=120)
     assert r.returncode == 0, r.stderr[-2000:]
     long_rows, slices = map(int, r.stdout.split())
     assert long_rows > 0 and slices >= 0  # threshold clamped to 1: every row with 2+ entries is long
+    # without the tuning switch the same environment is ignored: only rows above 256 are long
+    env.pop("HHP_TUNING")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, env=env, stdout=subprocess.PIPE,
+                       stderr=subprocess.PIPE, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr[-2000:]
+    long_default, _ = map(int, r.stdout.split())
+    assert 0 < long_default < long_rows
 
 
 def test_host_allocation_failure_is_a_status_not_a_crash():

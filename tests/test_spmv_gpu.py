@@ -153,3 +153,33 @@ def test_spmv_repeatable(ctx):
     ys = [gpu_spmv(ctx, A, x) for _ in range(3)]
     assert np.array_equal(ys[0], ys[1]) and np.array_equal(ys[1], ys[2])
     assert np.array_equal(A.spmv(x), ys[0])  # host-buffer entry point
+
+
+def test_device_inputs_written_by_torch_on_a_side_stream(ctx):
+    # Values and CSR arrays that torch is still writing on its current stream (a side stream,
+    # behind a slow kernel) are complete before the library reads them: set_values and
+    # from_csr_dev order themselves after torch's queued work.
+    s = synth.config("c1")
+    x = np.random.default_rng(3).standard_normal(s.n)
+    src_val = dev(2.0 * s.val)
+    src_rp, src_col = dev(s.rowptr, torch.int32), dev(s.col, torch.int32)
+    slow = torch.randn(4096, 4096, device="cuda")
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
+    with torch.cuda.stream(side):
+        val_d = torch.zeros(s.nnz, dtype=torch.float64, device="cuda")
+        rp_d = torch.zeros(s.m + 1, dtype=torch.int32, device="cuda")
+        col_d = torch.zeros(s.nnz, dtype=torch.int32, device="cuda")
+        for _ in range(8):
+            slow = slow @ slow * 1e-3
+        val_d.copy_(src_val)
+        rp_d.copy_(src_rp)
+        col_d.copy_(src_col)
+        A.set_values(val_d)
+        B = Matrix.from_csr_dev(ctx, s.m, s.n, rp_d, col_d, val_d)
+    y_ref = orc.spmv(s.rowptr, s.col, 2.0 * s.val, x, fma=True)
+    assert np.array_equal(A.spmv(x), y_ref)
+    assert np.array_equal(B.spmv(x), y_ref)
+    A.close()
+    B.close()

@@ -3,7 +3,7 @@
 Some callers own all device memory themselves (a host application with a fixed memory budget) or
 run between stream operations where cudaMalloc's implicit device synchronisation is not allowed;
 this entry point takes their raw device CSR arrays and uses only a scratch array built into the
-library. Checked here through the C ABI against hhp_spmv_dev on the same inputs, on two different
+library. Checked here through the C ABI against hhp_spmv_dev and the oracle on the same inputs, on two different
 calls in a row (the second call finds the first one's partial sums left in the shared scratch), and
 for its size limit. This file is collected last on purpose."""
 import ctypes
@@ -46,6 +46,10 @@ def _case(ctx, rp, col, val, n, alpha, beta, seed):
     # the rounding of the final alpha*s + beta*y
     tol = 2.0 * abs(alpha) * spmv_tolerance(rp, col, val, x) + 4.5e-16 * (abs(alpha) * absrow + abs(beta * y0))
     err = np.abs(y - y_ref)
+    assert np.all(err <= tol), (np.max(err / tol), int(np.argmax(err / tol)))
+    # and against the oracle (CSR_spmxv_seq's row order, then alpha*s + beta*y on the host)
+    y_orc = alpha * orc.spmv(rp, col, val, x) + beta * y0
+    err = np.abs(y - y_orc)
     assert np.all(err <= tol), (np.max(err / tol), int(np.argmax(err / tol)))
     return y
 
