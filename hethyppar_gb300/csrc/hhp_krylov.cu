@@ -260,7 +260,9 @@ template <typename T>
 __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const T *R, int nu, const double *part_xr,
                                            const double *part_s, int nparts, double *hist, int hist_cap,
                                            cudaGraphConditionalHandle cond, int first_in_body, const int *dev_err,
-                                           int use_cond) {
+                                           int use_cond, const int *gate = nullptr) {
+    // gate (direct launches of the mixed form): run only when the iteration made an FP64 update
+    if (gate && *reinterpret_cast<volatile const int *>(gate) == 0) return;
     const bool dead = dead_step(sc);  // tested after the operand and record loads are in flight
     // scalars written by earlier launches, read with the operand loads (off the critical path)
     const int iter = sc->iter, it0 = sc->iter_start, maxit = sc->maxit,
@@ -846,12 +848,15 @@ __global__ void __launch_bounds__(512) k_p_ru(DevScal *sc, double *X, float *D32
                                               const float *R, int nu4, const double *part_xr,
                                               const double *part_s, int nparts, double *hist, int hist_cap,
                                               cudaGraphConditionalHandle wcond, cudaGraphConditionalHandle icond,
-                                              int first_in_body, const int *dev_err) {
+                                              int first_in_body, const int *dev_err, int use_cond) {
     if (dead_step(sc)) {
         if (b0t0()) {
             if (first_in_body) sc->bodies += 1;
-            cudaGraphSetConditional(icond, 0u);
-            cudaGraphSetConditional(wcond, 0);
+            sc->ru_flag = 0;
+            if (use_cond) {
+                cudaGraphSetConditional(icond, 0u);
+                cudaGraphSetConditional(wcond, 0);
+            }
         }
         return;
     }
@@ -872,10 +877,7 @@ __global__ void __launch_bounds__(512) k_p_ru(DevScal *sc, double *X, float *D32
             if (!isfinite(rr) || rr > kDivergence2 * sc->true_rr) {
                 if (lead) sc->status = ST_BREAKDOWN;  // d is not folded into x
             } else if (rr <= sc->thr2 || rr < sc->inner_rtol2 * mx || it >= sc->maxit) {
-                if (lead) {
-                    sc->rr_max[(it + 1) & 1] = mx;
-                    sc->ru_flag = 1;
-                }
+                if (lead) sc->rr_max[(it + 1) & 1] = mx;
                 what = 2;
             } else {
                 if (lead) sc->rr_max[(it + 1) & 1] = fmax(mx, rr);
@@ -903,8 +905,11 @@ __global__ void __launch_bounds__(512) k_p_ru(DevScal *sc, double *X, float *D32
             }
         }
         if (lead) {
-            cudaGraphSetConditional(icond, what == 2 ? 1u : 0u);
-            if (what == 0) cudaGraphSetConditional(wcond, 0);
+            sc->ru_flag = what == 2 ? 1 : 0;  // this iteration's update decision
+            if (use_cond) {
+                cudaGraphSetConditional(icond, what == 2 ? 1u : 0u);
+                if (what == 0) cudaGraphSetConditional(wcond, 0);
+            }
         }
         go = what;
     }
@@ -948,7 +953,7 @@ __global__ void __launch_bounds__(512) k_xrp_ru(DevScal *sc, double *X, float *D
                                                 const float *Tv, const float *V, int nu4, SpmvParts sp,
                                                 const double *part_s, int nparts, double *hist, int hist_cap,
                                                 cudaGraphConditionalHandle wcond, cudaGraphConditionalHandle icond,
-                                                int first_in_body, const int *dev_err) {
+                                                int first_in_body, const int *dev_err, int use_cond) {
     const bool dead = dead_step(sc);  // tested after the operand and record loads are in flight
     // scalars written by earlier launches, read with the operand loads (off the critical path)
     const int it = sc->iter, it0 = sc->iter_start, maxit = sc->maxit,
@@ -976,8 +981,11 @@ __global__ void __launch_bounds__(512) k_xrp_ru(DevScal *sc, double *X, float *D
     if (dead) {
         if (b0t0()) {
             if (first_in_body) sc->bodies += 1;
-            cudaGraphSetConditional(icond, 0u);
-            cudaGraphSetConditional(wcond, 0);
+            sc->ru_flag = 0;
+            if (use_cond) {
+                cudaGraphSetConditional(icond, 0u);
+                cudaGraphSetConditional(wcond, 0);
+            }
         }
         return;
     }
@@ -1001,10 +1009,7 @@ __global__ void __launch_bounds__(512) k_xrp_ru(DevScal *sc, double *X, float *D
                 if (!isfinite(rr) || rr > kDivergence2 * true_rr) {
                     term = ST_BREAKDOWN;  // d is not folded into x
                 } else if (rr <= thr2 || rr < inner2 * mx || it >= maxit) {
-                    if (lead) {
-                        sc->rr_max[(it + 1) & 1] = mx;
-                        sc->ru_flag = 1;
-                    }
+                    if (lead) sc->rr_max[(it + 1) & 1] = mx;
                     what = 2;
                 } else {
                     if (lead) sc->rr_max[(it + 1) & 1] = fmax(mx, rr);
@@ -1032,8 +1037,11 @@ __global__ void __launch_bounds__(512) k_xrp_ru(DevScal *sc, double *X, float *D
             if (term != ST_RUNNING && what == 0) sc->status = term;
         }
         if (lead) {
-            cudaGraphSetConditional(icond, what == 2 ? 1u : 0u);
-            if (what == 0) cudaGraphSetConditional(wcond, 0);
+            sc->ru_flag = what == 2 ? 1 : 0;  // this iteration's update decision
+            if (use_cond) {
+                cudaGraphSetConditional(icond, what == 2 ? 1u : 0u);
+                if (what == 0) cudaGraphSetConditional(wcond, 0);
+            }
         }
         go = what;
     }
@@ -1350,7 +1358,8 @@ hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R,
     hhp_status st = HHP_OK;
     auto kp = [&](cudaStream_t q, cudaGraphConditionalHandle c, int first_in_body) -> hhp_status {
         HHP_CUDA(launch_k(k_p<T>, dim3(s->nblk), dim3(s->nthr), 0, q, sc, P, V, R, nu, part_xr, part_s, s->nblk,
-                          s->hist, s->hist_cap, c, first_in_body, A->ctx->dev_err, 1));
+                          s->hist, s->hist_cap, c, first_in_body, A->ctx->dev_err, 1,
+                          static_cast<const int *>(nullptr)));
         return HHP_OK;
     };
     cudaGraphConditionalHandle cond;
@@ -1392,7 +1401,7 @@ hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R,
             if (st != HHP_OK) break;
             if (launch_k(k_xrp_ru, dim3(s->nblk), dim3(s->nthr), 0, s->s2, s->sc32, s->X, s->D32, s->R32, s->P32,
                          s->S32, s->T32, s->V32, nu4, parts_of(pl), part_s, s->nblk, s->hist, s->hist_cap, cond,
-                         icond, k == 0 ? 1 : 0, A->ctx->dev_err) != cudaSuccess) {
+                         icond, k == 0 ? 1 : 0, A->ctx->dev_err, 1) != cudaSuccess) {
                 st = HHP_ERR_CUDA;
                 break;
             }
@@ -1443,7 +1452,7 @@ hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R,
         if (st != HHP_OK) break;
         if (launch_k(k_p_ru, dim3(s->nblk), dim3(s->nthr), 0, s->s2, s->sc32, s->X, s->D32, s->P32, s->V32, s->R32,
                      nu4, s->part_xr32, s->part_s32, s->nblk, s->hist, s->hist_cap, cond, icond, k == 0 ? 1 : 0,
-                     A->ctx->dev_err) != cudaSuccess) {
+                     A->ctx->dev_err, 1) != cudaSuccess) {
             st = HHP_ERR_CUDA;
             break;
         }
@@ -1486,7 +1495,7 @@ hhp_status run_direct64(Solver *s, bool merged) {
     auto kp = [&](int first) -> hhp_status {
         HHP_CUDA(launch_k(k_p<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->P, s->V, s->R, nu, s->part_xr,
                           s->part_s, s->nblk, s->hist, s->hist_cap, cudaGraphConditionalHandle(), first,
-                          A->ctx->dev_err, 0));
+                          A->ctx->dev_err, 0, static_cast<const int *>(nullptr)));
         A->ctx->kernel_launches += 1;
         return HHP_OK;
     };
@@ -1616,6 +1625,81 @@ hhp_status build_gmix(Solver *s, bool merged) {
     s->gmix_kernels_epi = 3;
     // launch_spmv* counted their captured launches; graph launches are counted when executed.
     A->ctx->kernel_launches -= 2 + 3 * s->unroll;
+    return HHP_OK;
+}
+
+// The mixed-form loop launched kernel by kernel (no graph; HHP_SOLVE_GRAPH=0, for profilers that
+// cannot see inside conditional graph nodes): the kernels of build_gmix in the same order. Each
+// iteration's update kernel records its decision in ru_flag, and the IF body's kernels (FP64
+// residual SpMV, residual replacement, K_P) are gated on it instead of on the IF node; the host
+// reads the status every `unroll` iterations.
+hhp_status run_direct_mix(Solver *s, bool merged) {
+    hhp_mat *A = s->A;
+    cudaStream_t st = A->ctx->stream;
+    HHP_TRY(ensure_plan(A, false));
+    HHP_TRY(ensure_plan(A, true));
+    const int nu4 = s->n_pad / 4;
+    const int *stop = &s->sc32->status;
+    const int *upd = &s->sc32->ru_flag;
+    const PlanDev &pl = A->plan32;
+    const cudaGraphConditionalHandle none = cudaGraphConditionalHandle();
+    long long &nk = A->ctx->kernel_launches;
+    HHP_CUDA(cudaMemcpyAsync(s->sc32, s->h_sc32, kCtlBytes, cudaMemcpyHostToDevice, st));
+    HHP_TRY(launch_x0check(s, st));
+    HHP_TRY(launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0, s->x0_nz));
+    HHP_CUDA(launch_k(k_mix_init, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc32, s->Y, s->B, s->R32, s->R0_32, s->D32,
+                      s->P32, s->V32, nu4, parts_of(A->plan64), s->x0_nz, s->part_b, s->nblk, s->part_xr32,
+                      s->part_s32));
+    nk += 2;
+    auto kp = [&](int first, const int *gate) -> hhp_status {
+        HHP_CUDA(launch_k(k_p<float>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc32, s->P32, s->V32, s->R32, nu4,
+                          s->part_xr32, s->part_s32, s->nblk, s->hist, s->hist_cap, none, first, A->ctx->dev_err, 0,
+                          gate));
+        nk += 1;
+        return HHP_OK;
+    };
+    // IF(update) { FP64 residual, residual replacement, K_P }, each gated on this iteration's flag
+    auto update_body = [&]() -> hhp_status {
+        HHP_TRY(launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0, upd));
+        HHP_CUDA(launch_k(k_ru_apply, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc32, s->Y, s->R32, s->R0_32, nu4,
+                          parts_of(A->plan64), s->part_xr32));
+        nk += 1;
+        return kp(0, upd);
+    };
+    HHP_TRY(kp(0, nullptr));  // stop tests on the initial residual
+    for (;;) {
+        for (int k = 0; k < s->unroll; ++k) {
+            HHP_TRY(launch_spmv32(A, st, EP_DOT1, s->P32, s->V32, s->R0_32, stop));
+            if (merged) {
+                HHP_CUDA(launch_k(k_s<float, true>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc32, s->S32, s->R32,
+                                  s->V32, s->R0_32, nu4, parts_of(pl), s->part_s32));
+                HHP_TRY(launch_spmv32(A, st, EP_DOT3, s->S32, s->T32, s->S32, stop, s->R0_32));
+                HHP_CUDA(launch_k(k_xrp_ru, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc32, s->X, s->D32, s->R32,
+                                  s->P32, s->S32, s->T32, s->V32, nu4, parts_of(pl), s->part_s32, s->nblk, s->hist,
+                                  s->hist_cap, none, none, k == 0 ? 1 : 0, A->ctx->dev_err, 0));
+            } else {
+                HHP_CUDA(launch_k(k_s<float>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc32, s->S32, s->R32, s->V32,
+                                  s->R0_32, nu4, parts_of(pl), s->part_s32));
+                HHP_TRY(launch_spmv32(A, st, EP_DOT2, s->S32, s->T32, s->S32, stop));
+                HHP_CUDA(launch_k(k_xr<float>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc32, s->D32, s->R32, s->P32,
+                                  s->S32, s->T32, s->R0_32, nu4, parts_of(pl), s->part_s32, s->nblk, s->part_xr32));
+                nk += 1;
+                HHP_CUDA(launch_k(k_p_ru, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc32, s->X, s->D32, s->P32, s->V32,
+                                  s->R32, nu4, s->part_xr32, s->part_s32, s->nblk, s->hist, s->hist_cap, none, none,
+                                  k == 0 ? 1 : 0, A->ctx->dev_err, 0));
+            }
+            nk += 2;
+            HHP_TRY(update_body());
+        }
+        HHP_CUDA(cudaMemcpyAsync(s->h_sc32, s->sc32, sizeof(DevScal), cudaMemcpyDeviceToHost, st));
+        HHP_CUDA(cudaStreamSynchronize(st));
+        if (s->h_sc32->status != ST_RUNNING) break;
+    }
+    HHP_CUDA(launch_k(k_mix_final, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc32, s->X, s->D32, nu4));
+    HHP_TRY(launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0));
+    HHP_CUDA(launch_k(k_finish, dim3(1), dim3(32), 0, st, s->sc32, parts_of(A->plan64)));
+    nk += 2;
+    HHP_CUDA(cudaGetLastError());
     return HHP_OK;
 }
 
@@ -1762,8 +1846,9 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
         HHP_TRY(fp64_passes(0));
     } else {
         const bool merged32 = o->loop != HHP_LOOP_CLASSIC;
+        const bool use_graph = env_int("HHP_SOLVE_GRAPH", 1) != 0;
         cudaGraphExec_t &gm = merged32 ? s->gmixm : s->gmix;
-        if (!gm) HHP_TRY(build_gmix(s, merged32));
+        if (use_graph && !gm) HHP_TRY(build_gmix(s, merged32));
         DevScal &h32 = *s->h_sc32;
         h32.rtol2 = o->rtol * o->rtol;
         const double delta = o->inner_rtol > 0.0 ? o->inner_rtol : 0.1;
@@ -1774,11 +1859,16 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
         for (int pass = 0; pass < 2; ++pass) {
             h32.restart = pass > 0 ? 1 : 0;
             const int upd0 = pass > 0 ? h32.updates : 0;
-            HHP_CUDA(cudaGraphLaunch(gm, st));
+            if (use_graph) {
+                HHP_CUDA(cudaGraphLaunch(gm, st));
+            } else {
+                HHP_TRY(run_direct_mix(s, merged32));
+            }
             HHP_TRY(readback(s->h_sc32, s->sc32));
             // 4 (merged) or 5 kernels per iteration, 3 more per FP64 update (the IF body)
-            ctx->kernel_launches += s->gmix_kernels_pro + s->gmix_kernels_epi +
-                                    (merged32 ? 4LL : 5LL) * s->unroll * h32.bodies + 3LL * (h32.updates - upd0);
+            if (use_graph)
+                ctx->kernel_launches += s->gmix_kernels_pro + s->gmix_kernels_epi +
+                                        (merged32 ? 4LL : 5LL) * s->unroll * h32.bodies + 3LL * (h32.updates - upd0);
             // an inner breakdown or divergence after some progress restarts the FP32 recurrences
             // once from the last FP64 iterate (its true residual becomes the new shadow
             // residual); a second one hands the solve to FP64 below

@@ -45,11 +45,27 @@ class System:
 
 
 def csr_matvec(rowptr: np.ndarray, col: np.ndarray, val: np.ndarray, x: np.ndarray) -> np.ndarray:
-    """y = A x (scipy's CSR kernel: each row summed in order)."""
-    import scipy.sparse as sp
+    """y = A x with every row summed in CSR order, each product and each sum rounded separately,
+    so that the result is the same on every machine (a compiled CSR kernel may contract the
+    multiply-adds into FMAs on one architecture and not on another, and the right-hand sides
+    b = A x_target must not depend on that). Rows are visited longest first: step k adds the k-th
+    entry of every row that has one."""
+    rowptr = np.asarray(rowptr, np.int64)
     m = rowptr.size - 1
-    A = sp.csr_matrix((val, col, rowptr), shape=(m, x.size))
-    return A @ x
+    lens = np.diff(rowptr)
+    order = np.argsort(-lens, kind="stable")
+    start = rowptr[:-1][order]
+    slen = lens[order]
+    acc = np.zeros(m)
+    active = m
+    for k in range(int(slen[0]) if m else 0):
+        while active > 0 and slen[active - 1] <= k:
+            active -= 1
+        idx = start[:active] + k
+        acc[:active] = acc[:active] + val[idx] * x[col[idx]]
+    y = np.empty(m)
+    y[order] = acc
+    return y
 
 
 def _from_coo_sorted(m: int, rows: np.ndarray, cols: np.ndarray, vals: np.ndarray):
@@ -130,7 +146,9 @@ def banded_random(m: int = 450_000, band: int = 64, n_band: int = 10, n_far: int
         cand = i + offs[None, :]
         key = rng.random(cand.shape, dtype=np.float32)
         key[(cand < 0) | (cand >= m)] = 2.0
-        pick = np.argpartition(key, n_band - 1, axis=1)[:, :n_band]
+        # the n_band smallest keys, in key order (a stable sort: the same columns in the same order
+        # on every machine, which a partial selection does not promise)
+        pick = np.argsort(key, axis=1, kind="stable")[:, :n_band]
         bc = np.take_along_axis(cand, pick, axis=1)
         # far columns: distinct, outside the band
         far = rng.integers(0, m, size=(r1 - r0, n_far), dtype=np.int64)

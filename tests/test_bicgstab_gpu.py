@@ -24,10 +24,8 @@ SOLVE_CASES = [n for n in golden_names() if n not in ("crafted5",)]
 
 
 def _within_5pct(k_gpu, k_ref):
-    """At most 5% (at least 1) more iterations than the reference needs for the same tolerance.
-    Fewer is allowed down to 80%: on ill-conditioned systems the rounding order (fused
-    multiply-adds, tree reductions) moves the count by a few percent either way."""
-    return 0.8 * k_ref - 1 <= k_gpu <= k_ref + max(1, math.ceil(0.05 * k_ref))
+    """Within 5% (at least 1) of the reference's iteration count for the same tolerance, either way."""
+    return abs(k_gpu - k_ref) <= max(1, math.ceil(0.05 * k_ref))
 
 
 @pytest.mark.parametrize("name", SOLVE_CASES)
@@ -62,7 +60,7 @@ def test_iterations_to_tolerance_match_reference(ctx, name):
 
 
 @pytest.mark.parametrize("cfg", ["c1", "c2"])
-def test_full_size_configs_against_oracle(ctx, cfg):
+def test_full_size_configs_against_oracle_live(ctx, cfg):
     s = synth.config(cfg)
     k_ref, x_ref, rr_ref = orc.iters_to_tol(s.rowptr, s.col, s.val, s.b, s.x0, 1e-10, 3000)
     assert k_ref > 0
@@ -354,3 +352,20 @@ def test_random_systems_all_schedules(ctx, seed):
         if prec == "fp64" and k_ref > 0:
             assert _within_5pct(r.iters, k_ref) or r.iters <= k_ref + 2, (loop, r.iters, k_ref)
     A.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("loop", ["merged", "classic"])
+def test_direct_launches_match_the_graph(ctx, monkeypatch, loop, precision):
+    # HHP_SOLVE_GRAPH=0 launches the loop's kernels one by one (profilers cannot see inside
+    # conditional graph nodes): the same kernels in the same order, so the same bits
+    s = synth.convdiff2d(48, 20.0, (1.0, 0.5), seed=3)
+    A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
+    xg, rg = bicgstab(ctx, A, s.b, s.x0, rtol=1e-10, maxit=2000, loop=loop, precision=precision)
+    monkeypatch.setenv("HHP_SOLVE_GRAPH", "0")
+    xd, rd = bicgstab(ctx, A, s.b, s.x0, rtol=1e-10, maxit=2000, loop=loop, precision=precision)
+    monkeypatch.delenv("HHP_SOLVE_GRAPH")
+    A.close()
+    assert rg.status == 0 and rd.status == 0
+    assert rd.iters == rg.iters and rd.outer_iters == rg.outer_iters
+    assert np.array_equal(xd, xg)
