@@ -285,19 +285,112 @@ def run_reference_arm(args, rk):
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
-def traffic_from_profile():
-    """DRAM bytes (read + write) of one C2 SpMV launch, from the committed ncu summary of the same
-    kernel on the same workload (captured at full size: one launch holds ~0.2 GB)."""
-    p = os.path.join(ROOT, "profiles", "k_spmv_fp64_banded450k.md")
-    if not os.path.exists(p):
-        return None
-    for line in open(p):
-        if line.startswith("traffic_bytes_per_launch:"):
-            try:
-                return float(line.split(":", 1)[1].strip())
-            except ValueError:
-                return None
-    return None
+def _event_ms(stream, fn, flush_l2, reps):
+    """Mean CUDA-event time of fn() on the library stream, L2 flushed before each rep."""
+    import torch
+    ts = []
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        flush_l2(sync=False)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return statistics.mean(ts)
+
+
+def spmv_other_configs(ctx, stream, flush_l2, hbm, fma_rate):
+    """The FP64 SpMV (y = A x, L2 flushed) on the other four systems: time, GB/s against the HBM
+    copy peak and the FP64 floor; on the power-law system (C3) also the merge-path split of the
+    allocation-free entry point (hhp_spmv_csr_noalloc: rows + nonzeros dealt evenly to CTAs) against
+    the library's sliced plan with long rows cut into 2048-nonzero chunks."""
+    import ctypes
+    import torch
+    from hethyppar_gb300 import Matrix, _lib, spmv_bytes, synth
+    res = {}
+    for cfg in ("c1", "c3", "c4", "c5"):
+        s = synth.config(cfg)
+        A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
+        x = torch.randn(s.n, dtype=torch.float64, device="cuda")
+        y = torch.empty(s.m, dtype=torch.float64, device="cuda")
+        for _ in range(3):
+            A.spmv_dev(x, y)
+        ms = _event_ms(stream, lambda: A.spmv_dev(x, y), flush_l2, 20)
+        nb = spmv_bytes(s.m, s.n, s.nnz)
+        r = {"m": s.m, "nnz": s.nnz, "us_l2_flushed": ms * 1e3, "gbs": nb / (ms * 1e-3) / 1e9,
+             "frac_of_hbm": nb / (ms * 1e-3) / 1e9 / hbm, "fp64_floor_us": s.nnz / fma_rate * 1e6,
+             "hbm_floor_us": nb / hbm / 1e3}
+        if cfg == "c3":
+            rp = torch.as_tensor(s.rowptr, device="cuda")
+            cl = torch.as_tensor(s.col, device="cuda")
+            vl = torch.as_tensor(s.val, device="cuda")
+            lib = _lib.lib()
+
+            def mp():
+                st = lib.hhp_spmv_csr_noalloc(s.m, s.n, s.nnz, rp.data_ptr(), cl.data_ptr(), vl.data_ptr(), 1.0,
+                                              x.data_ptr(), 0.0, y.data_ptr(), ctypes.c_void_p(ctx.stream))
+                assert st == 0
+            for _ in range(3):
+                mp()
+            ms_mp = _event_ms(stream, mp, flush_l2, 20)
+            r["merge_path_us_l2_flushed"] = ms_mp * 1e3
+            r["note"] = ("random columns over 3.5M rows: every x gather is a 32-byte L2 sector for 8 useful "
+                         "bytes, so the kernel is bound by L2 throughput, not HBM (ncu summary under profiles/); "
+                         "merge_path_us: the same product with an even merge-path split of rows + nonzeros "
+                         "over CTAs (the allocation-free entry point), against the sliced plan")
+            del rp, cl, vl
+        res[cfg] = r
+        A.close()
+        del x, y
+    return res
+
+
+def c1_solve(ctx, stream, flush_l2):
+    """C1 (2D 256^2 convection-diffusion, 65k rows): the launch-bound case, FP64 to 1e-10."""
+    import torch
+    from hethyppar_gb300 import Matrix, bicgstab, synth
+    s = synth.config("c1")
+    A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
+    b = torch.as_tensor(s.b, device="cuda")
+    x = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+    res = []
+
+    def run():
+        x.zero_()
+        res.append(bicgstab(ctx, A, b, x, rtol=RTOL, maxit=5000)[1])
+    run()
+    ms = _event_ms(stream, run, flush_l2, 5)
+    r = res[-1]
+    A.close()
+    return {"workload": "c1: 2D 5-point upwind convection-diffusion 256^2 (65,536 rows), Pe=50, FP64, rtol 1e-10",
+            "ms": ms, "iters": r.iters, "us_per_iter": ms * 1e3 / max(r.iters, 1), "rel_res_true": r.rel_res_true,
+            "status": r.status}
+
+
+def c3_fixed_iterations(ctx, stream, flush_l2, k=200):
+    """C3 (3.5M-row power law): unpreconditioned BiCGStab reaches neither 1e-10 here nor in the
+    reference (its diagonals span 1e-9 .. 9e4); time per iteration over k fixed iterations."""
+    import torch
+    from hethyppar_gb300 import Matrix, bicgstab, synth
+    s = synth.config("c3")
+    A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
+    b = torch.as_tensor(s.b, device="cuda")
+    x = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+    res = []
+
+    def run():
+        x.zero_()
+        res.append(bicgstab(ctx, A, b, x, rtol=0.0, maxit=k, fixed_iters=True)[1])
+    run()
+    ms = _event_ms(stream, run, flush_l2, 3)
+    r = res[-1]
+    A.close()
+    return {"workload": "c3: power-law 3.5M rows, 22.6M nnz, FP64, unpreconditioned", "fixed_iters": k, "ms": ms,
+            "us_per_iter": ms * 1e3 / k, "rel_res_true_after": r.rel_res_true,
+            "note": "fixed iterations (the reference's executables' mode, classic schedule): without "
+                    "preconditioning neither this library nor the reference reaches 1e-10 on C3"}
 
 
 def run_ours(args, rk):
@@ -493,10 +586,16 @@ def run_ours(args, rk):
     bsp = spmv_bytes(s.m, s.n, s.nnz)
     t_sp = statistics.mean(spmv_ms) * 1e-3  # mean: the event clock ticks in ~2 us steps
     achieved = bsp / t_sp / 1e9
-    traffic = traffic_from_profile()
+    fma_rate = ctx.fp64_fma_rate()  # measured FP64 FMA lanes per second of this device
     roof = {"bound": "hbm", "kernel": "k_spmv<double> (FP64 CSR SpMV)", "achieved": achieved, "peak": hbm,
-            "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": traffic,
+            "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": None,
+            "traffic_note": "DRAM bytes are counted by ncu, not by this run: see the ncu summary of this kernel "
+                            "on this workload under profiles/",
             "algorithmic_bytes_per_launch": bsp, "launch_us": t_sp * 1e6,
+            "fp64": {"fma_per_s_measured": fma_rate, "fmas_per_launch": s.nnz,
+                     "floor_us": s.nnz / fma_rate * 1e6, "frac_of_fp64_floor": s.nnz / fma_rate / t_sp,
+                     "note": "one FP64 FMA per nonzero; the FP64 pipe floor of the kernel beside its HBM floor "
+                             f"({bsp / hbm / 1e3:.2f} us)"},
             "note": "algorithmic bytes 12*nnz+20*m per launch / mean CUDA-event time over 30 launches, L2 flushed before each launch"}
 
     # one iteration against HBM: the minimum fused schedule moves 2 SpMVs + 16 vector passes; the
@@ -538,6 +637,9 @@ def run_ours(args, rk):
 
     # ---- extras: mixed vs FP64 (3D 160^3), forward + adjoint (2D 1024^2) ------------------------
     if args.extras:
+        out["spmv_configs"] = spmv_other_configs(ctx, stream, flush_l2, hbm, fma_rate)
+        out["c1_solve"] = c1_solve(ctx, stream, flush_l2)
+        out["c3_fixed"] = c3_fixed_iterations(ctx, stream, flush_l2)
         s4 = synth.config("c4")
         A4 = Matrix.from_csr(ctx, s4.rowptr, s4.col, s4.val)
         b4 = torch.as_tensor(s4.b, device="cuda")
@@ -566,12 +668,23 @@ def run_ours(args, rk):
             return bicgstab(ctx, A4, b4, xx, t4, rtol=RTOL, maxit=20000, precision=prec)[1]
         t64, r64 = timed(lambda: run4("fp64", x64), args.extra_reps)
         tm, rm = timed(lambda: run4("mixed", xm), args.extra_reps)
+        # the plain FP64 solve pushed to 1e-14 (or as far as it gets), the FP64 oracle the mixed
+        # result is measured against
+        x14 = torch.zeros_like(b4)
+        _, r14 = bicgstab(ctx, A4, b4, x14, t4, rtol=1e-14, maxit=20000)
+        xs14 = float(x14.abs().max().item())
         out["mixed"] = {"workload": "c4: 3D 7-point upwind convection-diffusion 160^3 (4.096M rows, 28.5M nnz), Pe=20",
                         "fp64_s": t64, "mixed_s": tm, "speedup": t64 / tm, "fp64_iters": r64.iters,
                         "mixed_inner_iters": rm.iters, "mixed_outer": rm.outer_iters,
                         "rel_res_true_fp64": r64.rel_res_true, "rel_res_true_mixed": rm.rel_res_true,
                         "err_vs_target_fp64": r64.err_vs_target, "err_vs_target_mixed": rm.err_vs_target,
-                        "max_abs_mixed_minus_fp64": float((xm - x64).abs().max().item())}
+                        "max_abs_mixed_minus_fp64": float((xm - x64).abs().max().item()),
+                        "fp64_1e14": {"rel_res_true": r14.rel_res_true, "status": r14.status, "iters": r14.iters},
+                        "err_vs_fp64_1e14": float((xm - x14).abs().max().item()) / xs14,
+                        "err_vs_fp64_1e14_fp64_solve": float((x64 - x14).abs().max().item()) / xs14,
+                        "err_note": "max |x - x_fp64(1e-14)| / max |x_fp64(1e-14)| for the mixed and the FP64 "
+                                    "solves to 1e-10"}
+        del x14
         del A4
         s5 = synth.config("c5")
         A5 = Matrix.from_csr(ctx, s5.rowptr, s5.col, s5.val)
@@ -609,6 +722,8 @@ def run_ours(args, rk):
                           (tf + ta) / tf, "forward_iters": rf.iters, "adjoint_iters": ra.iters,
                           "rel_res_true_forward": rf.rel_res_true, "rel_res_true_adjoint": ra.rel_res_true,
                           "adjoint_passes": ra.outer_iters, "adjoint_status": ra.status,
+                          "adjoint_reached_rtol": bool(ra.status == 0 and ra.rel_res_true <= 1e-12),
+                          "forward_reached_rtol": bool(rf.status == 0 and rf.rel_res_true <= 1e-12),
                           "transpose_build_s": t_tr,
                           "note": "transpose built once beforehand (not in the timed adjoint; transpose_build_s: "
                                   "transpose + its slice plan + one A^T SpMV, host clock); ratio_to_fp64_forward "

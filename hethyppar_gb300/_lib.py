@@ -68,6 +68,7 @@ SIGNATURES = [
     ("hhp_ctx_stream", _P, [_P]),
     ("hhp_ctx_sync", _I, [_P]),
     ("hhp_ctx_kernel_launches", ctypes.c_longlong, [_P]),
+    ("hhp_ctx_fp64_fma_rate", _I, [_P, _PD]),
     ("hhp_mat_from_csr", _I, [_P, _I, _I, _I, _P, _P, _P, _P, ctypes.POINTER(_P)]),
     ("hhp_mat_from_csr_dev", _I, [_P, _I, _I, _I, _P, _P, _P, ctypes.POINTER(_P)]),
     ("hhp_mat_from_mtx", _I, [_P, _S, ctypes.POINTER(_P)]),

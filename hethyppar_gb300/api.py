@@ -83,6 +83,12 @@ class Context:
     def kernel_launches(self) -> int:
         return int(lib().hhp_ctx_kernel_launches(self._h))
 
+    def fp64_fma_rate(self) -> float:
+        """Measured FP64 fused multiply-add throughput of the device (lane FMAs per second)."""
+        r = ctypes.c_double()
+        check(lib().hhp_ctx_fp64_fma_rate(self._h, ctypes.byref(r)), "hhp_ctx_fp64_fma_rate")
+        return r.value
+
     @property
     def alive(self) -> bool:
         return bool(self._h)

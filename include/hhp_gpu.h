@@ -108,6 +108,11 @@ void *hhp_ctx_stream(hhp_ctx *ctx);
 hhp_status hhp_ctx_sync(hhp_ctx *ctx);
 /* Number of kernels this context has launched (graph launches count their kernel nodes). */
 long long hhp_ctx_kernel_launches(const hhp_ctx *ctx);
+/* No counterpart in the reference: the device's FP64 fused multiply-add throughput (lane FMAs per
+ * second), measured by a short probe kernel on the context's stream (synchronises it). The FP64
+ * SpMV and vector kernels are bound by this rate as much as by HBM on GB300; it is the denominator
+ * of their FP64 floor. */
+hhp_status hhp_ctx_fp64_fma_rate(hhp_ctx *ctx, double *fma_per_s);
 
 /* ---- matrices: replace device_csr_create / device_csr_destroy (src/util/hhp_cuda.c:19-51,
  *      src/include/hhp_cuda.h:46-47) and buReadSparseMatrix (src/util/hhp_matrix.c:116) -------- */

@@ -97,3 +97,74 @@ def test_autograd_harness(ctx):
     assert np.max(np.abs(b.grad.cpu().numpy() - lam)) <= 1e-9 * np.max(np.abs(lam))
     assert np.max(np.abs(vals.grad.cpu().numpy() + lam[rows] * xd[s.col])) <= 1e-9 * np.max(np.abs(lam)) * \
         np.max(np.abs(xd))
+
+
+def test_finite_differences_c5_full_size(ctx):
+    """The adjoint gradient on the 1024^2 system (C5: 1.05M rows, Pe = 30, b ~ N(0,1) seed 4,
+    x_t ~ N(0,1) seed 5, L = 1/2 ||x - x_t||^2, solves at rtol 1e-12) against central differences
+    with h = 1e-6 on 64 random entries: 32 of b and 32 stored entries of A, for the FP64 and the
+    mixed-form gradients, within 1e-6 relative (relative to max(|g|, 1e-2 max|g|)).
+
+    Each perturbed solution x+- (of A+- x+- = b+-, A or b with one entry moved by +-h) is computed as
+    x + d+- with A+- d+- = b+- - A+- x = r0 +- (one entry): the solver runs on the perturbed matrix
+    to rtol 1e-12 relative to that small right-hand side, so d+- is accurate relative to itself. A
+    plain solve of each perturbed system to rtol 1e-12 from scratch would carry an error of about
+    cond(A) * 1e-12 * ||x|| (cond(A) ~ 4e5 here) in both x+ and x-, which does not cancel in the
+    difference and, over 2h = 2e-6, is larger than the gradient. r0 = b - A x is formed once by the
+    oracle. L(x+) - L(x-) = 1/2 (d+ - d-).(d+ + d- + 2 (x - x_t))."""
+    import math
+    from oracle import oracle as orc
+    s = synth.config("c5")
+    b, xt = s.b, s.x_target
+    A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
+    x, r0 = bicgstab(ctx, A, b, None, rtol=1e-12, maxit=50000)
+    assert r0.status == 0
+    g64 = bicgstab_backward(ctx, A, x, x - xt, rtol=1e-12, maxit=50000)
+    gmx = bicgstab_backward(ctx, A, x, x - xt, rtol=1e-12, maxit=50000, precision="mixed")
+    res0 = b - orc.spmv(s.rowptr, s.col, s.val, x)
+    rows = np.repeat(np.arange(s.m), np.diff(s.rowptr))
+    h = 1e-6
+
+    def delta(rhs):
+        d, rr = bicgstab(ctx, A, rhs, None, rtol=1e-12, maxit=50000)
+        assert rr.status == 0, rr
+        return d
+
+    def fd(dp, dm):
+        return 0.5 * np.dot(dp - dm, dp + dm + 2.0 * (x - xt)) / (2.0 * h)
+
+    rng = np.random.default_rng(64)
+    fd_b, fd_a = {}, {}
+    for i in rng.choice(s.m, 32, replace=False):
+        rp, rm = res0.copy(), res0.copy()
+        rp[i] += h
+        rm[i] -= h
+        fd_b[int(i)] = fd(delta(rp), delta(rm))
+    for kk in rng.choice(s.nnz, 32, replace=False):
+        i, j = int(rows[kk]), int(s.col[kk])
+        ds = []
+        for sgn in (1.0, -1.0):
+            v = s.val.copy()
+            v[kk] += sgn * h
+            A.set_values(v)
+            r = res0.copy()
+            r[i] -= sgn * h * x[j]
+            ds.append(delta(r))
+        fd_a[int(kk)] = fd(ds[0], ds[1])
+    A.set_values(s.val)
+    A.close()
+    worst = {}
+    for name, (dldb, dlda, rb) in (("fp64", g64), ("mixed", gmx)):
+        # the adjoint's true residual can stall just above 1e-12: lambda = A^-T (x - x_t) is ~1e3
+        # times larger than its right-hand side here, and the FP64 residual of an FP64 lambda
+        # cannot be resolved below eps * || |A^T| |lambda| || / ||g|| (a few 1e-12); the solver then
+        # stops on stagnation (HHP_ERR_MAXIT) with the residual it reached
+        assert rb.status == 0 or (rb.status == 6 and rb.rel_res_true <= 1e-11), (name, rb)
+        fb, fa = 1e-2 * np.max(np.abs(dldb)), 1e-2 * np.max(np.abs(dlda))
+        eb = [abs(g - dldb[i]) / max(abs(dldb[i]), fb) for i, g in fd_b.items()]
+        ea = [abs(g - dlda[k]) / max(abs(dlda[k]), fa) for k, g in fd_a.items()]
+        worst[name] = (max(eb), max(ea))
+    print("C5 gradient vs central differences (h = 1e-6) on 32 + 32 entries, worst relative error: " +
+          ", ".join(f"{n} b {v[0]:.2e} A {v[1]:.2e}" for n, v in worst.items()))
+    for name, (wb, wa) in worst.items():
+        assert wb <= 1e-6 and wa <= 1e-6, (name, wb, wa)

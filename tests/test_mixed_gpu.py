@@ -38,12 +38,14 @@ def test_mixed_reaches_fp64_tolerance(ctx, sysname):
 @pytest.mark.parametrize("sysname", ["c1", "cd3d_48"])
 def test_mixed_merged_and_classic_inner_loops(ctx, sysname):
     """The FP32 inner loop in both schedules: merged (4 kernels per iteration, the update test and
-    beta from the t = A s dot products) and classic (5). Both reach the FP64 tolerance with
-    iteration counts close to each other; the launch count follows 4 (or 5) per iteration plus 3
-    per FP64 update."""
+    beta from the t = A s dot products) and classic (5). Both reach the FP64 tolerance within the
+    mixed form's iteration bar (1.35x the FP64 solve's; the two FP32 schedules round differently
+    and their counts move apart by 10-15% either way from one system to the next); the launch
+    count follows 4 (or 5) per iteration plus 3 per FP64 update."""
     import math
     s = synth.config("c1") if sysname == "c1" else synth.convdiff3d(48, 20.0, seed=3)
     A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
+    _, r64 = bicgstab(ctx, A, s.b, s.x0, rtol=1e-10, maxit=5000)
     res = {}
     for loop, per_iter in (("merged", 4), ("classic", 5)):
         bicgstab(ctx, A, s.b, s.x0, rtol=1e-10, maxit=5000, precision="mixed", loop=loop)  # builds the graph
@@ -58,6 +60,7 @@ def test_mixed_merged_and_classic_inner_loops(ctx, sysname):
         assert n == 4 + per_iter * BODY * math.ceil(r.iters / BODY) + 3 * r.outer_iters + 3, (
             loop, n, r.iters, r.outer_iters)
         res[loop] = (x, r)
-    assert res["merged"][1].iters <= 1.1 * res["classic"][1].iters + 3
+    for loop in ("merged", "classic"):
+        assert res[loop][1].iters <= 1.35 * r64.iters + 5, (loop, res[loop][1].iters, r64.iters)
     scale = np.max(np.abs(s.x_target))
     assert np.max(np.abs(res["merged"][0] - res["classic"][0])) <= 1e-6 * scale
