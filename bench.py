@@ -386,11 +386,24 @@ def c3_fixed_iterations(ctx, stream, flush_l2, k=200):
     run()
     ms = _event_ms(stream, run, flush_l2, 3)
     r = res[-1]
+    # with row (left) Jacobi preconditioning the same system is solved to 1e-10 (the residual
+    # checked is that of A x = b itself)
+    resj = []
+
+    def runj():
+        x.zero_()
+        resj.append(bicgstab(ctx, A, b, x, rtol=RTOL, maxit=5000, precond="jacobi_row")[1])
+    runj()
+    msj = _event_ms(stream, runj, flush_l2, 3)
+    rj = resj[-1]
     A.close()
-    return {"workload": "c3: power-law 3.5M rows, 22.6M nnz, FP64, unpreconditioned", "fixed_iters": k, "ms": ms,
+    return {"workload": "c3: power-law 3.5M rows, 22.6M nnz, FP64", "fixed_iters": k, "ms": ms,
             "us_per_iter": ms * 1e3 / k, "rel_res_true_after": r.rel_res_true,
             "note": "fixed iterations (the reference's executables' mode, classic schedule): without "
-                    "preconditioning neither this library nor the reference reaches 1e-10 on C3"}
+                    "preconditioning neither this library nor the reference reaches 1e-10 on C3",
+            "row_jacobi_to_1e-10": {"ms": msj, "iters": rj.iters, "passes": rj.outer_iters,
+                                    "rel_res_true": rj.rel_res_true, "status": rj.status,
+                                    "us_per_iter": msj * 1e3 / max(rj.iters, 1)}}
 
 
 def run_ours(args, rk):

@@ -255,7 +255,7 @@ class SolveResult:
         return self.status == 0
 
 
-PRECONDS = {"none": 0, "jacobi": 1}
+PRECONDS = {"none": 0, "jacobi": 1, "jacobi_row": 2}
 # FP64 iteration schedule (hhp_loop): "merged" = 4 kernels per iteration, stop tests and beta from
 # the t = A s dot products; "classic" = the reference's order, rho and ||r|| as direct dot
 # products; "auto" = merged for forward solves, classic for the adjoint solve

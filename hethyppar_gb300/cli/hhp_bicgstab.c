@@ -59,7 +59,9 @@ static struct argp_option options[] = {
     {"out-format", OPT_OUTFMT, "compat|exact", 0, "Number format of the output X file", 0},
     {"device", OPT_DEVICE, "ID", 0, "CUDA device (default 0)", 0},
     {"write-csr", OPT_WCSR, "FILE", 0, "Also store the matrix as a binary CSR file (later runs: -m FILE)", 0},
-    {"precond", OPT_PRECOND, "none|jacobi", 0, "Preconditioner (default none, as the reference)", 0},
+    {"precond", OPT_PRECOND, "none|jacobi|jacobi_row", 0,
+     "Preconditioner: none (default, as the reference), jacobi (columns scaled by the diagonal), jacobi_row (rows)",
+     0},
     {"reorder", OPT_REORDER, "none|rcm", 0,
      "Row/column reordering for locality: rcm = reverse Cuthill-McKee (instead of a --perm file)", 0},
     {"loop", OPT_LOOP, "auto|merged|classic", 0,
@@ -104,8 +106,9 @@ static error_t parse_opt(int key, char *arg, struct argp_state *state) {
             else argp_error(state, "unknown loop '%s'", arg);
             break;
         case OPT_PRECOND:
-            if (strcmp(arg, "jacobi") == 0) a->jacobi = 1;
-            else if (strcmp(arg, "none") == 0) a->jacobi = 0;
+            if (strcmp(arg, "jacobi") == 0) a->jacobi = HHP_PRECOND_JACOBI;
+            else if (strcmp(arg, "jacobi_row") == 0) a->jacobi = HHP_PRECOND_JACOBI_ROW;
+            else if (strcmp(arg, "none") == 0) a->jacobi = HHP_PRECOND_NONE;
             else argp_error(state, "unknown preconditioner '%s'", arg);
             break;
         case ARGP_KEY_ARG: return 0;
@@ -239,7 +242,7 @@ int main(int argc, char **argv) {
     o.maxit = a.n_iters;
     o.precision = a.mixed ? HHP_PREC_MIXED : HHP_PREC_FP64;
     o.inner_rtol = 0.1;
-    o.precond = a.jacobi ? HHP_PRECOND_JACOBI : HHP_PRECOND_NONE;
+    o.precond = a.jacobi;
     o.loop = a.loop;
     o.fixed_iters = a.fixed;
     o.print_every = a.print_every;

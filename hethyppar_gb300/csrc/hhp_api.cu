@@ -505,7 +505,8 @@ static hhp_status check_solve(hhp_ctx *ctx, hhp_mat *A, const void *b, const voi
         return HHP_ERR_ARG;
     }
     if (o && (o->maxit < 0 || !(o->rtol >= 0.0) || (o->precision != HHP_PREC_FP64 && o->precision != HHP_PREC_MIXED) ||
-              (o->precond != HHP_PRECOND_NONE && o->precond != HHP_PRECOND_JACOBI) ||
+              (o->precond != HHP_PRECOND_NONE && o->precond != HHP_PRECOND_JACOBI &&
+               o->precond != HHP_PRECOND_JACOBI_ROW) ||
               (o->loop != HHP_LOOP_AUTO && o->loop != HHP_LOOP_MERGED && o->loop != HHP_LOOP_CLASSIC))) {
         set_error("bicgstab: invalid options (maxit %d, rtol %g, precision %d, precond %d, loop %d)", o->maxit,
                   o->rtol, o->precision, o->precond, o->loop);
@@ -520,6 +521,7 @@ hhp_status hhp_bicgstab(hhp_ctx *ctx, hhp_mat *A, const double *b, double *x, co
     HHP_TRY(check_solve(ctx, A, b, x, opts));
     const hhp_solve_opts o = opts ? *opts : default_opts();
     if (o.precond == HHP_PRECOND_JACOBI) return solve_jacobi(A, b, x, xt, &o, info, true);
+    if (o.precond == HHP_PRECOND_JACOBI_ROW) return solve_jacobi_row(A, b, x, xt, &o, info, true);
     return solve_any(A, b, x, xt, &o, info, true);
     HHP_API_END
 }
@@ -530,6 +532,7 @@ hhp_status hhp_bicgstab_dev(hhp_ctx *ctx, hhp_mat *A, const double *b, double *x
     HHP_TRY(check_solve(ctx, A, b, x, opts));
     const hhp_solve_opts o = opts ? *opts : default_opts();
     if (o.precond == HHP_PRECOND_JACOBI) return solve_jacobi(A, b, x, xt, &o, info, false);
+    if (o.precond == HHP_PRECOND_JACOBI_ROW) return solve_jacobi_row(A, b, x, xt, &o, info, false);
     return solve_any(A, b, x, xt, &o, info, false);
     HHP_API_END
 }

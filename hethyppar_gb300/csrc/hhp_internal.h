@@ -77,6 +77,9 @@ void build_plan(int m, const int *rowptr, int rpl, int long_thr, int cap, int wi
 void assign_units(const SellHost &P, int n_warps, std::vector<int> &warp_ptr, std::vector<int> &warp_units,
                   double *imbalance);
 
+// Long rows whose SpMV epilogue records are folded together inside the SpMV (see fold_long_group).
+constexpr int kLongGroup = 32;
+
 struct PlanDev {
     int rpl = 0, H = 0, n_slices = 0, n_long = 0, n_chunks = 0, ctas = 0, warps_per_cta = 0, unroll = 4;
     bool has_perm = false, sorted = false, d16 = false;  // d16: 16-bit column offsets (scol16)
@@ -99,6 +102,10 @@ struct PlanDev {
     double *chunk_part = nullptr;     // n_chunks
     unsigned *long_cnt = nullptr;     // n_long (kept at zero between launches)
     double *long_dot = nullptr;       // n_long * 4 epilogue contributions of long rows
+    int n_groups = 0;                 // long rows folded by groups of kLongGroup
+    unsigned *group_cnt = nullptr;    // n_groups (kept at zero between launches)
+    double *group_dot = nullptr;      // n_groups * 4: each group's long_dot records summed (the
+                                      // records the consumers reduce beside the CTA partials)
     double *cta_part = nullptr;       // ctas * 4 epilogue partials (records of 2, or 4 for EP_DOT3)
     bool built() const { return slice_ptr != nullptr; }
     void release();
@@ -140,6 +147,9 @@ struct hhp_mat {
     hhp_mat *jac = nullptr;
     double *dinv = nullptr;
     std::vector<double> dinv_host;
+    // row (left) Jacobi: A with row i scaled by 1/a_ii, and room for the scaled right-hand side
+    hhp_mat *jac_row = nullptr;
+    double *jac_row_b = nullptr;
 };
 
 namespace hhp {
@@ -187,6 +197,9 @@ hhp_status ensure_jacobi(hhp_mat *A);
 void release_jacobi(hhp_mat *A);
 hhp_status solve_jacobi(hhp_mat *A, const double *b, double *x, const double *xt, const hhp_solve_opts *o,
                         hhp_solve_info *info, bool host);
+// Row (left) Jacobi: BiCGStab on diag(A)^-1 A x = diag(A)^-1 b until b - A x meets rtol.
+hhp_status solve_jacobi_row(hhp_mat *A, const double *b, double *x, const double *xt, const hhp_solve_opts *o,
+                            hhp_solve_info *info, bool host);
 // Adjoint: lambda = A^-T g; dlda[k] = -lambda[row(k)] * x[col(k)].
 hhp_status backward_dev(hhp_mat *A, const double *x_dev, const double *g_dev, double *dldb_dev, double *dlda_dev,
                         const hhp_solve_opts *o, hhp_solve_info *info);

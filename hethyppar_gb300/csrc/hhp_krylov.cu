@@ -147,8 +147,8 @@ __device__ __forceinline__ bool dead_step(const DevScal *sc) {
 struct SpmvParts {
     const double *cta_part;
     int n_cta;
-    const double *long_dot;
-    int n_long;
+    const double *extra;  // the folded records of groups of long rows
+    int n_extra;
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(512) k_init(DevScal *sc, T *R, const T *B, T *
         reduce_partials<1>(part_b, nparts, nullptr, 0, q, red);
         v[0] = v[1] = q[0];
     } else {
-        reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
+        reduce_partials<2>(sp.cta_part, sp.n_cta, sp.extra, sp.n_extra, v, red);
     }
     const double rr = v[0], bb = v[1];
     constexpr int E = Unit<T>::E;
@@ -392,7 +392,7 @@ __global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const 
         }
     }
     double v[1];  // r0.v: the first component of the SpMV's 2-wide records
-    reduce_partials<1, 2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
+    reduce_partials<1, 2>(sp.cta_part, sp.n_cta, sp.extra, sp.n_extra, v, red);
     if (dead) return;
     if (threadIdx.x == 0) {
         int ok = 1;  // the status was running at entry
@@ -497,7 +497,7 @@ __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P,
         }
     }
     double q[4];  // t.s, t.t (2-wide SpMV records), s.s (4-wide K_S records)
-    reduce_two<2, 2, 1, 4, 4>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, part_s, nparts, q, red);
+    reduce_two<2, 2, 1, 4, 4>(sp.cta_part, sp.n_cta, sp.extra, sp.n_extra, part_s, nparts, q, red);
     if (dead) return;
     if (threadIdx.x == 0) {
         int ok = 1;  // the status was running at entry
@@ -621,7 +621,7 @@ __global__ void __launch_bounds__(512) k_xrp(DevScal *sc, T *X, T *R, T *P, cons
         }
     }
     double q[8];  // t.s, t.t, r0.t (4-wide SpMV records), s.s, r0.s (4-wide K_S records)
-    reduce_two<3, 4, 2, 4, 8>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, part_s, nparts, q, red);
+    reduce_two<3, 4, 2, 4, 8>(sp.cta_part, sp.n_cta, sp.extra, sp.n_extra, part_s, nparts, q, red);
     if (dead) {
         if (b0t0()) {
             if (first_in_body) sc->bodies += 1;
@@ -750,7 +750,7 @@ __global__ void __launch_bounds__(512) k_xrp(DevScal *sc, T *X, T *R, T *P, cons
 __global__ void k_finish(DevScal *sc, SpmvParts sp) {
     __shared__ double red[kRedScratch];
     double v[2];
-    reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
+    reduce_partials<2>(sp.cta_part, sp.n_cta, sp.extra, sp.n_extra, v, red);
     if (threadIdx.x == 0) {
         sc->true_rr = v[0];
         sc->bb = v[1];
@@ -782,7 +782,7 @@ __global__ void __launch_bounds__(512) k_mix_init(DevScal *sc, const double *Yd,
         reduce_partials<1>(part_b, nparts, nullptr, 0, q, red);
         v[0] = v[1] = q[0];
     } else {
-        reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
+        reduce_partials<2>(sp.cta_part, sp.n_cta, sp.extra, sp.n_extra, v, red);
     }
     const double rd2 = v[0], bb = v[1];
     double acc[1] = {0.0};
@@ -977,7 +977,7 @@ __global__ void __launch_bounds__(512) k_xrp_ru(DevScal *sc, double *X, float *D
         }
     }
     double q[8];  // t.s, t.t, r0.t (4-wide SpMV records), s.s, r0.s (4-wide K_S records)
-    reduce_two<3, 4, 2, 4, 8>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, part_s, nparts, q, red);
+    reduce_two<3, 4, 2, 4, 8>(sp.cta_part, sp.n_cta, sp.extra, sp.n_extra, part_s, nparts, q, red);
     if (dead) {
         if (b0t0()) {
             if (first_in_body) sc->bodies += 1;
@@ -1112,7 +1112,7 @@ __global__ void __launch_bounds__(512) k_ru_apply(DevScal *sc, const double *Rd,
     __shared__ double red[kRedScratch];
     if (!sc->ru_flag) return;
     double v[2];
-    reduce_partials<2>(sp.cta_part, sp.n_cta, sp.long_dot, sp.n_long, v, red);
+    reduce_partials<2>(sp.cta_part, sp.n_cta, sp.extra, sp.n_extra, v, red);
     const double rd2 = v[0];
     double acc[2] = {0.0, 0.0};
     for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu4; u += gridDim.x * blockDim.x) {
@@ -1184,7 +1184,8 @@ T *dalloc(size_t n, hhp_status &st, cudaStream_t stream) {
     return p;
 }
 
-SpmvParts parts_of(const PlanDev &p) { return SpmvParts{p.cta_part, p.ctas, p.long_dot, p.n_long}; }
+// The SpMV's partial records: one per CTA, then one per group of long rows.
+SpmvParts parts_of(const PlanDev &p) { return SpmvParts{p.cta_part, p.ctas, p.group_dot, p.n_groups}; }
 
 hhp_status ensure_solver(hhp_mat *A, Solver **out, int maxit) {
     Solver *s = A->solver;
@@ -1527,7 +1528,7 @@ hhp_status run_direct64(Solver *s, bool merged) {
         if (s->h_sc->status != ST_RUNNING) break;
     }
     HHP_TRY(launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0));
-    HHP_CUDA(launch_k(k_finish, dim3(1), dim3(32), 0, st, s->sc, parts_of(A->plan64)));
+    HHP_CUDA(launch_k(k_finish, dim3(1), dim3(128), 0, st, s->sc, parts_of(A->plan64)));
     A->ctx->kernel_launches += 1;
     HHP_CUDA(cudaGetLastError());
     return HHP_OK;
@@ -1558,7 +1559,7 @@ hhp_status build_g64(Solver *s, bool merged) {
         if (rc != HHP_OK) break;
         rc = launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0);
         if (rc != HHP_OK) break;
-        HHP_CUDA(launch_k(k_finish, dim3(1), dim3(32), 0, st, s->sc, parts_of(A->plan64)));
+        HHP_CUDA(launch_k(k_finish, dim3(1), dim3(128), 0, st, s->sc, parts_of(A->plan64)));
     } while (0);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(st, &g);
@@ -1607,7 +1608,7 @@ hhp_status build_gmix(Solver *s, bool merged) {
         HHP_CUDA(launch_k(k_mix_final, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc32, s->X, s->D32, nu4));
         rc = launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0);
         if (rc != HHP_OK) break;
-        HHP_CUDA(launch_k(k_finish, dim3(1), dim3(32), 0, st, s->sc32, parts_of(A->plan64)));
+        HHP_CUDA(launch_k(k_finish, dim3(1), dim3(128), 0, st, s->sc32, parts_of(A->plan64)));
     } while (0);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(st, &g);
@@ -1697,7 +1698,7 @@ hhp_status run_direct_mix(Solver *s, bool merged) {
     }
     HHP_CUDA(launch_k(k_mix_final, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc32, s->X, s->D32, nu4));
     HHP_TRY(launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0));
-    HHP_CUDA(launch_k(k_finish, dim3(1), dim3(32), 0, st, s->sc32, parts_of(A->plan64)));
+    HHP_CUDA(launch_k(k_finish, dim3(1), dim3(128), 0, st, s->sc32, parts_of(A->plan64)));
     nk += 2;
     HHP_CUDA(cudaGetLastError());
     return HHP_OK;

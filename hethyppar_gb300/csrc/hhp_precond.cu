@@ -37,6 +37,15 @@ __global__ void k_diag_inv(const int *__restrict__ rowptr, const int *__restrict
     }
 }
 
+// out[k] = val[k] * dinv[row of k]: row i of A scaled by 1/a_ii
+__global__ void k_scale_rows(const int *__restrict__ rowptr, const double *__restrict__ val,
+                             const double *__restrict__ dinv, int m, double *out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+        const double d = dinv[i];
+        for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) out[k] = val[k] * d;
+    }
+}
+
 __global__ void k_scale_cols(const int *__restrict__ col, const double *__restrict__ val,
                              const double *__restrict__ dinv, int nnz, double *out) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += gridDim.x * blockDim.x)
@@ -125,7 +134,43 @@ hhp_status ensure_jacobi(hhp_mat *A) {
     return HHP_OK;
 }
 
+// A with row i scaled by 1/a_ii (A->jac_row), and room for the scaled right-hand side.
+hhp_status ensure_jacobi_row(hhp_mat *A) {
+    if (A->jac_row) return HHP_OK;
+    HHP_TRY(ensure_jacobi(A));  // the diagonal (and its checks) come from the column-scaled form
+    cudaStream_t st = A->ctx->stream;
+    hhp_mat *J = nullptr;
+    HHP_TRY(mat_create_dev(A->ctx, A->m, A->n, A->nnz, &J));
+    hhp_status rc = HHP_OK;
+    if (cudaMemcpyAsync(J->rowptr, A->rowptr, sizeof(int) * (static_cast<size_t>(A->m) + 1), cudaMemcpyDeviceToDevice,
+                        st) != cudaSuccess ||
+        (A->nnz > 0 && cudaMemcpyAsync(J->col, A->col, sizeof(int) * static_cast<size_t>(A->nnz),
+                                       cudaMemcpyDeviceToDevice, st) != cudaSuccess))
+        rc = HHP_ERR_CUDA;
+    if (rc == HHP_OK && A->m > 0) {
+        k_scale_rows<<<grid_for(A, A->m), 256, 0, st>>>(A->rowptr, A->val, A->dinv, A->m, J->val);
+        if (cudaGetLastError() != cudaSuccess) rc = HHP_ERR_CUDA;
+    }
+    double *bs = nullptr;
+    if (rc == HHP_OK && cudaMalloc(&bs, sizeof(double) * (static_cast<size_t>(A->n) + 4)) != cudaSuccess) rc = HHP_ERR_OOM;
+    if (rc != HHP_OK) {
+        set_error("building the row-scaled matrix failed: %s", cudaGetErrorString(cudaGetLastError()));
+        hhp_mat_destroy(J);
+        cudaFree(bs);
+        return rc;
+    }
+    J->rowptr_host = A->rowptr_host;
+    A->jac_row = J;
+    A->jac_row_b = bs;
+    HHP_CUDA(cudaStreamSynchronize(st));
+    return HHP_OK;
+}
+
 void release_jacobi(hhp_mat *A) {
+    if (A->jac_row) hhp_mat_destroy(A->jac_row);
+    A->jac_row = nullptr;
+    cudaFree(A->jac_row_b);
+    A->jac_row_b = nullptr;
     if (A->jac) hhp_mat_destroy(A->jac);
     A->jac = nullptr;
     cudaFree(A->dinv);
@@ -175,6 +220,79 @@ hhp_status solve_jacobi(hhp_mat *A, const double *b, double *x, const double *xt
     }
     in.err_vs_target = err;
     if (info) *info = in;
+    return rc;
+}
+
+// Row (left) Jacobi: BiCGStab on M^-1 A x = M^-1 b, M = diag(A), which equilibrates rows whose
+// scales differ by orders of magnitude (a power-law matrix with diagonals from 1e-9 to 1e5 is
+// not solved to 1e-10 unpreconditioned, nor with column scaling). The scaled solve's stop test is
+// on M^-1 (b - A x); after each pass the residual of A x = b itself is formed (a zero-iteration
+// solve of A from x: the FP64 residual SpMV), and while it is above rtol the scaled solve
+// continues from x with its tolerance tightened by the shortfall. The status and the reported
+// residual are those of A x = b.
+hhp_status solve_jacobi_row(hhp_mat *A, const double *b, double *x, const double *xt, const hhp_solve_opts *o,
+                            hhp_solve_info *info, bool host) {
+    HHP_TRY(ensure_jacobi_row(A));
+    const int n = A->n;
+    cudaStream_t st = A->ctx->stream;
+    std::vector<double> bs_host;
+    const double *bs = nullptr;
+    if (host) {
+        bs_host.resize(static_cast<size_t>(n));
+        for (int i = 0; i < n; ++i) bs_host[static_cast<size_t>(i)] = b[i] * A->dinv_host[static_cast<size_t>(i)];
+        bs = bs_host.data();
+    } else {
+        HHP_CUDA(cudaMemcpyAsync(A->jac_row_b, b, sizeof(double) * static_cast<size_t>(n), cudaMemcpyDeviceToDevice, st));
+        if (n > 0) {
+            k_scale_vec<<<grid_for(A, n), 256, 0, st>>>(A->jac_row_b, A->dinv, n, 0);
+            HHP_CUDA(cudaGetLastError());
+        }
+        bs = A->jac_row_b;
+    }
+    hhp_solve_opts os = *o;
+    os.precond = HHP_PRECOND_NONE;
+    hhp_solve_opts oc = *o;  // the residual check: no iterations, no callback
+    oc.precond = HHP_PRECOND_NONE;
+    oc.maxit = 0;
+    oc.fixed_iters = 0;
+    oc.print_every = 0;
+    oc.cb = nullptr;
+    hhp_solve_info is{}, ic{};
+    hhp_status rc = HHP_ERR_MAXIT;
+    int iters = 0, passes = 0;
+    double t = 0.0, rtol_s = o->rtol;
+    for (int pass = 0; pass < 8; ++pass) {
+        os.rtol = rtol_s;
+        os.maxit = o->maxit - iters;
+        const hhp_status rs = solve_any(A->jac_row, bs, x, nullptr, &os, &is, host);
+        if (rs != HHP_OK && rs != HHP_ERR_MAXIT && rs != HHP_ERR_BREAKDOWN) return rs;
+        iters += is.iters;
+        passes += std::max(is.outer_iters, 1);
+        t += is.t_solve_s;
+        const hhp_status rcheck = solve_any(A, b, x, xt, &oc, &ic, host);
+        if (rcheck != HHP_OK && rcheck != HHP_ERR_MAXIT) return rcheck;
+        t += ic.t_solve_s;
+        if (ic.rel_res_true <= o->rtol) {
+            rc = HHP_OK;
+            break;
+        }
+        rc = rs == HHP_OK ? HHP_ERR_MAXIT : rs;  // reported if this is the last pass
+        if (rs != HHP_OK || iters >= o->maxit) break;
+        // the scaled residual met its tolerance but the original one did not: ask the scaled solve
+        // for the missing factor (and a margin), never less than 1e-4 per pass
+        rtol_s *= std::max(1e-4, 0.5 * o->rtol / ic.rel_res_true);
+        if (rtol_s < 1e-17) break;
+    }
+    if (info) {
+        *info = ic;
+        info->iters = iters;
+        info->outer_iters = passes;
+        info->half_step = is.half_step;
+        info->rel_res_recursive = is.rel_res_recursive;
+        info->t_solve_s = t;
+        info->status = rc;
+        info->fp64_fallback = is.fp64_fallback;
+    }
     return rc;
 }
 

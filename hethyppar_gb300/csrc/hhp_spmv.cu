@@ -124,6 +124,8 @@ struct SellArgs {
     double *chunk_part;
     unsigned *long_cnt;
     double *long_dot;
+    unsigned *group_cnt;  // per group of kLongGroup long rows: rows finished this launch
+    double *group_dot;    // per group: the fixed-order sum of its rows' long_dot records
     double *cta_part;
     const VT *x;
     VT *y;
@@ -134,7 +136,7 @@ struct SellArgs {
     const int *gate;   // nullable: skip the whole launch when *gate == 0
     const int *stop;   // nullable: skip the whole launch when *stop != 0
     int *err;
-    int m, n_slices, n_chunks;
+    int m, n_slices, n_chunks, n_long;
     bool has_perm;
 };
 
@@ -292,6 +294,38 @@ __device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, long long
     if (EP == EP_DOT3) d2 += static_cast<double>(e2);
 }
 
+// Long rows' epilogue records are folded by groups of kLongGroup consecutive long rows: the warp
+// that completes the last row of a group sums the group's records, one per lane, with a fixed
+// butterfly, so consumers reduce n_long / kLongGroup records instead of n_long (a 3.5M-row power
+// law has ~4600 long rows: their records made every consumer block's reduction several times
+// longer than the vector work it precedes).
+template <typename VT, int EP>
+__device__ __forceinline__ void fold_long_group(const SellArgs<VT> &a, int l, int lane) {
+    constexpr int S = EP == EP_DOT3 ? 4 : 2;
+    const int g = l / kLongGroup, first = g * kLongGroup, size = min(kLongGroup, a.n_long - first);
+    unsigned last = 0;
+    if (lane == 0) {
+        __threadfence();  // this row's long_dot record before the group count
+        last = atomicAdd(&a.group_cnt[g], 1u) == static_cast<unsigned>(size - 1);
+    }
+    last = __shfl_sync(0xffffffffu, last, 0);
+    if (!last) return;
+    __threadfence();
+    const double *rec = a.long_dot + static_cast<size_t>(first + lane) * S;
+    if (EP == EP_DOT3) {
+        const double v[4] = {lane < size ? __ldcg(rec) : 0.0, lane < size ? __ldcg(rec + 1) : 0.0,
+                             lane < size ? __ldcg(rec + 2) : 0.0, 0.0};
+        const double r = warp_reduce<4>(v, lane);  // quantity q in lanes [8q, 8q + 8)
+        if ((lane & 7) == 0) a.group_dot[static_cast<size_t>(g) * 4 + (lane >> 3)] = r;
+    } else {
+        double d0 = lane < size ? __ldcg(rec) : 0.0, d1 = lane < size ? __ldcg(rec + 1) : 0.0;
+        warp_sum2(d0, d1, lane);
+        if (lane == 0) a.group_dot[static_cast<size_t>(g) * 2] = d0;
+        if (lane == 16) a.group_dot[static_cast<size_t>(g) * 2 + 1] = d1;
+    }
+    if (lane == 0) a.group_cnt[g] = 0u;  // ready for the next launch
+}
+
 template <typename VT, int EP>
 __device__ __forceinline__ void do_chunk(const SellArgs<VT> &a, int c, int lane) {
     const int4 d = __ldg(&a.chunks[c]);
@@ -312,6 +346,7 @@ __device__ __forceinline__ void do_chunk(const SellArgs<VT> &a, int c, int lane)
             if (k + 32 * u < d.w) acc = vfma(v[u], xv[u], acc);
     }
     acc = warp_sum(acc);
+    int done = -1;  // the long row this warp completed (its epilogue record written), else -1
     if (lane == 0) {
         const int cid = d.y;
         a.chunk_part[cid] = static_cast<double>(acc);
@@ -337,7 +372,12 @@ __device__ __forceinline__ void do_chunk(const SellArgs<VT> &a, int c, int lane)
                 a.long_dot[2 * l] = e0;
                 a.long_dot[2 * l + 1] = e1;
             }
+            done = l;
         }
+    }
+    if (EP != EP_AXPBY && EP != EP_Y) {
+        done = __shfl_sync(0xffffffffu, done, 0);
+        if (done >= 0) fold_long_group<VT, EP>(a, done, lane);
     }
 }
 
@@ -599,6 +639,11 @@ hhp_status build_plan_dev(hhp_mat *A, PlanDev &p) {
     HHP_CUDA(cudaMemsetAsync(p.long_cnt, 0, sizeof(unsigned) * std::max(1, p.n_long), ctx->stream));
     HHP_CUDA(cudaMalloc(&p.long_dot, sizeof(double) * 4 * std::max(1, p.n_long)));
     HHP_CUDA(cudaMemsetAsync(p.long_dot, 0, sizeof(double) * 4 * std::max(1, p.n_long), ctx->stream));
+    p.n_groups = (p.n_long + kLongGroup - 1) / kLongGroup;
+    HHP_CUDA(cudaMalloc(&p.group_cnt, sizeof(unsigned) * std::max(1, p.n_groups)));
+    HHP_CUDA(cudaMemsetAsync(p.group_cnt, 0, sizeof(unsigned) * std::max(1, p.n_groups), ctx->stream));
+    HHP_CUDA(cudaMalloc(&p.group_dot, sizeof(double) * 4 * std::max(1, p.n_groups)));
+    HHP_CUDA(cudaMemsetAsync(p.group_dot, 0, sizeof(double) * 4 * std::max(1, p.n_groups), ctx->stream));
     HHP_CUDA(cudaMalloc(&p.cta_part, sizeof(double) * 4 * p.ctas));
     HHP_CUDA(cudaMemsetAsync(p.cta_part, 0, sizeof(double) * 4 * p.ctas, ctx->stream));
     HHP_TRY(fill_values<VT>(A, p, true));
@@ -627,6 +672,8 @@ SellArgs<VT> make_args(hhp_mat *A, const PlanDev &p, const VT *csr_val, const VT
     a.chunk_part = p.chunk_part;
     a.long_cnt = p.long_cnt;
     a.long_dot = p.long_dot;
+    a.group_cnt = p.group_cnt;
+    a.group_dot = p.group_dot;
     a.cta_part = p.cta_part;
     a.x = x;
     a.y = y;
@@ -642,6 +689,7 @@ SellArgs<VT> make_args(hhp_mat *A, const PlanDev &p, const VT *csr_val, const VT
     a.m = A->m;
     a.n_slices = p.n_slices;
     a.n_chunks = p.n_chunks;
+    a.n_long = p.n_long;
     a.has_perm = p.has_perm;
     return a;
 }
@@ -664,6 +712,8 @@ void PlanDev::release() {
     cudaFree(chunk_part);
     cudaFree(long_cnt);
     cudaFree(long_dot);
+    cudaFree(group_cnt);
+    cudaFree(group_dot);
     cudaFree(cta_part);
     *this = PlanDev();
 }

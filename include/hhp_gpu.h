@@ -49,8 +49,14 @@ typedef enum { HHP_PREC_FP64 = 0, HHP_PREC_MIXED = 1 } hhp_precision;
 /* Preconditioner. JACOBI: right preconditioning with M = diag(A) (the diagonal form of the ILU path
  * left commented out in gpu_BiCGStab, src/entry/bicgstab_gpu.c:185-201, 238-254): BiCGStab runs on
  * A M^-1 (a column-scaled copy of A built once per matrix) and x = M^-1 y; the stop test and the
- * reported residual are those of A x = b. Needs a nonzero diagonal (HHP_ERR_ARG otherwise). */
-typedef enum { HHP_PRECOND_NONE = 0, HHP_PRECOND_JACOBI = 1 } hhp_precond;
+ * reported residual are those of A x = b. JACOBI_ROW: left preconditioning with the same M (row
+ * equilibration, for matrices whose rows differ in scale by orders of magnitude): BiCGStab runs on
+ * M^-1 A x = M^-1 b (a row-scaled copy of A), and after each pass the residual of A x = b itself is
+ * checked; while it is above rtol the scaled solve continues from x with a tolerance tightened by
+ * the shortfall, so the reported residual and the status are those of A x = b (iters counts the
+ * scaled solve's iterations, outer_iters its passes; the callback sees the scaled residual). Both
+ * need a nonzero diagonal (HHP_ERR_ARG otherwise). */
+typedef enum { HHP_PRECOND_NONE = 0, HHP_PRECOND_JACOBI = 1, HHP_PRECOND_JACOBI_ROW = 2 } hhp_precond;
 
 /* FP64 iteration schedule. MERGED: the stop tests and beta come from the dot products of the
  * t = A s step (||r_new||^2 = s.s - omega t.s, r0.r_new = r0.s - omega r0.t), so one iteration is

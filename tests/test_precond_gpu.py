@@ -88,3 +88,28 @@ def test_jacobi_refuses_a_zero_diagonal(ctx):
         bicgstab(ctx, A, np.ones(3), rtol=1e-10, maxit=100, precond="jacobi")
     assert e.value.status == 1 and "row 1" in str(e.value)
     A.close()
+
+
+def test_row_jacobi_solves_a_badly_row_scaled_power_law(ctx):
+    """Rows whose scales span many orders of magnitude (a power-law matrix whose diagonal is 1.1x its
+    row's absolute sum: diagonals from ~1e-7 to ~1e4): unpreconditioned BiCGStab stalls far from
+    1e-10, row (left) Jacobi reaches it, and the reported residual is that of A x = b itself
+    (recomputed here by the oracle), on the host and device entry points alike."""
+    import math
+    from oracle import oracle as orc
+    s = synth.powerlaw(300_000, max_len=20_000, n_dense=4, dense_lo=5_000, dense_hi=20_000, seed=13)
+    A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
+    _, r0 = bicgstab(ctx, A, s.b, rtol=1e-10, maxit=300)
+    assert r0.status != 0 and r0.rel_res_true > 1e-6
+    x, r = bicgstab(ctx, A, s.b, None, s.x_target, rtol=1e-10, maxit=2000, precond="jacobi_row")
+    assert r.status == 0 and r.rel_res_true <= 1e-10, r
+    res = s.b - orc.spmv(s.rowptr, s.col, s.val, x)
+    assert math.sqrt(orc.dot(res, res) / orc.dot(s.b, s.b)) <= 1.0000001e-10
+    assert r.err_vs_target <= 1e-6
+    xd = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+    xd, rd = bicgstab(ctx, A, dev(s.b), xd, None, rtol=1e-10, maxit=2000, precond="jacobi_row")
+    assert rd.status == 0 and rd.iters == r.iters and np.array_equal(xd.cpu().numpy(), x)
+    # the mixed form through the same scaling
+    xm, rm = bicgstab(ctx, A, s.b, rtol=1e-10, maxit=4000, precond="jacobi_row", precision="mixed")
+    assert rm.status == 0 and rm.rel_res_true <= 1e-10, rm
+    A.close()
