@@ -62,48 +62,138 @@ __device__ __forceinline__ void merge_path(const int *__restrict__ rowptr, int m
     k = d - lo;
 }
 
-__device__ __forceinline__ double warp_range_sum(const int *__restrict__ col, const double *__restrict__ val,
-                                                 const double *__restrict__ x, long long a, long long b, int lane) {
-    double s = 0.0;
-    for (long long k = a + lane; k < b; k += 32) s = fma(__ldg(val + k), __ldg(x + __ldg(col + k)), s);
-    return hhp::warp_sum(s);
+constexpr int kIpt = 8;                   // merge items per thread per tile
+constexpr int kTile = kThreads * kIpt;    // merge items per tile (2048)
+constexpr int kMaxTiles = static_cast<int>(kItemsPerCtaMax / kTile);
+
+// Inclusive segmented scan over the block, in thread order, of (row, v) pairs whose rows do not
+// decrease with the thread index: the sum of v over the run of threads up to and including this
+// one that carry the same row, earlier values first. Fixed order: reproducible.
+__device__ __forceinline__ double seg_scan(int row, double v, int *srow, double *sv) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int r2 = __shfl_up_sync(0xffffffffu, row, o);
+        const double v2 = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o && r2 == row) v = v2 + v;
+    }
+    if (lane == 31) {
+        srow[warp] = row;
+        sv[warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {  // the warps' totals, in order (8 of them)
+        for (int w = 1; w < nw; ++w)
+            if (srow[w] == srow[w - 1]) sv[w] = sv[w - 1] + sv[w];
+    }
+    __syncthreads();
+    if (warp > 0 && srow[warp - 1] == row) v = sv[warp - 1] + v;
+    return v;
 }
 
+// Merge-path SpMV, thread-sequential: CTA c takes merge items [c*D, (c+1)*D) of the list of row
+// ends and nonzeros, in tiles of kTile items. Per tile the CTA stages, with coalesced loads, the
+// row ends, the values and the gathered x[col] of its nonzeros in shared memory; thread t walks
+// kIpt items of it, summing its rows in CSR order with one FMA per nonzero and writing every row
+// that starts and ends inside its walk. The partial sums of rows that cross threads are combined
+// by a segmented scan (fixed order), and a row still open at the end of a tile carries into the
+// next tile; the row open at the end of the CTA's range goes to the CTA's carry slot.
 __global__ void __launch_bounds__(kThreads) k_mp_spmv(int m, long long nnz, const int *__restrict__ rowptr,
                                                       const int *__restrict__ col, const double *__restrict__ val,
                                                       double alpha, const double *__restrict__ x, double beta,
                                                       double *y, long long D, double *carry_val, int *carry_row) {
-    const int c = blockIdx.x;
+    __shared__ int s_rend[kTile + 1];
+    __shared__ double s_val[kTile], s_x[kTile];
+    __shared__ long long s_bound_k[kMaxTiles + 1];
+    __shared__ int s_bound_r[kMaxTiles + 1];
+    __shared__ int s_srow[32];
+    __shared__ double s_sv[32];
+    const int c = blockIdx.x, t = threadIdx.x;
     const long long total = static_cast<long long>(m) + nnz;
-    // the last CTAs can start past the end when the split is rounded up: they get an empty range
-    const long long d0 = static_cast<long long>(c) * D < total ? static_cast<long long>(c) * D : total;
-    const long long d1 = d0 + D < total ? d0 + D : total;
-    int r0, r1;
-    long long k0, k1;
-    merge_path(rowptr, m, nnz, d0, r0, k0);
-    merge_path(rowptr, m, nnz, d1, r1, k1);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    // rows ending inside this CTA's range
-    for (int r = r0 + warp; r < r1; r += nw) {
-        const long long a = rowptr[r] > k0 ? rowptr[r] : k0;
-        const double s = warp_range_sum(col, val, x, a, rowptr[r + 1], lane);
-        if (lane == 0) y[r] = beta != 0.0 ? fma(beta, y[r], alpha * s) : alpha * s;
+    const long long c0 = static_cast<long long>(c) * D < total ? static_cast<long long>(c) * D : total;
+    const long long c1 = c0 + D < total ? c0 + D : total;
+    const int ntiles = static_cast<int>((c1 - c0 + kTile - 1) / kTile);
+    // every tile boundary of the CTA's range at once (one search latency, not one per tile)
+    if (t <= ntiles) {
+        const long long d = c0 + static_cast<long long>(t) * kTile < c1 ? c0 + static_cast<long long>(t) * kTile : c1;
+        int r;
+        long long k;
+        merge_path(rowptr, m, nnz, d, r, k);
+        s_bound_r[t] = r;
+        s_bound_k[t] = k;
     }
-    // the row left open at the end of the range
-    if (warp == 0) {
-        double s = 0.0;
-        int cr = -1;
-        if (r1 < m) {
-            const long long a = rowptr[r1] > k0 ? rowptr[r1] : k0;
-            if (k1 > a) {
-                s = warp_range_sum(col, val, x, a, k1, lane);
-                cr = r1;
+    __syncthreads();
+    double tile_carry = 0.0;  // the open row's sum from earlier tiles of this CTA (row s_bound_r[tile])
+    for (int tile = 0; tile < ntiles; ++tile) {
+        const int ra = s_bound_r[tile], rb = s_bound_r[tile + 1];
+        const long long ka = s_bound_k[tile], kb = s_bound_k[tile + 1];
+        const int nr = rb - ra, nk = static_cast<int>(kb - ka);
+        for (int i = t; i < nr; i += kThreads) s_rend[i] = rowptr[ra + i + 1];
+        for (int i = t; i < nk; i += kThreads) {
+            const long long k = ka + i;
+            s_val[i] = __ldg(val + k);
+            s_x[i] = __ldg(x + __ldg(col + k));
+        }
+        __syncthreads();
+        // this thread's start on the tile's merge path
+        const long long da = ka + ra;
+        const long long dt = da + static_cast<long long>(t) * kIpt < kb + rb ? da + static_cast<long long>(t) * kIpt : kb + rb;
+        const long long de = dt + kIpt < kb + rb ? dt + kIpt : kb + rb;
+        long long lo = dt - kb > ra ? dt - kb : ra, hi = dt - ka < rb ? dt - ka : rb;
+        while (lo < hi) {
+            const long long mid = (lo + hi) >> 1;
+            if (s_rend[mid - ra] <= dt - mid - 1) lo = mid + 1;
+            else hi = mid;
+        }
+        int r = static_cast<int>(lo);
+        long long k = dt - lo;
+        double acc = 0.0, first_acc = 0.0;
+        int first_row = -1;
+        for (long long d = dt; d < de; ++d) {
+            if (r < rb && s_rend[r - ra] <= k) {  // row r ends here
+                if (first_row < 0) {
+                    first_row = r;
+                    first_acc = acc;
+                } else {
+                    y[r] = beta != 0.0 ? fma(beta, y[r], alpha * acc) : alpha * acc;
+                }
+                acc = 0.0;
+                ++r;
+            } else {
+                acc = fma(s_val[k - ka], s_x[k - ka], acc);
+                ++k;
             }
         }
-        if (lane == 0) {
-            carry_val[c] = s;
-            carry_row[c] = cr;
+        // thread 0's run continues the tile's carried row; the scan combines the runs across threads
+        const double own = (t == 0 && first_row < 0) ? tile_carry + acc : acc;
+        const double run = seg_scan(r, own, s_srow, s_sv);
+        // thread t - 1's run and row (every lane takes part in the shuffles)
+        const double prev = __shfl_up_sync(0xffffffffu, run, 1);
+        const int prow = __shfl_up_sync(0xffffffffu, r, 1);
+        if (first_row >= 0) {
+            // the runs of the earlier threads on this row, or the tile's carry for thread 0
+            double cin = t == 0 ? tile_carry : 0.0;
+            if ((t & 31) != 0) {
+                if (prow == first_row) cin = prev;
+            } else if (t > 0 && s_srow[(t >> 5) - 1] == first_row) {
+                cin = s_sv[(t >> 5) - 1];
+            }
+            const double tot = cin + first_acc;
+            y[first_row] = beta != 0.0 ? fma(beta, y[first_row], alpha * tot) : alpha * tot;
         }
+        // the row open at the tile's end carries into the next tile (the last thread's run)
+        if (t == kThreads - 1) s_sv[31] = run;
+        __syncthreads();
+        tile_carry = s_sv[31];
+        __syncthreads();
+    }
+    if (t == 0) {
+        // the row left open at the end of the CTA's range, if this CTA consumed any of its nonzeros
+        const int ro = s_bound_r[ntiles];
+        const long long ko = s_bound_k[ntiles], k0 = s_bound_k[0];
+        const bool open = ntiles > 0 && ro < m && ko > (rowptr[ro] > k0 ? rowptr[ro] : k0);
+        carry_val[c] = open ? tile_carry : 0.0;
+        carry_row[c] = open ? ro : -1;
     }
 }
 
