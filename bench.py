@@ -862,6 +862,44 @@ def run_spmv_only(args):
                       "env": {k: v for k, v in os.environ.items() if k.startswith("HHP_")}}), flush=True)
 
 
+def run_config_solve(args):
+    """One configuration's solve, timed alone (profiler target and per-config check): --steps solves
+    of --config in FP64 (--precision fp64) or the mixed form (--precision fp32), rtol 1e-10 (C5:
+    1e-12; C3: --iters fixed iterations, as it does not converge unpreconditioned). Prints one JSON
+    line with the median CUDA-event time, L2 flushed before each solve."""
+    import torch
+    from hethyppar_gb300 import Context, Matrix, bicgstab, synth
+    ctx = Context(0)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    flush_r = torch.ones(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def flush_l2(sync=False):
+        with torch.cuda.stream(stream):
+            flush.add_(1.0)
+            flush_r.sum()
+    s = synth.config(args.config)
+    A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
+    b = torch.as_tensor(s.b, device="cuda")
+    x = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+    kw = {"rtol": 1e-12 if args.config == "c5" else RTOL, "maxit": 50000,
+          "precision": "mixed" if args.precision == "fp32" else "fp64"}
+    if args.config == "c3":
+        kw = {"rtol": 0.0, "maxit": args.iters, "fixed_iters": True}
+    res = []
+
+    def run():
+        x.zero_()
+        res.append(bicgstab(ctx, A, b, x, **kw)[1])
+    for _ in range(args.warmup):
+        run()
+    ms = _event_ms(stream, run, flush_l2, args.steps)
+    r = res[-1]
+    print(json.dumps({"mode": "solve-config", "config": args.config, "precision": kw.get("precision", "fp64"),
+                      "ms": ms, "iters": r.iters, "us_per_iter": ms * 1e3 / max(r.iters, 1),
+                      "rel_res_true": r.rel_res_true, "status": r.status}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -871,13 +909,18 @@ def main():
     ap.add_argument("--no-extras", dest="extras", action="store_false")
     ap.add_argument("--extra-reps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mode", default="solve", choices=["solve", "spmv"],
-                    help="spmv: time the SpMV kernel alone on --config (kernel sweeps, profiler target)")
+    ap.add_argument("--mode", default="solve", choices=["solve", "spmv", "solve-config"],
+                    help="spmv: time the SpMV kernel alone on --config (kernel sweeps, profiler target); "
+                         "solve-config: time the solve of --config alone")
+    ap.add_argument("--iters", type=int, default=200, help="solve-config on c3: fixed iterations")
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     args = ap.parse_args()
     if args.mode == "spmv":
         run_spmv_only(args)
+        return
+    if args.mode == "solve-config":
+        run_config_solve(args)
         return
     from hethyppar_gb300 import dist
     rk = dist.init_from_env()
