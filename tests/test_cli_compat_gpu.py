@@ -110,6 +110,18 @@ def test_cli_rcm_reorder():
         assert r.returncode != 0 and "exclusive" in r.stdout
 
 
+@pytest.mark.parametrize("precond", ["jacobi", "jacobi_row"])
+def test_cli_preconditioners(precond):
+    g = load_golden("sample320")
+    with tempfile.TemporaryDirectory() as td:
+        p = _files(td, g)
+        out = os.path.join(td, "X.txt")
+        kv, _ = _run(["-m", p["A"], "-x", p["x0"], "-y", p["b"], "-o", out, "--precond", precond, "-n", "500",
+                      "--rtol", "1e-11", "--out-format", "exact"])
+        assert float(kv["relative_residual"]) <= 1e-11
+        assert np.max(np.abs(np.loadtxt(out) - np.arange(1, 321))) < 1e-6
+
+
 def test_spmv_cli_known_answer():
     """hhp-spmv, the spmv-gpu drop-in: A X_mul = [1..16] (the reference's data/sample X_mul), the
     same stdout keys, and Y bit-identical to the oracle's fused row sums."""
