@@ -241,7 +241,7 @@ int main(int argc, char **argv) {
     o.rtol = a.rtol;
     o.maxit = a.n_iters;
     o.precision = a.mixed ? HHP_PREC_MIXED : HHP_PREC_FP64;
-    o.inner_rtol = 0.1;
+    o.inner_rtol = 0.05;
     o.precond = a.jacobi;
     o.loop = a.loop;
     o.fixed_iters = a.fixed;

@@ -490,7 +490,7 @@ static hhp_solve_opts default_opts() {
     o.rtol = 1e-10;
     o.maxit = 2000;
     o.precision = HHP_PREC_FP64;
-    o.inner_rtol = 0.1;
+    o.inner_rtol = 0.05;
     o.max_outer = 50;
     return o;
 }
@@ -546,6 +546,7 @@ hhp_status hhp_bicgstab_backward_dev(hhp_ctx *ctx, hhp_mat *A, const double *x, 
         return HHP_ERR_ARG;
     }
     hhp_solve_opts o = opts ? *opts : default_opts();
+    if (!opts) o.inner_rtol = 0.0;  // the adjoint's own default factor
     o.fixed_iters = 0;
     return backward_dev(A, x, dldx, dldb, dlda, &o, info);
     HHP_API_END
@@ -571,6 +572,7 @@ hhp_status hhp_bicgstab_backward(hhp_ctx *ctx, hhp_mat *A, const double *x, cons
     }
     if (rc == HHP_OK) {
         hhp_solve_opts o = opts ? *opts : default_opts();
+        if (!opts) o.inner_rtol = 0.0;  // the adjoint's own default factor
         o.fixed_iters = 0;
         rc = backward_dev(A, dx, dg, db, dlda ? da : nullptr, &o, info);
     }

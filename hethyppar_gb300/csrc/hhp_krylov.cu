@@ -1852,7 +1852,7 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
         if (use_graph && !gm) HHP_TRY(build_gmix(s, merged32));
         DevScal &h32 = *s->h_sc32;
         h32.rtol2 = o->rtol * o->rtol;
-        const double delta = o->inner_rtol > 0.0 ? o->inner_rtol : 0.1;
+        const double delta = o->inner_rtol > 0.0 ? o->inner_rtol : 0.05;
         h32.inner_rtol2 = delta * delta;
         h32.maxit = o->maxit;
         h32.fixed = 0;
@@ -1971,6 +1971,10 @@ hhp_status backward_dev(hhp_mat *A, const double *x_dev, const double *g_dev, do
     HHP_CUDA(cudaMemsetAsync(dldb_dev, 0, sizeof(double) * static_cast<size_t>(A->n), st));
     hhp_solve_opts oa = *o;
     if (oa.loop == HHP_LOOP_AUTO) oa.loop = HHP_LOOP_CLASSIC;
+    // Adjoint tolerances sit near the FP64 rounding floor: the mixed form hands over to FP64
+    // earlier there (0.1 rather than the solves' 0.05), which on the 1024x1024 stencil reached
+    // 2.8e-12 where 0.05 stalled at 1.3e-11.
+    if (oa.inner_rtol <= 0.0) oa.inner_rtol = 0.1;
     hhp_status rc = solve_dev(A->t, g_dev, dldb_dev, nullptr, &oa, info);
     if (rc != HHP_OK && rc != HHP_ERR_MAXIT) return rc;
     if (dlda_dev) HHP_TRY(launch_dlda(A, st, dldb_dev, x_dev, dlda_dev));

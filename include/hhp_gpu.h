@@ -76,7 +76,8 @@ typedef struct {
     int precision;      /* hhp_precision                                                          */
     double inner_rtol;  /* mixed form: the FP32 recurrences run until their residual has dropped by
                            this factor since the last FP64 refinement step x += d,
-                           r = b - A x (<= 0: 0.1)                                               */
+                           r = b - A x (<= 0: 0.05 for solves, 0.1 for the adjoint entry points,
+                           whose tolerances sit near the FP64 rounding floor)                    */
     int max_outer;      /* FP64 form: cap on residual-replacement restarts (<= 0: 50)            */
     int fixed_iters;    /* 1: run exactly maxit iterations with no stop test, like the reference's
                            executables (src/entry/bicgstab_cpu.c:200); FP64 only                  */
