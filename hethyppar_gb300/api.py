@@ -236,6 +236,20 @@ class Matrix:
         with _Ordered(self.ctx, x, y):
             check(lib().hhp_spmv_t_dev(self.ctx.handle, self._h, _ptr(x), _ptr(y)), "hhp_spmv_t_dev")
 
+    # -- ILU(0) ----------------------------------------------------------------------------------
+    def ilu0_factor(self):
+        """ILU(0) factors (hhp_ilu0_factor), built on the device if needed -> (lu in CSR order:
+        L's multipliers below the diagonal, U on and above; (levels of L, levels of U))."""
+        lu = np.empty(max(self.nnz, 1), np.float64)
+        lev = (ctypes.c_int * 2)()
+        check(lib().hhp_ilu0_factor(self.ctx.handle, self._h, _ptr(lu), lev), "hhp_ilu0_factor")
+        return lu[:self.nnz], (lev[0], lev[1])
+
+    def ilu0_apply_dev(self, r, z):
+        """z = U^-1 L^-1 r on device tensors, on the context's stream (asynchronous)."""
+        with _Ordered(self.ctx, r, z):
+            check(lib().hhp_ilu0_apply_dev(self.ctx.handle, self._h, _ptr(r), _ptr(z)), "hhp_ilu0_apply_dev")
+
 
 @dataclass
 class SolveResult:
@@ -255,7 +269,7 @@ class SolveResult:
         return self.status == 0
 
 
-PRECONDS = {"none": 0, "jacobi": 1, "jacobi_row": 2}
+PRECONDS = {"none": 0, "jacobi": 1, "jacobi_row": 2, "ilu0": 3}
 # FP64 iteration schedule (hhp_loop): "merged" = 4 kernels per iteration, stop tests and beta from
 # the t = A s dot products; "classic" = the reference's order, rho and ||r|| as direct dot
 # products; "auto" = merged for forward solves, classic for the adjoint solve
@@ -372,6 +386,18 @@ def reorder_rcm(rowptr, col) -> np.ndarray:
     perm = np.empty(max(m, 0), np.int32)
     check(lib().hhp_reorder_rcm(m, _ptr(rp), _ptr(cl), _ptr(perm)), "hhp_reorder_rcm")
     return perm
+
+
+def reorder_color(rowptr, col):
+    """Multicolour order of a square CSR pattern (hhp_reorder_color, host only) for ILU(0) ->
+    (perm in csr_permute's convention, number of colours)."""
+    rp = _host(rowptr, np.int32)
+    cl = _host(col, np.int32)
+    m = rp.size - 1
+    perm = np.empty(max(m, 1), np.int32)
+    nc = ctypes.c_int()
+    check(lib().hhp_reorder_color(m, _ptr(rp), _ptr(cl), _ptr(perm), ctypes.byref(nc)), "hhp_reorder_color")
+    return perm[:m], nc.value
 
 
 def vector_read(path: str, size: int) -> np.ndarray:

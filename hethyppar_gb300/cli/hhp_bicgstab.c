@@ -18,7 +18,10 @@
  *   --print-every K   print "Iteration = i; Error Norm = e" every K iterations
  *                     (gpu_BiCGStab's per-iteration line, bicgstab_gpu.c:156)
  *   --out-format F    compat (default, "%lf" like vector_write) | exact ("%.17g")
- *   --reorder rcm     reverse Cuthill-McKee row/column order (instead of a --perm file)
+ *   --reorder R       rcm: reverse Cuthill-McKee row/column order; color: multicolour order, for
+ *                     --precond ilu0 (either instead of a --perm file)
+ *   --precond P       none (default) | jacobi | jacobi_row | ilu0 (the SpSV path that
+ *                     bicgstab_gpu.c:185-201 leaves commented out)
  *   --loop L          auto (default: merged) | merged (4 kernels per iteration) | classic (the
  *                     reference's dot products; --fixed always runs it)
  *
@@ -59,11 +62,13 @@ static struct argp_option options[] = {
     {"out-format", OPT_OUTFMT, "compat|exact", 0, "Number format of the output X file", 0},
     {"device", OPT_DEVICE, "ID", 0, "CUDA device (default 0)", 0},
     {"write-csr", OPT_WCSR, "FILE", 0, "Also store the matrix as a binary CSR file (later runs: -m FILE)", 0},
-    {"precond", OPT_PRECOND, "none|jacobi|jacobi_row", 0,
-     "Preconditioner: none (default, as the reference), jacobi (columns scaled by the diagonal), jacobi_row (rows)",
+    {"precond", OPT_PRECOND, "none|jacobi|jacobi_row|ilu0", 0,
+     "Preconditioner: none (default, as the reference), jacobi (columns scaled by the diagonal), jacobi_row (rows), "
+     "ilu0 (incomplete LU, the reference's commented SpSV path)",
      0},
-    {"reorder", OPT_REORDER, "none|rcm", 0,
-     "Row/column reordering for locality: rcm = reverse Cuthill-McKee (instead of a --perm file)", 0},
+    {"reorder", OPT_REORDER, "none|rcm|color", 0,
+     "Row/column reordering (instead of a --perm file): rcm = reverse Cuthill-McKee for locality, color = "
+     "multicolour order, which lets ilu0's triangular solves run one colour at a time", 0},
     {"loop", OPT_LOOP, "auto|merged|classic", 0,
      "FP64 iteration schedule: merged (the default for a solve, 4 kernels per iteration) or classic (the reference's dot products)", 0},
     {0}};
@@ -96,6 +101,7 @@ static error_t parse_opt(int key, char *arg, struct argp_state *state) {
         case OPT_WCSR: a->write_csr = arg; break;
         case OPT_REORDER:
             if (strcmp(arg, "rcm") == 0) a->rcm = 1;
+            else if (strcmp(arg, "color") == 0) a->rcm = 2;
             else if (strcmp(arg, "none") == 0) a->rcm = 0;
             else argp_error(state, "unknown reordering '%s'", arg);
             break;
@@ -108,6 +114,7 @@ static error_t parse_opt(int key, char *arg, struct argp_state *state) {
         case OPT_PRECOND:
             if (strcmp(arg, "jacobi") == 0) a->jacobi = HHP_PRECOND_JACOBI;
             else if (strcmp(arg, "jacobi_row") == 0) a->jacobi = HHP_PRECOND_JACOBI_ROW;
+            else if (strcmp(arg, "ilu0") == 0) a->jacobi = HHP_PRECOND_ILU0;
             else if (strcmp(arg, "none") == 0) a->jacobi = HHP_PRECOND_NONE;
             else argp_error(state, "unknown preconditioner '%s'", arg);
             break;
@@ -174,7 +181,7 @@ int main(int argc, char **argv) {
     if (access(a.input_x, F_OK) == -1) FAIL("Input X '%s' does not exist", a.input_x);
     if (access(a.input_y, F_OK) == -1) FAIL("Input B '%s' does not exist", a.input_y);
     if (a.n_iters < 0) FAIL("-n must be >= 0");
-    if (a.rcm && a.perm) FAIL("--reorder rcm and --perm are exclusive");
+    if (a.rcm && a.perm) FAIL("--reorder and --perm are exclusive");
 
     /* HHP_PROFILE (set, not "0"): phase times as extra "profile_* : value" lines, and a second,
      * warm solve from the same start that separates one-time setup (slice layout, graph capture)
@@ -218,7 +225,12 @@ int main(int argc, char **argv) {
         int *rp = malloc(sizeof(int) * ((size_t)m + 1)), *cl = malloc(sizeof(int) * (size_t)(nnz > 0 ? nnz : 1));
         double *vl = malloc(sizeof(double) * (size_t)(nnz > 0 ? nnz : 1));
         CHECK(hhp_mat_get_csr(A, rp, cl, vl));
-        if (a.rcm) CHECK(hhp_reorder_rcm(m, rp, cl, perm));
+        if (a.rcm == 1) CHECK(hhp_reorder_rcm(m, rp, cl, perm));
+        if (a.rcm == 2) {
+            int colors = 0;
+            CHECK(hhp_reorder_color(m, rp, cl, perm, &colors));
+            printf("colors : %d\n", colors);
+        }
         hhp_mat_destroy(A);
         A = NULL;
         CHECK(hhp_mat_from_csr(ctx, m, n, nnz, rp, cl, vl, perm, &A));

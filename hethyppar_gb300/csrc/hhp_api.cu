@@ -366,6 +366,7 @@ void hhp_mat_destroy(hhp_mat *A) {
     if (A->ctx && A->ctx->stream) cudaStreamSynchronize(A->ctx->stream);
     if (A->t) hhp_mat_destroy(A->t);
     release_jacobi(A);
+    release_ilu(A);
     solver_release(A->solver);
     A->plan64.release();
     A->plan32.release();
@@ -396,6 +397,7 @@ static hhp_status set_values(hhp_mat *A, const double *v, cudaMemcpyKind kind) {
     if (A->val32 || A->t || A->plan64.built() || A->plan32.built()) HHP_TRY(mat_refresh_derived(A));
     HHP_CUDA(cudaStreamSynchronize(A->ctx->stream));
     release_jacobi(A);  // rebuilt from the new values on the next preconditioned solve
+    release_ilu(A);
     return HHP_OK;
 }
 
@@ -506,7 +508,7 @@ static hhp_status check_solve(hhp_ctx *ctx, hhp_mat *A, const void *b, const voi
     }
     if (o && (o->maxit < 0 || !(o->rtol >= 0.0) || (o->precision != HHP_PREC_FP64 && o->precision != HHP_PREC_MIXED) ||
               (o->precond != HHP_PRECOND_NONE && o->precond != HHP_PRECOND_JACOBI &&
-               o->precond != HHP_PRECOND_JACOBI_ROW) ||
+               o->precond != HHP_PRECOND_JACOBI_ROW && o->precond != HHP_PRECOND_ILU0) ||
               (o->loop != HHP_LOOP_AUTO && o->loop != HHP_LOOP_MERGED && o->loop != HHP_LOOP_CLASSIC))) {
         set_error("bicgstab: invalid options (maxit %d, rtol %g, precision %d, precond %d, loop %d)", o->maxit,
                   o->rtol, o->precision, o->precond, o->loop);
@@ -534,6 +536,30 @@ hhp_status hhp_bicgstab_dev(hhp_ctx *ctx, hhp_mat *A, const double *b, double *x
     if (o.precond == HHP_PRECOND_JACOBI) return solve_jacobi(A, b, x, xt, &o, info, false);
     if (o.precond == HHP_PRECOND_JACOBI_ROW) return solve_jacobi_row(A, b, x, xt, &o, info, false);
     return solve_any(A, b, x, xt, &o, info, false);
+    HHP_API_END
+}
+
+hhp_status hhp_ilu0_factor(hhp_ctx *ctx, hhp_mat *A, double *lu, int *levels) {
+    HHP_API_BEGIN
+    if (!ctx || !A || A->ctx != ctx) {
+        set_error("ilu0_factor: null argument or matrix from another context");
+        return HHP_ERR_ARG;
+    }
+    HHP_TRY(ensure_ilu(A, levels));
+    if (lu) HHP_TRY(ilu_factors(A, lu));
+    return HHP_OK;
+    HHP_API_END
+}
+
+hhp_status hhp_ilu0_apply_dev(hhp_ctx *ctx, hhp_mat *A, const double *r_dev, double *z_dev) {
+    HHP_API_BEGIN
+    if (!ctx || !A || A->ctx != ctx || !r_dev || !z_dev) {
+        set_error("ilu0_apply: null argument or matrix from another context");
+        return HHP_ERR_ARG;
+    }
+    HHP_TRY(ensure_ilu(A));
+    HHP_CUDA(cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), ctx->stream));
+    return launch_ilu_apply(A, ctx->stream, r_dev, z_dev, nullptr);
     HHP_API_END
 }
 

@@ -113,6 +113,7 @@ struct PlanDev {
 
 // ---- context and matrix ------------------------------------------------------------------------
 struct Solver;  // per-matrix solver workspace (hhp_krylov.cu)
+struct IluDev;  // ILU(0) factors and their level-ordered solve layouts (hhp_ilu.cu)
 
 }  // namespace hhp
 
@@ -150,6 +151,7 @@ struct hhp_mat {
     // row (left) Jacobi: A with row i scaled by 1/a_ii, and room for the scaled right-hand side
     hhp_mat *jac_row = nullptr;
     double *jac_row_b = nullptr;
+    hhp::IluDev *ilu = nullptr;       // ILU(0) factors (lazily built)
 };
 
 namespace hhp {
@@ -200,6 +202,15 @@ hhp_status solve_jacobi(hhp_mat *A, const double *b, double *x, const double *xt
 // Row (left) Jacobi: BiCGStab on diag(A)^-1 A x = diag(A)^-1 b until b - A x meets rtol.
 hhp_status solve_jacobi_row(hhp_mat *A, const double *b, double *x, const double *xt, const hhp_solve_opts *o,
                             hhp_solve_info *info, bool host);
+// ILU(0) (hhp_ilu.cu): factors A on the device (levels[2], nullable: the level counts of L and U);
+// out = U^-1 L^-1 in as two cooperative launches on `st` (nothing when *stop != 0); the factors
+// in A's CSR order, to the host.
+hhp_status ensure_ilu(hhp_mat *A, int *levels = nullptr);
+void release_ilu(hhp_mat *A);
+hhp_status launch_ilu_apply(hhp_mat *A, cudaStream_t st, const double *in, double *out, const int *stop);
+hhp_status ilu_factors(hhp_mat *A, double *lu_host);
+// Identifies the current factorization (0: none); graphs that captured its arrays compare it.
+long long ilu_generation(const hhp_mat *A);
 // Adjoint: lambda = A^-T g; dlda[k] = -lambda[row(k)] * x[col(k)].
 hhp_status backward_dev(hhp_mat *A, const double *x_dev, const double *g_dev, double *dldb_dev, double *dlda_dev,
                         const hhp_solve_opts *o, hhp_solve_info *info);

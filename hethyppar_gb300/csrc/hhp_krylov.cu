@@ -79,6 +79,11 @@ struct Solver {
     cudaStream_t s2 = nullptr, s3 = nullptr;  // capture streams: loop body, IF body
     cudaEvent_t ev_in = nullptr;              // joins the two input uploads
     cudaGraphExec_t g64 = nullptr, g64m = nullptr, gmix = nullptr, gmixm = nullptr;  // classic / merged
+    // ILU(0)-preconditioned FP64 loop: p^ and s^, and its graph with the factorization generation
+    // it was captured against (a refactorization reallocates the factors)
+    double *PH = nullptr, *SH = nullptr;
+    cudaGraphExec_t g64i = nullptr;
+    long long g64i_gen = 0;
     int g64_kernels_pro = 0, g64_kernels_epi = 0, gmix_kernels_pro = 0, gmix_kernels_epi = 0, unroll = 4;
 };
 
@@ -470,11 +475,12 @@ __global__ void __launch_bounds__(512) k_s(DevScal *sc, T *S, const T *R, const 
 }
 
 // K_XR: omega = (t.s)/(t.t), x += alpha p + omega s, r = s - omega t, partials (r.r0, r.r).
-// Half step (||s|| below the threshold): x += alpha p, r = s.
-template <typename T>
+// Half step (||s|| below the threshold): x += alpha p, r = s. PC (right preconditioning): the
+// directions added to x are P = M^-1 p and SX = M^-1 s, while r is formed from s itself.
+template <typename T, bool PC = false>
 __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P, const T *S, const T *Tv,
                                             const T *R0, int nu, SpmvParts sp, const double *part_s, int nparts,
-                                            double *part_xr) {
+                                            double *part_xr, const T *SX) {
     const bool dead = dead_step(sc);  // tested after the operand and record loads are in flight
     const double thr2 = sc->thr2_rec, alpha = sc->alpha;  // read with the operand loads
     __shared__ double red[kRedScratch];
@@ -484,7 +490,7 @@ __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P,
     const int stride = gridDim.x * blockDim.x, u0 = blockIdx.x * blockDim.x + threadIdx.x;
     // operands of the first kPre units requested before the reductions (t too: the rare half
     // step, known only after them, does not need it)
-    T x[kPre][E], p[kPre][E], s[kPre][E], r0[kPre][E], t[kPre][E];
+    T x[kPre][E], p[kPre][E], s[kPre][E], r0[kPre][E], t[kPre][E], sx[PC ? kPre : 1][E];
 #pragma unroll
     for (int k = 0; k < kPre; ++k) {
         const int u = u0 + k * stride;
@@ -494,6 +500,7 @@ __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P,
             ldu(s[k], S, u);
             ldu(r0[k], R0, u);
             ldu(t[k], Tv, u);
+            if constexpr (PC) ldu(sx[k], SX, u);
         }
     }
     double q[4];  // t.s, t.t (2-wide SpMV records), s.s (4-wide K_S records)
@@ -526,12 +533,13 @@ __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P,
     const T ta = static_cast<T>(bc[0]), tw = static_cast<T>(bc[1]), tnw = static_cast<T>(-bc[1]);
     double acc[2] = {0.0, 0.0};
     // x += alpha p + omega s, r = s - omega t (half step: x += alpha p, r = s); (r.r0, r.r)
-    auto unit = [&](int u, T(&xx)[E], const T(&pp)[E], const T(&ss)[E], const T(&rr0)[E], const T(&tt)[E]) {
+    auto unit = [&](int u, T(&xx)[E], const T(&pp)[E], const T(&ss)[E], const T(&rr0)[E], const T(&tt)[E],
+                    const T(&sxx)[E]) {
         T r[E];
         if (!half) {
 #pragma unroll
             for (int e = 0; e < E; ++e) {
-                xx[e] = tfma(tw, ss[e], tfma(ta, pp[e], xx[e]));
+                xx[e] = tfma(tw, PC ? sxx[e] : ss[e], tfma(ta, pp[e], xx[e]));
                 r[e] = tfma(tnw, tt[e], ss[e]);
             }
         } else {
@@ -549,7 +557,7 @@ __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P,
 #pragma unroll
     for (int k = 0; k < kPre; ++k) {
         const int u = u0 + k * stride;
-        if (u < nu) unit(u, x[k], p[k], s[k], r0[k], t[k]);
+        if (u < nu) unit(u, x[k], p[k], s[k], r0[k], t[k], sx[PC ? k : 0]);
     }
     // whole batches of kPre units, then the last few one at a time (see K_P)
     int ub = u0 + kPre * stride;
@@ -561,18 +569,20 @@ __global__ void __launch_bounds__(512) k_xr(DevScal *sc, T *X, T *R, const T *P,
             ldu(s[k], S, ub + k * stride);
             ldu(r0[k], R0, ub + k * stride);
             ldu(t[k], Tv, ub + k * stride);
+            if constexpr (PC) ldu(sx[k], SX, ub + k * stride);
         }
 #pragma unroll
-        for (int k = 0; k < kPre; ++k) unit(ub + k * stride, x[k], p[k], s[k], r0[k], t[k]);
+        for (int k = 0; k < kPre; ++k) unit(ub + k * stride, x[k], p[k], s[k], r0[k], t[k], sx[PC ? k : 0]);
     }
     for (int u = ub; u < nu; u += stride) {
-        T xx[E], pp[E], ss[E], rr0[E], tt[E];
+        T xx[E], pp[E], ss[E], rr0[E], tt[E], sxx[E];
         ldu(xx, X, u);
         ldu(pp, P, u);
         ldu(ss, S, u);
         ldu(rr0, R0, u);
         ldu(tt, Tv, u);
-        unit(u, xx, pp, ss, rr0, tt);
+        if constexpr (PC) ldu(sxx, SX, u);
+        unit(u, xx, pp, ss, rr0, tt, sxx);
     }
     block_sum<2>(acc, red);
     if (threadIdx.x == 0) {
@@ -1237,7 +1247,8 @@ hhp_status ensure_solver(hhp_mat *A, Solver **out, int maxit) {
         if (s->g64m) cudaGraphExecDestroy(s->g64m);
         if (s->gmix) cudaGraphExecDestroy(s->gmix);
         if (s->gmixm) cudaGraphExecDestroy(s->gmixm);
-        s->g64 = s->g64m = s->gmix = s->gmixm = nullptr;
+        if (s->g64i) cudaGraphExecDestroy(s->g64i);
+        s->g64 = s->g64m = s->gmix = s->gmixm = s->g64i = nullptr;
     }
     *out = s;
     return HHP_OK;
@@ -1350,7 +1361,7 @@ hhp_status end_if_body(Solver *s, hhp_status rc) {
 // the skipped launches after it.
 template <typename T>
 hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R, T *R0, T *P, T *V, T *S, T *Tv,
-                        double *part_xr, double *part_s, bool fp32, bool merged) {
+                        double *part_xr, double *part_s, bool fp32, bool merged, bool ilu = false) {
     hhp_mat *A = s->A;
     constexpr int E = Unit<T>::E;
     const int nu = s->n_pad / E, nu4 = s->n_pad / 4;
@@ -1417,6 +1428,32 @@ hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R,
             st = end_if_body(s, st);
             continue;
         }
+        if constexpr (std::is_same<T, double>::value) {
+            if (ilu) {
+                // right ILU(0) preconditioning, the classic schedule with p^ = M^-1 p and
+                // s^ = M^-1 s: [M^-1 p, SpMV v = A p^ + r0.v, K_S, M^-1 s, SpMV t = A s^ + t.s/t.t,
+                // K_XR (x += alpha p^ + omega s^, r = s - omega t), K_P]
+                st = launch_ilu_apply(A, s->s2, P, s->PH, stop);
+                if (st == HHP_OK) st = launch_spmv64(A, s->s2, EP_DOT1, s->PH, V, R0, 1.0, 0.0, nullptr, nullptr, stop);
+                if (st != HHP_OK) break;
+                if (launch_k(k_s<double>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, sc, S, R, V, R0, nu, parts_of(pl),
+                             part_s) != cudaSuccess) {
+                    st = HHP_ERR_CUDA;
+                    break;
+                }
+                st = launch_ilu_apply(A, s->s2, S, s->SH, stop);
+                if (st == HHP_OK) st = launch_spmv64(A, s->s2, EP_DOT2, s->SH, Tv, S, 1.0, 0.0, nullptr, nullptr, stop);
+                if (st != HHP_OK) break;
+                if (launch_k(k_xr<double, true>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, sc, X, R,
+                             static_cast<const double *>(s->PH), S, Tv, R0, nu, parts_of(pl), part_s, s->nblk, part_xr,
+                             static_cast<const double *>(s->SH)) != cudaSuccess) {
+                    st = HHP_ERR_CUDA;
+                    break;
+                }
+                st = kp(s->s2, cond, k == 0 ? 1 : 0);
+                continue;
+            }
+        }
         if (fp32)
             st = launch_spmv32(A, s->s2, EP_DOT1, reinterpret_cast<const float *>(P), reinterpret_cast<float *>(V),
                                reinterpret_cast<const float *>(R0), stop);
@@ -1438,7 +1475,7 @@ hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R,
                                nullptr, stop);
         if (st != HHP_OK) break;
         if (launch_k(k_xr<T>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, sc, X, R, P, S, Tv, R0, nu, parts_of(pl),
-                     part_s, s->nblk, part_xr) != cudaSuccess) {
+                     part_s, s->nblk, part_xr, static_cast<const T *>(S)) != cudaSuccess) {
             st = HHP_ERR_CUDA;
             break;
         }
@@ -1481,7 +1518,7 @@ hhp_status launch_x0check(Solver *s, cudaStream_t st) {
 // The FP64 loop launched kernel by kernel (no graph), for profilers that cannot see inside
 // conditional graph nodes: same kernels and order; the host reads the status every `unroll`
 // iterations. Selected with HHP_SOLVE_GRAPH=0.
-hhp_status run_direct64(Solver *s, bool merged) {
+hhp_status run_direct64(Solver *s, bool merged, bool ilu) {
     hhp_mat *A = s->A;
     cudaStream_t st = A->ctx->stream;
     const int nu = s->n_pad / 2;
@@ -1515,12 +1552,26 @@ hhp_status run_direct64(Solver *s, bool merged) {
                 continue;
             }
             HHP_TRY(kp(k == 0));
-            HHP_TRY(launch_spmv64(A, st, EP_DOT1, s->P, s->V, s->R0, 1.0, 0.0, nullptr, nullptr, stop));
+            const double *pv = s->P, *sv = s->S;
+            if (ilu) {
+                HHP_TRY(launch_ilu_apply(A, st, s->P, s->PH, stop));
+                pv = s->PH;
+            }
+            HHP_TRY(launch_spmv64(A, st, EP_DOT1, pv, s->V, s->R0, 1.0, 0.0, nullptr, nullptr, stop));
             HHP_CUDA(launch_k(k_s<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->S, s->R, s->V, s->R0, nu,
                               parts_of(pl), s->part_s));
-            HHP_TRY(launch_spmv64(A, st, EP_DOT2, s->S, s->T, s->S, 1.0, 0.0, nullptr, nullptr, stop));
-            HHP_CUDA(launch_k(k_xr<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->X, s->R, s->P, s->S, s->T,
-                              s->R0, nu, parts_of(pl), s->part_s, s->nblk, s->part_xr));
+            if (ilu) {
+                HHP_TRY(launch_ilu_apply(A, st, s->S, s->SH, stop));
+                sv = s->SH;
+            }
+            HHP_TRY(launch_spmv64(A, st, EP_DOT2, sv, s->T, s->S, 1.0, 0.0, nullptr, nullptr, stop));
+            if (ilu)
+                HHP_CUDA(launch_k(k_xr<double, true>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->X, s->R, pv, s->S,
+                                  s->T, s->R0, nu, parts_of(pl), s->part_s, s->nblk, s->part_xr, sv));
+            else
+                HHP_CUDA(launch_k(k_xr<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->X, s->R, s->P, s->S,
+                                  s->T, s->R0, nu, parts_of(pl), s->part_s, s->nblk, s->part_xr,
+                                  static_cast<const double *>(s->S)));
             A->ctx->kernel_launches += 2;
         }
         HHP_CUDA(cudaMemcpyAsync(s->h_sc, s->sc, sizeof(DevScal), cudaMemcpyDeviceToHost, st));
@@ -1536,7 +1587,7 @@ hhp_status run_direct64(Solver *s, bool merged) {
 
 // FP64 solve graph (classic or merged loop): ctl copy, x0 check, residual SpMV (skipped for
 // x0 = 0), init, WHILE{loop}, true-residual SpMV, finish.
-hhp_status build_g64(Solver *s, bool merged) {
+hhp_status build_g64(Solver *s, bool merged, bool ilu = false) {
     hhp_mat *A = s->A;
     cudaStream_t st = A->ctx->stream;
     HHP_TRY(ensure_plan(A, false));
@@ -1555,7 +1606,7 @@ hhp_status build_g64(Solver *s, bool merged) {
         HHP_CUDA(launch_k(k_init<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->R, s->B, s->R0, s->P, s->V,
                           nu, parts_of(A->plan64), s->x0_nz, s->part_b, s->nblk, s->part_xr, s->part_s));
         rc = capture_loop<double>(s, st, s->sc, s->X, s->R, s->R0, s->P, s->V, s->S, s->T, s->part_xr, s->part_s,
-                                  false, merged);
+                                  false, merged && !ilu, ilu);
         if (rc != HHP_OK) break;
         rc = launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0);
         if (rc != HHP_OK) break;
@@ -1568,14 +1619,16 @@ hhp_status build_g64(Solver *s, bool merged) {
         return rc;
     }
     HHP_CUDA(e);
-    cudaGraphExec_t &ge = merged ? s->g64m : s->g64;
+    cudaGraphExec_t &ge = ilu ? s->g64i : merged ? s->g64m : s->g64;
     cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
     cudaGraphDestroy(g);
     HHP_CUDA(ie);
     s->g64_kernels_pro = 4;
     s->g64_kernels_epi = 2;
-    // launch_spmv64 counted its captured launches; graph launches are counted when executed.
-    A->ctx->kernel_launches -= 2 + 2 * s->unroll;
+    // launch_spmv64 / launch_ilu_apply counted their captured launches; graph launches are counted
+    // when executed.
+    A->ctx->kernel_launches -= 2 + (ilu ? 6 : 2) * s->unroll;
+    if (ilu) s->g64i_gen = ilu_generation(A);
     return HHP_OK;
 }
 
@@ -1683,7 +1736,8 @@ hhp_status run_direct_mix(Solver *s, bool merged) {
                                   s->R0_32, nu4, parts_of(pl), s->part_s32));
                 HHP_TRY(launch_spmv32(A, st, EP_DOT2, s->S32, s->T32, s->S32, stop));
                 HHP_CUDA(launch_k(k_xr<float>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc32, s->D32, s->R32, s->P32,
-                                  s->S32, s->T32, s->R0_32, nu4, parts_of(pl), s->part_s32, s->nblk, s->part_xr32));
+                                  s->S32, s->T32, s->R0_32, nu4, parts_of(pl), s->part_s32, s->nblk, s->part_xr32,
+                                  static_cast<const float *>(s->S32)));
                 nk += 1;
                 HHP_CUDA(launch_k(k_p_ru, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc32, s->X, s->D32, s->P32, s->V32,
                                   s->R32, nu4, s->part_xr32, s->part_s32, s->nblk, s->hist, s->hist_cap, none, none,
@@ -1746,8 +1800,26 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
     hhp_ctx *ctx = A->ctx;
     cudaStream_t st = ctx->stream;
     const bool mixed = o->precision == HHP_PREC_MIXED;
+    const bool ilu = o->precond == HHP_PRECOND_ILU0;
+    if (ilu && mixed) {
+        set_error("ilu0 preconditioning runs in FP64 only");
+        return HHP_ERR_ARG;
+    }
     Solver *s = nullptr;
     HHP_TRY(ensure_solver(A, &s, o->maxit));
+    if (ilu) {
+        HHP_TRY(ensure_ilu(A));
+        if (!s->PH) {
+            hhp_status ast = HHP_OK;
+            s->PH = dalloc<double>(static_cast<size_t>(s->n_pad), ast, ctx->stream);
+            s->SH = dalloc<double>(static_cast<size_t>(s->n_pad), ast, ctx->stream);
+            HHP_TRY(ast);
+        }
+        if (s->g64i && s->g64i_gen != ilu_generation(A)) {
+            cudaGraphExecDestroy(s->g64i);
+            s->g64i = nullptr;
+        }
+    }
     if (mixed) HHP_TRY(ensure_fp32_inner(A, s));
     HHP_CUDA(cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), st));
     HHP_TRY(copy_in(s->B, b_in, A->m, st, host));
@@ -1793,10 +1865,11 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
         // the merged loop unless the caller asked for the classic one or for the reference's
         // fixed-iteration runs (which follow its dot products exactly); an adjoint solve has
         // resolved AUTO to CLASSIC before it gets here
-        const bool merged = o->loop != HHP_LOOP_CLASSIC && !h.fixed;
-        cudaGraphExec_t &ge = merged ? s->g64m : s->g64;
-        if (use_graph && !ge) HHP_TRY(build_g64(s, merged));
-        const long long per_iter = merged ? 4 : 5;
+        // (ILU(0) runs the classic schedule with its two applications, 4 more kernels)
+        const bool merged = o->loop != HHP_LOOP_CLASSIC && !h.fixed && !ilu;
+        cudaGraphExec_t &ge = ilu ? s->g64i : merged ? s->g64m : s->g64;
+        if (use_graph && !ge) HHP_TRY(build_g64(s, merged, ilu));
+        const long long per_iter = ilu ? 9 : merged ? 4 : 5;
         h.maxit = o->maxit - it_before;
         int dev_status = ST_RUNNING;
         double prev_true = INFINITY;
@@ -1806,7 +1879,7 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
             if (use_graph) {
                 HHP_CUDA(cudaGraphLaunch(ge, st));
             } else {
-                HHP_TRY(run_direct64(s, merged));
+                HHP_TRY(run_direct64(s, merged, ilu));
             }
             HHP_TRY(readback(s->h_sc, s->sc));
             ++outer;
@@ -1943,8 +2016,9 @@ void solver_release(Solver *s) {
     if (s->g64m) cudaGraphExecDestroy(s->g64m);
     if (s->gmix) cudaGraphExecDestroy(s->gmix);
     if (s->gmixm) cudaGraphExecDestroy(s->gmixm);
+    if (s->g64i) cudaGraphExecDestroy(s->g64i);
     double *d[] = {s->X, s->B, s->R, s->R0, s->P, s->V, s->S, s->T, s->Y, s->part_xr, s->part_s, s->part_xr32,
-                   s->part_s32, s->part_b, s->hist};
+                   s->part_s32, s->part_b, s->hist, s->PH, s->SH};
     cudaFree(s->x0_nz);
     for (double *p : d) cudaFree(p);
     float *f[] = {s->D32, s->R32, s->R0_32, s->P32, s->V32, s->S32, s->T32};
@@ -1970,6 +2044,7 @@ hhp_status backward_dev(hhp_mat *A, const double *x_dev, const double *g_dev, do
     // lambda starts from zero
     HHP_CUDA(cudaMemsetAsync(dldb_dev, 0, sizeof(double) * static_cast<size_t>(A->n), st));
     hhp_solve_opts oa = *o;
+    oa.precond = HHP_PRECOND_NONE;  // the adjoint runs unpreconditioned
     if (oa.loop == HHP_LOOP_AUTO) oa.loop = HHP_LOOP_CLASSIC;
     // Adjoint tolerances sit near the FP64 rounding floor: the mixed form hands over to FP64
     // earlier there (0.1 rather than the solves' 0.05), which on the 1024x1024 stencil reached

@@ -1,4 +1,5 @@
-// hhp_reorder.cpp -- reverse Cuthill-McKee ordering of a square CSR pattern, host side.
+// hhp_reorder.cpp -- reverse Cuthill-McKee and multicolour orderings of a square CSR pattern, host
+// side (the multicolour order, for ILU(0), is at the end of the file).
 //
 // The reference reorders rows by a partition vector (csr_permute, src/util/hhp_dp_helpers.c:18-37,
 // grouped GPU-part first as src/entry/bicgstab_hybrid_dist_dp.c:221-233 does) that PaToH computed
@@ -106,28 +107,38 @@ int lowest_degree(const Graph &g, const std::vector<int> &nodes) {
 
 using namespace hhp;
 
-hhp_status hhp_reorder_rcm(int m, const int *rowptr, const int *col, int *perm) {
-    HHP_API_BEGIN
+namespace hhp {
+namespace {
+hhp_status check_square_csr(const char *who, int m, const int *rowptr, const int *col, const int *perm) {
     if (m < 0 || (m > 0 && (!rowptr || !perm)) || (m > 0 && rowptr[m] > 0 && !col)) {
-        set_error("reorder_rcm: null argument or negative size");
+        set_error("%s: null argument or negative size", who);
         return HHP_ERR_ARG;
     }
     if (m == 0) return HHP_OK;
     if (rowptr[0] != 0) {
-        set_error("reorder_rcm: rowptr[0] must be 0");
+        set_error("%s: rowptr[0] must be 0", who);
         return HHP_ERR_ARG;
     }
     for (int i = 0; i < m; ++i) {
         if (rowptr[i + 1] < rowptr[i]) {
-            set_error("reorder_rcm: rowptr decreases at row %d", i);
+            set_error("%s: rowptr decreases at row %d", who, i);
             return HHP_ERR_ARG;
         }
         for (int k = rowptr[i]; k < rowptr[i + 1]; ++k)
             if (col[k] < 0 || col[k] >= m) {
-                set_error("reorder_rcm: column %d of row %d outside [0, %d)", col[k], i, m);
+                set_error("%s: column %d of row %d outside [0, %d)", who, col[k], i, m);
                 return HHP_ERR_ARG;
             }
     }
+    return HHP_OK;
+}
+}  // namespace
+}  // namespace hhp
+
+hhp_status hhp_reorder_rcm(int m, const int *rowptr, const int *col, int *perm) {
+    HHP_API_BEGIN
+    HHP_TRY(check_square_csr("reorder_rcm", m, rowptr, col, perm));
+    if (m == 0) return HHP_OK;
     const Graph g = symmetrise(m, rowptr, col);
     std::vector<int> order;
     order.reserve(static_cast<size_t>(m));
@@ -171,6 +182,41 @@ hhp_status hhp_reorder_rcm(int m, const int *rowptr, const int *col, int *perm) 
         }
     }
     for (int i = 0; i < m; ++i) perm[i] = order[static_cast<size_t>(m - 1 - i)];
+    return HHP_OK;
+    HHP_API_END
+}
+
+// Greedy multicolouring (the first-fit colouring of graph-colouring practice, in natural node
+// order) of A + A^T: rows of one colour share no entry, so in the reordered matrix the rows of a
+// colour depend only on rows of earlier colours and the triangles of ILU(0) have at most as many
+// dependency levels as there are colours.
+hhp_status hhp_reorder_color(int m, const int *rowptr, const int *col, int *perm, int *n_colors) {
+    HHP_API_BEGIN
+    HHP_TRY(check_square_csr("reorder_color", m, rowptr, col, perm));
+    if (n_colors) *n_colors = 0;
+    if (m == 0) return HHP_OK;
+    const Graph g = symmetrise(m, rowptr, col);
+    std::vector<int> color(static_cast<size_t>(m), -1), taken;
+    int nc = 0;
+    for (int v = 0; v < m; ++v) {
+        // taken[c] == v: a neighbour coloured before v has colour c
+        for (long long k = g.ptr[static_cast<size_t>(v)]; k < g.ptr[static_cast<size_t>(v) + 1]; ++k) {
+            const int c = color[static_cast<size_t>(g.adj[static_cast<size_t>(k)])];
+            if (c >= 0) taken[static_cast<size_t>(c)] = v;
+        }
+        int c = 0;
+        while (c < nc && taken[static_cast<size_t>(c)] == v) ++c;
+        if (c == nc) {
+            ++nc;
+            taken.push_back(-1);
+        }
+        color[static_cast<size_t>(v)] = c;
+    }
+    std::vector<int> start(static_cast<size_t>(nc) + 1, 0);
+    for (int v = 0; v < m; ++v) ++start[static_cast<size_t>(color[static_cast<size_t>(v)]) + 1];
+    for (int c = 0; c < nc; ++c) start[static_cast<size_t>(c) + 1] += start[static_cast<size_t>(c)];
+    for (int v = 0; v < m; ++v) perm[start[static_cast<size_t>(color[static_cast<size_t>(v)])]++] = v;
+    if (n_colors) *n_colors = nc;
     return HHP_OK;
     HHP_API_END
 }

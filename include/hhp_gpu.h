@@ -55,8 +55,23 @@ typedef enum { HHP_PREC_FP64 = 0, HHP_PREC_MIXED = 1 } hhp_precision;
  * checked; while it is above rtol the scaled solve continues from x with a tolerance tightened by
  * the shortfall, so the reported residual and the status are those of A x = b (iters counts the
  * scaled solve's iterations, outer_iters its passes; the callback sees the scaled residual). Both
- * need a nonzero diagonal (HHP_ERR_ARG otherwise). */
-typedef enum { HHP_PRECOND_NONE = 0, HHP_PRECOND_JACOBI = 1, HHP_PRECOND_JACOBI_ROW = 2 } hhp_precond;
+ * need a nonzero diagonal (HHP_ERR_ARG otherwise). ILU0: right preconditioning with M = L U, the
+ * ILU(0) factorization of A in its stored order -- the SpSV path itself (steps 9 and 14 of
+ * gpu_BiCGStab: p^ = M^-1 p, v = A p^, x += alpha p^; s^ = M^-1 s, t = A s^, x += omega s^). The
+ * factors are built on the device on first use (and again after hhp_mat_set_values); each
+ * application is two triangular solves walking the dependency levels of L and U, so its cost
+ * grows with their number: reorder a stencil-like matrix with hhp_reorder_color first (two levels
+ * for the 5- and 7-point stencils) -- the natural order of an N x N grid has 2N - 1. FP64 only
+ * (HHP_ERR_ARG with the mixed form); the classic loop. Rows may store their entries in any
+ * column order (each is factored and solved in ascending column order); every diagonal must be
+ * stored and no column twice in a row (HHP_ERR_ARG), and the pivots u_ii must be nonzero
+ * (HHP_ERR_BREAKDOWN). */
+typedef enum {
+    HHP_PRECOND_NONE = 0,
+    HHP_PRECOND_JACOBI = 1,
+    HHP_PRECOND_JACOBI_ROW = 2,
+    HHP_PRECOND_ILU0 = 3
+} hhp_precond;
 
 /* FP64 iteration schedule. MERGED: the stop tests and beta come from the dot products of the
  * t = A s step (||r_new||^2 = s.s - omega t.s, r0.r_new = r0.s - omega r0.t), so one iteration is
@@ -214,6 +229,23 @@ hhp_status hhp_copy_dev(hhp_ctx *ctx, int n, const double *src_dev, double *dst_
  * orders rows by (src/entry/bicgstab_hybrid_dist_dp.c:217-233) when none is at hand. Deterministic;
  * HHP_ERR_ARG for a malformed CSR. */
 hhp_status hhp_reorder_rcm(int m, const int *rowptr, const int *col, int *perm);
+
+/* Multicolour order for ILU(0): a greedy colouring of the pattern of A + A^T (rows in ascending
+ * order take the smallest colour none of their coloured neighbours has), rows then grouped by
+ * colour, ascending inside a colour. perm[m] in csr_permute's convention; *n_colors (nullable)
+ * receives the number of colours, which bounds the dependency levels of the reordered matrix's
+ * triangles. Host only; HHP_ERR_ARG for a malformed or non-square CSR. */
+hhp_status hhp_reorder_color(int m, const int *rowptr, const int *col, int *perm, int *n_colors);
+
+/* ---- ILU(0) factors (the csrilu02 and SpSV steps of the same path) ------------------------------ */
+/* Builds the ILU(0) factors of A on the device if they do not exist yet (as a solve with
+ * HHP_PRECOND_ILU0 would). lu (nullable, host, nnz doubles) receives them in A's CSR order: L's
+ * multipliers below the diagonal (L has a unit diagonal), U on and above it. levels (nullable,
+ * 2 ints) receives the dependency levels of L and of U. */
+hhp_status hhp_ilu0_factor(hhp_ctx *ctx, hhp_mat *A, double *lu, int *levels);
+/* z = U^-1 L^-1 r for device vectors of length m (z may be r), factoring A first if needed.
+ * Ordered on the context's stream; returns after the work is queued. */
+hhp_status hhp_ilu0_apply_dev(hhp_ctx *ctx, hhp_mat *A, const double *r_dev, double *z_dev);
 
 /* ---- host-side helpers exposed for testing the work plan without a GPU ---------------------- */
 /* The SpMV work plan of a host CSR (rows_per_lane 2 = the FP64 kernel's slices of 64 rows, 4 =

@@ -431,3 +431,196 @@ void orc_csr_permute(int m, int nnz, const int *rowptr, const int *col, const do
         }
     }
 }
+
+/* ---------------------------------------------------------------------------------------------
+ * ILU(0): IKJ factorization (Saad, Algorithm 10.4), the two triangular solves, the
+ * preconditioned loop of src/entry/bicgstab_gpu.c:155-290 with steps 9 and 14 enabled, and the
+ * greedy multicolouring.
+ * ------------------------------------------------------------------------------------------- */
+static int diag_positions(int m, const int *rowptr, const int *col, int *dpos) {
+    for (int i = 0; i < m; ++i) {
+        dpos[i] = -1;
+        for (int p = rowptr[i]; p < rowptr[i + 1]; ++p) {
+            if (col[p] < 0 || col[p] >= m) return ORC_ERR_ARG;
+            if (p > rowptr[i] && col[p] <= col[p - 1]) return ORC_ERR_ARG;
+            if (col[p] == i) dpos[i] = p;
+        }
+        if (dpos[i] < 0) return ORC_ERR_ARG;
+    }
+    return ORC_OK;
+}
+
+int orc_ilu0(int m, const int *rowptr, const int *col, const double *val, double *lu, int *bad_row) {
+    if (m <= 0) return ORC_ERR_ARG;
+    int *dpos = (int *)malloc(sizeof(int) * (size_t)m);
+    if (!dpos) return ORC_ERR_IO;
+    int rc = diag_positions(m, rowptr, col, dpos);
+    if (rc != ORC_OK) {
+        free(dpos);
+        return rc;
+    }
+    memcpy(lu, val, sizeof(double) * (size_t)rowptr[m]);
+    if (bad_row) *bad_row = -1;
+    for (int i = 0; i < m && rc == ORC_OK; ++i) {
+        const int end = rowptr[i + 1];
+        for (int p = rowptr[i]; p < dpos[i]; ++p) {
+            const int k = col[p];
+            const double l = lu[p] / lu[dpos[k]];
+            lu[p] = l;
+            const int kb = dpos[k] + 1, ke = rowptr[k + 1];
+            for (int q = p + 1; q < end; ++q) {
+                int lo = kb, hi = ke;
+                const int j = col[q];
+                while (lo < hi) {
+                    int mid = lo + (hi - lo) / 2;
+                    if (col[mid] < j) lo = mid + 1;
+                    else hi = mid;
+                }
+                if (lo < ke && col[lo] == j) lu[q] = fma(-l, lu[lo], lu[q]);
+            }
+        }
+        const double u = lu[dpos[i]];
+        if (u == 0.0 || !isfinite(u)) {
+            if (bad_row) *bad_row = i;
+            rc = ORC_ERR_FORMAT;
+        }
+    }
+    free(dpos);
+    return rc;
+}
+
+/* the butterfly of the GPU's warp-wide rows: at each distance every slot adds its partner */
+static double butterfly32(double *a) {
+    double b[32];
+    for (int off = 16; off >= 1; off >>= 1) {
+        for (int l = 0; l < 32; ++l) b[l] = a[l] + a[l ^ off];
+        memcpy(a, b, sizeof(b));
+    }
+    return a[0];
+}
+
+static double tri_row(const int *col, const double *lu, int b, int e, const double *z, double rhs) {
+    if (e - b <= ORC_ILU_LONG) {
+        double acc = rhs;
+        for (int p = b; p < e; ++p) acc = fma(-lu[p], z[col[p]], acc);
+        return acc;
+    }
+    if (e - b <= ORC_ILU_BIG) {
+        double a[32] = {0};
+        for (int p = b; p < e; ++p) a[(p - b) & 31] = fma(lu[p], z[col[p]], a[(p - b) & 31]);
+        return rhs - butterfly32(a);
+    }
+    /* ORC_ILU_BLOCK partial sums, a butterfly over each group of 32, the group sums in order */
+    static double a[ORC_ILU_BLOCK];
+    memset(a, 0, sizeof(a));
+    for (int p = b; p < e; ++p) a[(p - b) % ORC_ILU_BLOCK] = fma(lu[p], z[col[p]], a[(p - b) % ORC_ILU_BLOCK]);
+    double tot = 0.0;
+    for (int w = 0; w < ORC_ILU_BLOCK / 32; ++w) tot += butterfly32(a + 32 * w);
+    return rhs - tot;
+}
+
+void orc_ilu0_apply(int m, const int *rowptr, const int *col, const double *lu, const double *r, double *z) {
+    int *dpos = (int *)malloc(sizeof(int) * (size_t)(m > 0 ? m : 1));
+    if (!dpos || diag_positions(m, rowptr, col, dpos) != ORC_OK) {
+        free(dpos);
+        for (int i = 0; i < m; ++i) z[i] = NAN;
+        return;
+    }
+    for (int i = 0; i < m; ++i) z[i] = tri_row(col, lu, rowptr[i], dpos[i], z, r[i]);
+    for (int i = m - 1; i >= 0; --i) {
+        const double dinv = 1.0 / lu[dpos[i]];
+        z[i] = tri_row(col, lu, dpos[i] + 1, rowptr[i + 1], z, z[i]) * dinv;
+    }
+    free(dpos);
+}
+
+int orc_bicgstab_ilu0_iters_to_tol(int m, const int *rowptr, const int *col, const double *val, const double *b,
+                                   double *x, double rtol, int maxit, double *relres) {
+    if (m <= 0 || maxit < 0) return -1;
+    const size_t nz = (size_t)rowptr[m];
+    double *lu = (double *)malloc(sizeof(double) * (nz ? nz : 1));
+    double *blk = (double *)calloc((size_t)9 * (size_t)m, sizeof(double));
+    if (!lu || !blk) {
+        free(lu);
+        free(blk);
+        return -2;
+    }
+    if (orc_ilu0(m, rowptr, col, val, lu, NULL) != ORC_OK) {
+        free(lu);
+        free(blk);
+        return -2;
+    }
+    double *R = blk, *R0 = blk + m, *P = blk + 2 * (size_t)m, *V = blk + 3 * (size_t)m, *S = blk + 4 * (size_t)m,
+           *T = blk + 5 * (size_t)m, *PH = blk + 6 * (size_t)m, *SH = blk + 7 * (size_t)m, *Y = blk + 8 * (size_t)m;
+    orc_spmv(m, rowptr, col, val, x, Y);
+    for (int i = 0; i < m; ++i) R[i] = R0[i] = b[i] - Y[i];
+    double delta = orc_dot(m, R0, R), delta_prev = delta, alpha = 1.0, omega = 1.0;
+    double rr = true_relres(m, rowptr, col, val, b, x, Y);
+    int found = rr <= rtol ? 0 : -1;
+    for (int it = 1; found < 0 && it <= maxit; ++it) {
+        if (it == 1) {
+            memcpy(P, R, sizeof(double) * (size_t)m);
+        } else {
+            delta = orc_dot(m, R0, R);
+            const double beta = (delta / delta_prev) * (alpha / omega);
+            delta_prev = delta;
+            for (int i = 0; i < m; ++i) P[i] = R[i] + beta * (P[i] - omega * V[i]);
+        }
+        orc_ilu0_apply(m, rowptr, col, lu, P, PH);
+        orc_spmv(m, rowptr, col, val, PH, V);
+        alpha = delta / orc_dot(m, R0, V);
+        for (int i = 0; i < m; ++i) {
+            x[i] += alpha * PH[i];
+            S[i] = R[i] - alpha * V[i];
+        }
+        orc_ilu0_apply(m, rowptr, col, lu, S, SH);
+        orc_spmv(m, rowptr, col, val, SH, T);
+        omega = orc_dot(m, T, S) / orc_dot(m, T, T);
+        for (int i = 0; i < m; ++i) {
+            x[i] += omega * SH[i];
+            R[i] = S[i] - omega * T[i];
+        }
+        rr = true_relres(m, rowptr, col, val, b, x, Y);
+        if (rr <= rtol) found = it;
+    }
+    if (relres) *relres = rr;
+    free(lu);
+    free(blk);
+    return found;
+}
+
+int orc_color(int m, const int *rowptr, const int *col, int *color) {
+    /* adjacency of A + A^T without the diagonal: the rows of A and the rows of A^T */
+    int *tptr = (int *)calloc((size_t)m + 1, sizeof(int));
+    int *tcol = (int *)malloc(sizeof(int) * (size_t)(rowptr[m] > 0 ? rowptr[m] : 1));
+    int *mark = (int *)malloc(sizeof(int) * (size_t)m + sizeof(int));
+    if (!tptr || !tcol || !mark) {
+        free(tptr);
+        free(tcol);
+        free(mark);
+        return -1;
+    }
+    for (int p = 0; p < rowptr[m]; ++p) tptr[col[p] + 1]++;
+    for (int j = 0; j < m; ++j) tptr[j + 1] += tptr[j];
+    int *fill = (int *)calloc((size_t)m + 1, sizeof(int));
+    for (int i = 0; i < m; ++i)
+        for (int p = rowptr[i]; p < rowptr[i + 1]; ++p) tcol[tptr[col[p]] + fill[col[p]]++] = i;
+    free(fill);
+    int ncol = 0;
+    for (int i = 0; i < m; ++i) mark[i] = -1;
+    for (int i = 0; i < m; ++i) {
+        /* mark[c] == i: colour c is taken by a neighbour of i */
+        for (int p = rowptr[i]; p < rowptr[i + 1]; ++p)
+            if (col[p] != i && col[p] < i) mark[color[col[p]]] = i;
+        for (int p = tptr[i]; p < tptr[i + 1]; ++p)
+            if (tcol[p] != i && tcol[p] < i) mark[color[tcol[p]]] = i;
+        int c = 0;
+        while (mark[c] == i) ++c;
+        color[i] = c;
+        if (c + 1 > ncol) ncol = c + 1;
+    }
+    free(tptr);
+    free(tcol);
+    free(mark);
+    return ncol;
+}

@@ -94,6 +94,55 @@ void orc_csr_to_csc(int m, int n, int nnz, const int *rowptr, const int *col, co
 void orc_csr_permute(int m, int nnz, const int *rowptr, const int *col, const double *val,
                      const int *perm, const int *perm_inv, int *orowptr, int *ocol, double *oval);
 
+/* ---- ILU(0) --------------------------------------------------------------------------------
+ * The preconditioner of the SpSV path of gpu_BiCGStab (src/entry/bicgstab_gpu.c:185-201 and
+ * 238-254, commented out there; cuSPARSE's csrilu02 and SpSV would supply the factorization and
+ * the triangular solves, neither of which is part of the reference's own sources). Restated from
+ * the published algorithm: ILU(0) in its IKJ form (Saad, Iterative Methods for Sparse Linear
+ * Systems, 2nd ed., Algorithm 10.4), M = L U with L unit lower and U upper on A's pattern.
+ * No reference output exists to pin these against; the tests pin them by the defining property
+ * of ILU(0), (L U)_ij = a_ij on the pattern, and by the closed form of the 5-point stencil. */
+
+/* Factors A in place of a copy: lu (nnz) receives L's multipliers below the diagonal and U on
+ * and above it, in A's CSR order. Row by row, for each k < i with a_ik stored, in ascending k:
+ * l_ik = a_ik / u_kk, then a_ij = fma(-l_ik, u_kj, a_ij) for every j > k stored in both rows i
+ * and k. Needs square A, every row's columns strictly ascending and every diagonal stored
+ * (ORC_ERR_ARG otherwise). A zero or non-finite pivot u_ii returns ORC_ERR_FORMAT with the first
+ * such row in *bad_row. */
+int orc_ilu0(int m, const int *rowptr, const int *col, const double *val, double *lu, int *bad_row);
+
+/* Rows of one triangle with more than ORC_ILU_LONG stored entries are summed as the GPU's
+ * warp-wide path sums them, rows with more than ORC_ILU_BIG as its block-wide path (blocks of
+ * ORC_ILU_BLOCK threads) does (below); shorter rows sequentially. */
+#define ORC_ILU_LONG 64
+#define ORC_ILU_BIG 2048
+#define ORC_ILU_BLOCK 1024
+
+/* z = U^-1 L^-1 r. Forward, rows ascending: z_i = r_i - sum_{k<i} l_ik z_k; backward, rows
+ * descending: z_i = (z_i - sum_{j>i} u_ij z_j) * d_i with d_i = 1 / u_ii rounded once (the GPU
+ * stores these reciprocals). A row whose triangle part has at most
+ * ORC_ILU_LONG entries is summed in ascending column order as acc = fma(-v, z, acc) starting from
+ * the right-hand value; a longer row accumulates 32 partial sums (entry e into slot e mod 32,
+ * acc = fma(v, z, acc) from 0), adds them by a butterfly (at distances 16, 8, 4, 2, 1 every slot
+ * adds its partner) and subtracts slot 0 from the right-hand value; a row above ORC_ILU_BIG
+ * accumulates ORC_ILU_BLOCK partial sums the same way, reduces each group of 32 by the butterfly
+ * and adds the group sums in group order from 0. These are the GPU's orders, so results agree bit
+ * for bit. */
+void orc_ilu0_apply(int m, const int *rowptr, const int *col, const double *lu, const double *r, double *z);
+
+/* Right-preconditioned BiCGStab with M = ILU(0) of A, the loop of bicgstab_gpu.c:155-290 with
+ * its preconditioning steps 9 and 14 in place: p^ = M^-1 p, v = A p^, x += alpha p^,
+ * s^ = M^-1 s, t = A s^, x += omega s^. Returns the first iteration whose true relative residual
+ * ||b - A x|| / ||b|| is <= rtol (-1 if maxit iterations do not reach it, -2 on an ILU error);
+ * x is updated in place and *relres receives its residual. */
+int orc_bicgstab_ilu0_iters_to_tol(int m, const int *rowptr, const int *col, const double *val,
+                                   const double *b, double *x, double rtol, int maxit, double *relres);
+
+/* Greedy multicolouring of the pattern of A + A^T: rows in ascending order take the smallest
+ * colour none of their coloured neighbours has. color[m] receives the colours; returns their
+ * number. */
+int orc_color(int m, const int *rowptr, const int *col, int *color);
+
 #ifdef __cplusplus
 }
 #endif

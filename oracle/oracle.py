@@ -47,6 +47,10 @@ def lib():
             "orc_bicgstab_fixed_mt": (_I, [_I, _P, _P, _P, _P, _P, _I, _I, ctypes.POINTER(_D)]),
             "orc_csr_to_csc": (None, [_I, _I, _I, _P, _P, _P, _P, _P, _P]),
             "orc_csr_permute": (None, [_I, _I, _P, _P, _P, _P, _P, _P, _P, _P]),
+            "orc_ilu0": (_I, [_I, _P, _P, _P, _P, ctypes.POINTER(_I)]),
+            "orc_ilu0_apply": (None, [_I, _P, _P, _P, _P, _P]),
+            "orc_bicgstab_ilu0_iters_to_tol": (_I, [_I, _P, _P, _P, _P, _P, _D, _I, ctypes.POINTER(_D)]),
+            "orc_color": (_I, [_I, _P, _P, _P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(h, name)
@@ -210,3 +214,43 @@ def ref():
             f.restype, f.argtypes = res, args
         _ref = h
     return _ref
+
+
+def ilu0(rowptr, col, val):
+    """ILU(0) factors in A's CSR order (L's multipliers below the diagonal, U on and above) ->
+    (status, lu, first bad pivot row or -1)."""
+    rowptr, col, val = _csr(rowptr, col, val)
+    lu = np.empty(max(col.size, 1), np.float64)
+    bad = _I(-1)
+    st = lib().orc_ilu0(rowptr.size - 1, _ptr(rowptr), _ptr(col), _ptr(val), _ptr(lu), ctypes.byref(bad))
+    return st, lu[:col.size], bad.value
+
+
+def ilu0_apply(rowptr, col, lu, r):
+    """z = U^-1 L^-1 r in the GPU's summation orders."""
+    rowptr, col, lu = _csr(rowptr, col, lu)
+    r = np.ascontiguousarray(r, np.float64)
+    z = np.empty_like(r)
+    lib().orc_ilu0_apply(rowptr.size - 1, _ptr(rowptr), _ptr(col), _ptr(lu), _ptr(r), _ptr(z))
+    return z
+
+
+def ilu0_iters_to_tol(rowptr, col, val, b, x0, rtol: float, maxit: int):
+    """ILU(0)-preconditioned BiCGStab (src/entry/bicgstab_gpu.c:155-290, steps 9 and 14 enabled):
+    (first iteration with true rel-res <= rtol or -1, x, relres)."""
+    rowptr, col, val = _csr(rowptr, col, val)
+    b = np.ascontiguousarray(b, np.float64)
+    x = np.array(x0, np.float64, copy=True)
+    rr = _D()
+    k = lib().orc_bicgstab_ilu0_iters_to_tol(rowptr.size - 1, _ptr(rowptr), _ptr(col), _ptr(val), _ptr(b), _ptr(x),
+                                             rtol, maxit, ctypes.byref(rr))
+    return k, x, rr.value
+
+
+def color(rowptr, col):
+    """Greedy colouring of A + A^T -> (colours, count)."""
+    rowptr = np.ascontiguousarray(rowptr, np.int32)
+    col = np.ascontiguousarray(col, np.int32)
+    c = np.empty(rowptr.size - 1, np.int32)
+    n = lib().orc_color(rowptr.size - 1, _ptr(rowptr), _ptr(col), _ptr(c))
+    return c, n

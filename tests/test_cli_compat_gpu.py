@@ -110,16 +110,19 @@ def test_cli_rcm_reorder():
         assert r.returncode != 0 and "exclusive" in r.stdout
 
 
-@pytest.mark.parametrize("precond", ["jacobi", "jacobi_row"])
-def test_cli_preconditioners(precond):
+@pytest.mark.parametrize("precond,reorder", [("jacobi", "none"), ("jacobi_row", "none"), ("ilu0", "none"),
+                                             ("ilu0", "color")])
+def test_cli_preconditioners(precond, reorder):
     g = load_golden("sample320")
     with tempfile.TemporaryDirectory() as td:
         p = _files(td, g)
         out = os.path.join(td, "X.txt")
-        kv, _ = _run(["-m", p["A"], "-x", p["x0"], "-y", p["b"], "-o", out, "--precond", precond, "-n", "500",
-                      "--rtol", "1e-11", "--out-format", "exact"])
+        kv, _ = _run(["-m", p["A"], "-x", p["x0"], "-y", p["b"], "-o", out, "--precond", precond, "--reorder", reorder,
+                      "-n", "500", "--rtol", "1e-11", "--out-format", "exact"])
         assert float(kv["relative_residual"]) <= 1e-11
         assert np.max(np.abs(np.loadtxt(out) - np.arange(1, 321))) < 1e-6
+        if reorder == "color":
+            assert int(kv["colors"]) >= 2
 
 
 def test_spmv_cli_known_answer():
