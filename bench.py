@@ -917,10 +917,11 @@ def run_spmv_only(args):
 def run_config_solve(args):
     """One configuration's solve, timed alone (profiler target and per-config check): --steps solves
     of --config in FP64 (--precision fp64) or the mixed form (--precision fp32), rtol 1e-10 (C5:
-    1e-12; C3: --iters fixed iterations, as it does not converge unpreconditioned). Prints one JSON
-    line with the median CUDA-event time, L2 flushed before each solve."""
+    1e-12; C3: --iters fixed iterations, as it does not converge unpreconditioned). --precond ilu0:
+    the ILU(0)-preconditioned solve of the multicolour-ordered system, --iters fixed iterations.
+    Prints one JSON line with the median CUDA-event time, L2 flushed before each solve."""
     import torch
-    from hethyppar_gb300 import Context, Matrix, bicgstab, synth
+    from hethyppar_gb300 import Context, Matrix, bicgstab, reorder_color, synth
     ctx = Context(0)
     stream = torch.cuda.ExternalStream(ctx.stream)
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
@@ -931,13 +932,16 @@ def run_config_solve(args):
             flush.add_(1.0)
             flush_r.sum()
     s = synth.config(args.config)
-    A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
-    b = torch.as_tensor(s.b, device="cuda")
+    perm = reorder_color(s.rowptr, s.col)[0] if args.precond == "ilu0" else None
+    A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val, perm=perm)
+    b = torch.as_tensor(s.b if perm is None else s.b[perm], device="cuda")
     x = torch.zeros(s.n, dtype=torch.float64, device="cuda")
     kw = {"rtol": 1e-12 if args.config == "c5" else RTOL, "maxit": 50000,
           "precision": "mixed" if args.precision == "fp32" else "fp64"}
-    if args.config == "c3":
+    if args.config == "c3" or args.precond == "ilu0":
         kw = {"rtol": 0.0, "maxit": args.iters, "fixed_iters": True}
+    if args.precond == "ilu0":
+        kw["precond"] = "ilu0"
     res = []
 
     def run():
@@ -948,6 +952,7 @@ def run_config_solve(args):
     ms = _event_ms(stream, run, flush_l2, args.steps)
     r = res[-1]
     print(json.dumps({"mode": "solve-config", "config": args.config, "precision": kw.get("precision", "fp64"),
+                      "precond": args.precond,
                       "ms": ms, "iters": r.iters, "us_per_iter": ms * 1e3 / max(r.iters, 1),
                       "rel_res_true": r.rel_res_true, "status": r.status}), flush=True)
 
@@ -967,6 +972,8 @@ def main():
     ap.add_argument("--iters", type=int, default=200, help="solve-config on c3: fixed iterations")
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--precond", default="none", choices=["none", "ilu0"],
+                    help="solve-config: ilu0 = ILU(0) on the multicolour-ordered system")
     args = ap.parse_args()
     if args.mode == "spmv":
         run_spmv_only(args)

@@ -10,10 +10,12 @@
 
 namespace hhp {
 
-// Device error codes for the context's error word. No kernel of this library waits on another
-// (the long-row combine is a last-arriver atomic count, every other ordering is a kernel
-// boundary), so nothing sets it today; SpMV launches and the solve loop check it, so a future
-// bounded wait that gives up stops every later launch and the solve returns HHP_ERR_TIMEOUT.
+// Device error codes for the context's error word. The only waits in this library are the grid
+// barriers between dependency levels inside the ILU(0) kernels (cooperative launches, so every
+// block is resident); each is bounded, and one that runs out sets DEV_ERR_TIMEOUT. SpMV launches,
+// the ILU kernels and the solve loop check the word, so every later launch stops and the solve
+// returns HHP_ERR_TIMEOUT. (The SpMV's long-row combine is a last-arriver atomic count, not a
+// wait; every other ordering is a kernel boundary.)
 enum : int {
     DEV_OK = 0,
     DEV_ERR_TIMEOUT = 1,
