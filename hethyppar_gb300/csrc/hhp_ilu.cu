@@ -293,30 +293,45 @@ __global__ void __launch_bounds__(kIluThreads, 1) k_ilu_tri(TriArgs t, const int
                 __stcg(out + row, r);
             }
         }
-        for (int s = t.lev_slice[lev] + gw; s < t.lev_slice[lev + 1]; s += W) {
-            const int row = t.slice_row[32 * s + lane];
-            if (row >= 0) {
-                const int len = t.slice_len[32 * s + lane];
-                const long long base = t.slice_ptr[s] + lane;
-                double acc = in[row];
-                int k = 0;
-                for (; k + 4 <= len; k += 4) {
-                    const long long q = base + 32LL * k;
-                    const int c0 = t.scol[q], c1 = t.scol[q + 32], c2 = t.scol[q + 64], c3 = t.scol[q + 96];
-                    const double v0 = t.sval[q], v1 = t.sval[q + 32], v2 = t.sval[q + 64], v3 = t.sval[q + 96];
-                    const double z0 = z(c0), z1 = z(c1), z2 = z(c2), z3 = z(c3);
-                    acc = fma(-v0, z0, acc);
-                    acc = fma(-v1, z1, acc);
-                    acc = fma(-v2, z2, acc);
-                    acc = fma(-v3, z3, acc);
+        // Two slices per pass (s and s + W), four steps at a time: every load of a group is issued
+        // before its FMAs, so a warp has two slices' chains of dependent requests (row data, then
+        // slots, then gathers) in flight at once. A step past a lane's row length loads nothing
+        // and adds fma(-0, 0, acc), which leaves acc unchanged bit for bit.
+        const int s_hi = t.lev_slice[lev + 1];
+        for (int s = t.lev_slice[lev] + gw; s < s_hi; s += 2 * W) {
+            const int sb = s + W;
+            const bool two = sb < s_hi;
+            const int r0 = t.slice_row[32 * s + lane];
+            const int n0 = t.slice_len[32 * s + lane];
+            const long long q0 = t.slice_ptr[s] + lane;
+            const int r1 = two ? t.slice_row[32 * sb + lane] : -1;
+            const int n1 = two ? t.slice_len[32 * sb + lane] : 0;
+            const long long q1 = two ? t.slice_ptr[sb] + lane : 0;
+            double a0 = r0 >= 0 ? in[r0] : 0.0, a1 = r1 >= 0 ? in[r1] : 0.0;
+            const int len = max(n0, n1);
+            for (int k = 0; k < len; k += 4) {
+                int c[8];
+                double v[8], zz[8];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const bool p0 = k + j < n0, p1 = k + j < n1;
+                    c[j] = p0 ? t.scol[q0 + 32LL * (k + j)] : 0;
+                    v[j] = p0 ? t.sval[q0 + 32LL * (k + j)] : 0.0;
+                    c[4 + j] = p1 ? t.scol[q1 + 32LL * (k + j)] : 0;
+                    v[4 + j] = p1 ? t.sval[q1 + 32LL * (k + j)] : 0.0;
                 }
-                for (; k < len; ++k) {
-                    const long long q = base + 32LL * k;
-                    acc = fma(-t.sval[q], z(t.scol[q]), acc);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    zz[j] = k + j < n0 ? z(c[j]) : 0.0;
+                    zz[4 + j] = k + j < n1 ? z(c[4 + j]) : 0.0;
                 }
-                if (UPPER) acc = acc * dinv[row];
-                __stcg(out + row, acc);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) a0 = fma(-v[j], zz[j], a0);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) a1 = fma(-v[4 + j], zz[4 + j], a1);
             }
+            if (r0 >= 0) __stcg(out + r0, UPPER ? a0 * dinv[r0] : a0);
+            if (r1 >= 0) __stcg(out + r1, UPPER ? a1 * dinv[r1] : a1);
         }
         if (lev >= 1 && lev + 1 < t.n_levels && !grid_barrier(bar, ++barriers, dev_err)) return;
     }
@@ -424,7 +439,10 @@ hhp_status upload_tri(const TriHost &h, IluTri &d, int **sidx_dev) {
     return HHP_OK;
 }
 
-cudaError_t launch_coop(const void *func, int grid, void **args, cudaStream_t st) {
+// A launch whose blocks wait on one another (coop) is cooperative: the runtime guarantees that
+// all of them are resident together. A triangle of at most two levels has no barrier (levels 0
+// and 1 share a pass), so its launch is an ordinary one.
+cudaError_t launch_coop(const void *func, int grid, void **args, cudaStream_t st, bool coop = true) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(static_cast<unsigned>(grid));
     cfg.blockDim = dim3(kIluThreads);
@@ -432,8 +450,8 @@ cudaError_t launch_coop(const void *func, int grid, void **args, cudaStream_t st
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
     attr[0].val.cooperative = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cfg.attrs = coop ? attr : nullptr;
+    cfg.numAttrs = coop ? 1 : 0;
     return cudaLaunchKernelExC(&cfg, func, args);
 }
 
@@ -688,7 +706,7 @@ hhp_status launch_ilu_apply(hhp_mat *A, cudaStream_t st, const double *in, doubl
         const double *x = in;
         double *y = I->y;
         void *args[] = {&t, &rp, &col, &dpos, &lu, &dinv, &x, &y, &b, &bo, &stop, &err};
-        HHP_CUDA(launch_coop(reinterpret_cast<const void *>(k_ilu_tri<false>), I->grid, args, st));
+        HHP_CUDA(launch_coop(reinterpret_cast<const void *>(k_ilu_tri<false>), I->grid, args, st, I->L.n_levels > 2));
     }
     {  // out = U^-1 y
         TriArgs t = args_of(I->U);
@@ -696,7 +714,7 @@ hhp_status launch_ilu_apply(hhp_mat *A, cudaStream_t st, const double *in, doubl
         const double *x = I->y;
         double *y = out;
         void *args[] = {&t, &rp, &col, &dpos, &lu, &dinv, &x, &y, &b, &bo, &stop, &err};
-        HHP_CUDA(launch_coop(reinterpret_cast<const void *>(k_ilu_tri<true>), I->grid, args, st));
+        HHP_CUDA(launch_coop(reinterpret_cast<const void *>(k_ilu_tri<true>), I->grid, args, st, I->U.n_levels > 2));
     }
     A->ctx->kernel_launches += 2;
     return HHP_OK;
