@@ -673,7 +673,13 @@ hhp_status ensure_ilu(hhp_mat *A, int *levels) {
         return HHP_ERR_ARG;
     }
     IluDev *I = new IluDev();
-    const hhp_status rc = build_ilu(A, I, levels);
+    hhp_status rc;
+    try {
+        rc = build_ilu(A, I, levels);
+    } catch (...) {  // host allocation failure: release the device arrays, then report
+        free_ilu(I);
+        throw;
+    }
     if (rc != HHP_OK) {
         free_ilu(I);
         return rc;

@@ -93,7 +93,12 @@ def test_factors_and_application_are_bit_exact(ctx, name, colored):
     z = torch.empty(rp.size - 1, dtype=torch.float64, device="cuda")
     A.ilu0_apply_dev(dev(r), z)
     ctx.sync()
-    assert np.array_equal(z.cpu().numpy(), orc.ilu0_apply(rp, col, lu_ref, r))
+    z_ref = orc.ilu0_apply(rp, col, lu_ref, r)
+    assert np.array_equal(z.cpu().numpy(), z_ref)
+    rz = dev(r)
+    A.ilu0_apply_dev(rz, rz)  # in place
+    ctx.sync()
+    assert np.array_equal(rz.cpu().numpy(), z_ref)
     A.close()
 
 
