@@ -29,6 +29,8 @@ enum : int {
     ST_BREAKDOWN = 4,      // rho, (r0,v) or (t,t) is zero or not finite
     ST_MAXIT = 5,          // iteration cap reached
     ST_DEVICE_ERROR = 6,   // a kernel recorded a device error (e.g. a wait timeout)
+    ST_UPDATE_PENDING = 7, // mixed form, not terminal: an FP64 update is decided and the loop's
+                           // kernels skip until the update's K_P has run and reset the status
 };
 
 __device__ __forceinline__ double warp_sum(double v) {

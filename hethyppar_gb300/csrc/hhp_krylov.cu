@@ -280,7 +280,10 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
                                            int use_cond, const int *gate = nullptr) {
     // gate (direct launches of the mixed form): run only when the iteration made an FP64 update
     if (gate && *reinterpret_cast<volatile const int *>(gate) == 0) return;
-    const bool dead = dead_step(sc);  // tested after the operand and record loads are in flight
+    // tested after the operand and record loads are in flight; a pending FP64 update of the mixed
+    // form is live here: this launch is the update's K_P, which completes it
+    const int st_in = *reinterpret_cast<volatile const int *>(&sc->status);
+    const bool dead = st_in != ST_RUNNING && st_in != ST_UPDATE_PENDING;
     // scalars written by earlier launches, read with the operand loads (off the critical path)
     const int iter = sc->iter, it0 = sc->iter_start, maxit = sc->maxit,
               dev_error = *reinterpret_cast<volatile const int *>(dev_err);
@@ -336,6 +339,9 @@ __global__ void __launch_bounds__(512) k_p(DevScal *sc, T *P, const T *V, const 
                     sc->rho_cur = rho_new;
                     sc->beta = beta;
                     sc->rr_last = rr;
+                    // every block of this launch treats a pending update as live, so the reset
+                    // cannot split them
+                    if (st_in == ST_UPDATE_PENDING) sc->status = ST_RUNNING;
                 }
             }
         }
@@ -976,7 +982,9 @@ __global__ void __launch_bounds__(512) k_xrp_ru(DevScal *sc, double *X, float *D
                                                 const double *part_s, int nparts, double *hist, int hist_cap,
                                                 cudaGraphConditionalHandle wcond, cudaGraphConditionalHandle icond,
                                                 int first_in_body, const int *dev_err, int use_cond) {
-    const bool dead = dead_step(sc);  // tested after the operand and record loads are in flight
+    // tested after the operand and record loads are in flight
+    const int st_in = *reinterpret_cast<volatile const int *>(&sc->status);
+    const bool dead = st_in != ST_RUNNING;
     // scalars written by earlier launches, read with the operand loads (off the critical path)
     const int it = sc->iter, it0 = sc->iter_start, maxit = sc->maxit,
               dev_error = *reinterpret_cast<volatile const int *>(dev_err);
@@ -1003,10 +1011,14 @@ __global__ void __launch_bounds__(512) k_xrp_ru(DevScal *sc, double *X, float *D
     if (dead) {
         if (b0t0()) {
             if (first_in_body) sc->bodies += 1;
-            sc->ru_flag = 0;
-            if (use_cond) {
-                cudaGraphSetConditional(icond, 0u);
-                cudaGraphSetConditional(wcond, 0);
+            // a slot after this body's pending FP64 update keeps the update's flag and the loop
+            // running: the IF node at the end of the body carries out the update
+            if (st_in != ST_UPDATE_PENDING) {
+                sc->ru_flag = 0;
+                if (use_cond) {
+                    cudaGraphSetConditional(icond, 0u);
+                    cudaGraphSetConditional(wcond, 0);
+                }
             }
         }
         return;
@@ -1057,6 +1069,8 @@ __global__ void __launch_bounds__(512) k_xrp_ru(DevScal *sc, double *X, float *D
         if (atomicAdd(&sc->arrivals, 1) == static_cast<int>(gridDim.x) - 1) {
             sc->arrivals = 0;
             if (term != ST_RUNNING && what == 0) sc->status = term;
+            // an update: the rest of the body's slots skip until its K_P has run
+            if (what == 2) sc->status = ST_UPDATE_PENDING;
         }
         if (lead) {
             sc->ru_flag = what == 2 ? 1 : 0;  // this iteration's update decision
@@ -1387,6 +1401,7 @@ hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R,
         return HHP_OK;
     };
     cudaGraphConditionalHandle cond;
+    cudaGraphConditionalHandle icond_body = cudaGraphConditionalHandle();  // mixed merged: the body's IF
     HHP_TRY(make_cond(stream, &cond));
     HHP_TRY(kp(stream, cond, 0));  // stop tests on the initial residual, before the node
     HHP_TRY(begin_loop_body(s, stream, cond));
@@ -1409,8 +1424,16 @@ hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R,
                 continue;
             }
         } else if (merged) {
-            // mixed form, merged: [SpMV + r0.v, K_S + r0.s, SpMV + t.s/t.t/r0.t, K_XRP_RU],
-            // IF(update) { FP64 residual, residual replacement, K_P }
+            // mixed form, merged: `unroll` slots [SpMV + r0.v, K_S + r0.s, SpMV + t.s/t.t/r0.t,
+            // K_XRP_RU], then one IF(update) { FP64 residual, residual replacement, K_P } for the
+            // body. A slot that decides an update sets the status to ST_UPDATE_PENDING, so the
+            // body's later slots skip and the IF carries the update out: the same sequence of
+            // states as an IF after every slot, with one conditional node per body instead of one
+            // per iteration (a never-taken IF node costs ~3 us)
+            if (k == 0) {
+                st = make_cond_if(s->s2, &icond_body);
+                if (st != HHP_OK) break;
+            }
             st = launch_spmv32(A, s->s2, EP_DOT1, P, V, R0, stop);
             if (st != HHP_OK) break;
             if (launch_k(k_s<float, true>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, sc, S, R, V, R0, nu,
@@ -1420,16 +1443,14 @@ hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R,
             }
             st = launch_spmv32(A, s->s2, EP_DOT3, S, Tv, S, stop, R0);
             if (st != HHP_OK) break;
-            cudaGraphConditionalHandle icond;
-            st = make_cond_if(s->s2, &icond);
-            if (st != HHP_OK) break;
             if (launch_k(k_xrp_ru, dim3(s->nblk), dim3(s->nthr), 0, s->s2, s->sc32, s->X, s->D32, s->R32, s->P32,
                          s->S32, s->T32, s->V32, nu4, parts_of(pl), part_s, s->nblk, s->hist, s->hist_cap, cond,
-                         icond, k == 0 ? 1 : 0, A->ctx->dev_err, 1) != cudaSuccess) {
+                         icond_body, k == 0 ? 1 : 0, A->ctx->dev_err, 1) != cudaSuccess) {
                 st = HHP_ERR_CUDA;
                 break;
             }
-            st = begin_if_body(s, icond);
+            if (k + 1 < s->unroll) continue;
+            st = begin_if_body(s, icond_body);
             if (st != HHP_OK) break;
             st = launch_spmv64(A, s->s3, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0);
             if (st == HHP_OK &&
