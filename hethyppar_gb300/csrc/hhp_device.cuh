@@ -33,6 +33,20 @@ enum : int {
                            // kernels skip until the update's K_P has run and reset the status
 };
 
+// float -> double, exactly, on the integer pipe for normal numbers: the IEEE 754 binary32 fields
+// re-biased into binary64 (exponent + 1023 - 127, fraction shifted up by 29 bits). Zero,
+// subnormal, infinite and NaN inputs take the hardware conversion. Same value as
+// static_cast<double>(f) in every case; it keeps conversions off GB300's narrow FP64 pipe.
+__device__ __forceinline__ double widen(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned ex = (u >> 23) & 0xffu;
+    if (ex - 1u >= 254u) return static_cast<double>(f);
+    const unsigned hi = (u & 0x80000000u) | ((ex + (1023u - 127u)) << 20) | ((u & 0x7fffffu) >> 3);
+    const unsigned lo = u << 29;
+    return __hiloint2double(static_cast<int>(hi), static_cast<int>(lo));
+}
+__device__ __forceinline__ double widen(double f) { return f; }
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

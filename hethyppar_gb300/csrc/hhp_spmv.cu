@@ -288,10 +288,10 @@ __device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, long long
         if (r >= 0 && r < a.m) row_epilogue<VT, EP>(a, r, acc[t], e0, e1, e2, w1v[t], w2v[t]);
     }
     if (EP != EP_AXPBY && EP != EP_Y) {
-        d0 += static_cast<double>(e0);
-        d1 += static_cast<double>(e1);
+        d0 += widen(e0);
+        d1 += widen(e1);
     }
-    if (EP == EP_DOT3) d2 += static_cast<double>(e2);
+    if (EP == EP_DOT3) d2 += widen(e2);
 }
 
 // Long rows' epilogue records are folded by groups of kLongGroup consecutive long rows: the warp
