@@ -964,7 +964,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-extras", dest="extras", action="store_false")
-    ap.add_argument("--extra-reps", type=int, default=3)
+    ap.add_argument("--extra-reps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", default="solve", choices=["solve", "spmv", "solve-config"],
                     help="spmv: time the SpMV kernel alone on --config (kernel sweeps, profiler target); "
