@@ -204,9 +204,9 @@ __global__ void __launch_bounds__(kIluThreads) k_ilu_factor(const int *__restric
 
 // The value of dependency c: out[c], written by this kernel at an earlier level (read from L2:
 // another SM wrote it), except on level 1, whose dependencies are all level-0 rows -- rows with
-// no entries in this triangle, out[c] = in[c] (forward) or in[c] / u_cc (backward) -- read
-// straight from `in`, so levels 0 and 1 share one pass with no grid barrier between them. Both
-// ways give the same bits.
+// no entries in this triangle, out[c] = in[c] (forward) or in[c] * (1 / u_cc) (backward) --
+// formed straight from `in`, so levels 0 and 1 share one pass with no grid barrier between them.
+// Both ways give the same bits.
 template <bool UPPER>
 struct Dep {
     const double *in, *dinv, *out;
@@ -411,30 +411,34 @@ void layout_triangle(int m, const std::vector<int> &lev, int nlev, const int *co
     }
 }
 
+// Host array -> new device array, ordered on the context's (non-blocking) stream like every other
+// upload of the library: a legacy-stream copy from pageable memory may still be in flight when the
+// call returns, unordered against that stream's kernels. (A pageable source is staged before the
+// call returns, so the host vector may go right after.)
 template <typename V>
-hhp_status upload(V **dst, const std::vector<V> &src) {
+hhp_status upload(V **dst, const std::vector<V> &src, cudaStream_t st) {
     if (src.empty()) return HHP_OK;
     HHP_CUDA(cudaMalloc(dst, sizeof(V) * src.size()));
-    HHP_CUDA(cudaMemcpy(*dst, src.data(), sizeof(V) * src.size(), cudaMemcpyHostToDevice));
+    HHP_CUDA(cudaMemcpyAsync(*dst, src.data(), sizeof(V) * src.size(), cudaMemcpyHostToDevice, st));
     return HHP_OK;
 }
 
-hhp_status upload_tri(const TriHost &h, IluTri &d, int **sidx_dev) {
+hhp_status upload_tri(const TriHost &h, IluTri &d, int **sidx_dev, cudaStream_t st) {
     d.n_levels = h.n_levels;
     d.n_slices = static_cast<int>(h.slice_ptr.size()) - 1;
     d.n_long = static_cast<int>(h.long_row.size());
     d.n_big = static_cast<int>(h.big_row.size());
     d.slots = h.slice_ptr.back();
-    HHP_TRY(upload(&d.lev_slice, h.lev_slice));
-    HHP_TRY(upload(&d.lev_long, h.lev_long));
-    HHP_TRY(upload(&d.slice_ptr, h.slice_ptr));
-    HHP_TRY(upload(&d.slice_row, h.slice_row));
-    HHP_TRY(upload(&d.slice_len, h.slice_len));
-    HHP_TRY(upload(&d.scol, h.scol));
-    HHP_TRY(upload(&d.long_row, h.long_row));
-    HHP_TRY(upload(&d.lev_big, h.lev_big));
-    HHP_TRY(upload(&d.big_row, h.big_row));
-    HHP_TRY(upload(sidx_dev, h.sidx));
+    HHP_TRY(upload(&d.lev_slice, h.lev_slice, st));
+    HHP_TRY(upload(&d.lev_long, h.lev_long, st));
+    HHP_TRY(upload(&d.slice_ptr, h.slice_ptr, st));
+    HHP_TRY(upload(&d.slice_row, h.slice_row, st));
+    HHP_TRY(upload(&d.slice_len, h.slice_len, st));
+    HHP_TRY(upload(&d.scol, h.scol, st));
+    HHP_TRY(upload(&d.long_row, h.long_row, st));
+    HHP_TRY(upload(&d.lev_big, h.lev_big, st));
+    HHP_TRY(upload(&d.big_row, h.big_row, st));
+    HHP_TRY(upload(sidx_dev, h.sidx, st));
     if (d.slots > 0) HHP_CUDA(cudaMalloc(&d.sval, sizeof(double) * static_cast<size_t>(d.slots)));
     return HHP_OK;
 }
@@ -539,12 +543,12 @@ hhp_status build_ilu(hhp_mat *A, IluDev *I, int *levels_out) {
     int *sidxL = nullptr, *sidxU = nullptr;
     hhp_status rc = HHP_OK;
     do {
-        if (!sorted && (rc = upload(&I->col, col)) != HHP_OK) break;
-        if ((rc = upload(&I->dpos, dpos)) != HHP_OK) break;
-        if ((rc = upload(&I->frow, frow)) != HHP_OK) break;
-        if ((rc = upload(&I->flev, flev)) != HHP_OK) break;
-        if ((rc = upload_tri(TL, I->L, &sidxL)) != HHP_OK) break;
-        if ((rc = upload_tri(TU, I->U, &sidxU)) != HHP_OK) break;
+        if (!sorted && (rc = upload(&I->col, col, st)) != HHP_OK) break;
+        if ((rc = upload(&I->dpos, dpos, st)) != HHP_OK) break;
+        if ((rc = upload(&I->frow, frow, st)) != HHP_OK) break;
+        if ((rc = upload(&I->flev, flev, st)) != HHP_OK) break;
+        if ((rc = upload_tri(TL, I->L, &sidxL, st)) != HHP_OK) break;
+        if ((rc = upload_tri(TU, I->U, &sidxU, st)) != HHP_OK) break;
         if (cudaMalloc(&I->lu, sizeof(double) * (static_cast<size_t>(A->nnz) + 1)) != cudaSuccess ||
             cudaMalloc(&I->dinv, sizeof(double) * static_cast<size_t>(m)) != cudaSuccess ||
             cudaMalloc(&I->y, sizeof(double) * static_cast<size_t>(m)) != cudaSuccess ||
@@ -587,7 +591,7 @@ hhp_status build_ilu(hhp_mat *A, IluDev *I, int *levels_out) {
             }
         } else {
             int *src_dev = nullptr;
-            if ((rc = upload(&src_dev, I->src)) != HHP_OK) break;
+            if ((rc = upload(&src_dev, I->src, st)) != HHP_OK) break;
             k_ilu_gather<<<4 * A->ctx->num_sms, 256, 0, st>>>(A->val, src_dev, A->nnz, I->lu);
             const cudaError_t ge = cudaGetLastError();
             const cudaError_t se = cudaStreamSynchronize(st);
