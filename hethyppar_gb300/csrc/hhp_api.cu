@@ -56,6 +56,7 @@ const Tuning &tuning() {
         d.rpl64 = env_int("HHP_SPMV_RPL64", d.rpl64);
         d.rpl32 = env_int("HHP_SPMV_RPL32", d.rpl32);
         d.d16 = env_int("HHP_SPMV_D16", d.d16);
+        d.uni = env_int("HHP_SPMV_UNI", d.uni);
         // out-of-range overrides fall back to the defaults' valid ranges (a zero window or chunk
         // cap would never advance the plan builder's loops)
         const Tuning def;
@@ -71,6 +72,7 @@ const Tuning &tuning() {
         if (d.rpl64 != 0 && d.rpl64 != 1 && d.rpl64 != 2) d.rpl64 = def.rpl64;
         if (d.rpl32 != 2 && d.rpl32 != 4) d.rpl32 = def.rpl32;
         d.d16 = d.d16 != 0 ? 1 : 0;
+        d.uni = d.uni != 0 ? 1 : 0;
         return d;
     }();
     return t;

@@ -77,12 +77,23 @@ void build_plan(int m, const int *rowptr, int rpl, int long_thr, int cap, int wi
 void assign_units(const SellHost &P, int n_warps, std::vector<int> &warp_ptr, std::vector<int> &warp_units,
                   double *imbalance);
 
+// Uniform diagonals (hhp_plan.cpp): true when every entry lies on one of at most max_k diagonals
+// col - row, every row's columns ascend, and padding every row to all of them adds at most
+// max_pad of the nonzeros; then doff[0..K) are the offsets ascending and mask[i] has bit k set
+// when row i stores an entry on diagonal doff[k].
+constexpr int kMaxDiag = 16;
+bool uniform_diagonals(int m, const int *rowptr, const int *col, int max_k, double max_pad, int *doff, int &K,
+                       std::vector<int> &mask);
+
 // Long rows whose SpMV epilogue records are folded together inside the SpMV (see fold_long_group).
 constexpr int kLongGroup = 32;
 
 struct PlanDev {
     int rpl = 0, H = 0, n_slices = 0, n_long = 0, n_chunks = 0, ctas = 0, warps_per_cta = 0, unroll = 4;
     bool has_perm = false, sorted = false, d16 = false;  // d16: 16-bit column offsets (scol16)
+    bool uni = false;                 // uniform diagonals: no index stream, see uniform_diagonals
+    int K = 0;                        // number of diagonals (slice width) when uni
+    int doff[kMaxDiag] = {};          // their offsets col - row, ascending
     long long total = 0;
     double padding = 1.0;
     long long *slice_ptr = nullptr;   // n_slices + 1
@@ -233,7 +244,7 @@ inline int pad4(int n) { return (n + 3) & ~3; }
 struct Tuning {
     // ctas_per_sm, spmv_unroll, rpl64: 0 = chosen per matrix at plan time; d16 0: never 16-bit offsets
     int cap = 2048, long_thr = 256, window = 8192, wpc = 8, ctas_per_sm = 0, vec_blocks_per_sm = 1,
-        unroll_iters = 4, spmv_unroll = 0, rpl64 = 0, rpl32 = 4, d16 = 1;
+        unroll_iters = 4, spmv_unroll = 0, rpl64 = 0, rpl32 = 4, d16 = 1, uni = 1;
 };
 const Tuning &tuning();
 

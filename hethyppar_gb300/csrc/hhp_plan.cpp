@@ -239,6 +239,72 @@ bool rows_ascending(int m, const int *rowptr) {
 }
 }  // namespace
 
+
+// Uniform diagonals. A matrix whose entries all lie on at most max_k diagonals (offsets col - row;
+// stencils: 5 or 7) needs no per-entry index in its slices: step k of every slice row holds the
+// entry on diagonal doff[k] (zero where the row has none, marked absent in the row's bit mask),
+// and the kernel forms the column as row + doff[k]. Accepted when every row's columns ascend
+// (the steps then keep the CSR order of each row's sum), there are at most max_k distinct offsets,
+// and padding all rows to all of them adds at most max_pad of the nonzeros. The distinct offsets
+// are found per host thread and merged; a range that meets more than max_k stops at once.
+bool uniform_diagonals(int m, const int *rowptr, const int *col, int max_k, double max_pad, int *doff, int &K,
+                       std::vector<int> &mask) {
+    K = 0;
+    if (m <= 0 || max_k <= 0 || max_k > 31) return false;
+    const long long nnz = rowptr[m];
+    if (nnz <= 0) return false;
+    const size_t n = static_cast<size_t>(m);
+    const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t nt = std::min({hw, size_t{32}, std::max<size_t>(1, n / 65536)});
+    std::vector<std::vector<int>> sets(nt);
+    std::vector<char> ok(nt, 1);
+    const size_t step = (n + nt - 1) / nt;
+    parallel_ranges(n, 65536, [&](size_t b, size_t e) {
+        const size_t id = step ? b / step : 0;
+        std::vector<int> &d = sets[std::min(id, nt - 1)];
+        for (size_t i = b; i < e; ++i) {
+            const int r = static_cast<int>(i);
+            for (int p = rowptr[i]; p < rowptr[i + 1]; ++p) {
+                if (p > rowptr[i] && col[p] <= col[p - 1]) {
+                    ok[std::min(id, nt - 1)] = 0;
+                    return;
+                }
+                const int o = col[p] - r;
+                if (std::find(d.begin(), d.end(), o) == d.end()) {
+                    if (static_cast<int>(d.size()) == max_k) {
+                        ok[std::min(id, nt - 1)] = 0;
+                        return;
+                    }
+                    d.push_back(o);
+                }
+            }
+        }
+    });
+    std::vector<int> all;
+    for (size_t t = 0; t < nt; ++t) {
+        if (!ok[t]) return false;
+        for (int o : sets[t])
+            if (std::find(all.begin(), all.end(), o) == all.end()) all.push_back(o);
+        if (static_cast<int>(all.size()) > max_k) return false;
+    }
+    std::sort(all.begin(), all.end());
+    if (static_cast<double>(all.size()) * static_cast<double>(m) > (1.0 + max_pad) * static_cast<double>(nnz)) return false;
+    K = static_cast<int>(all.size());
+    std::copy(all.begin(), all.end(), doff);
+    mask.assign(n, 0);
+    parallel_ranges(n, 65536, [&](size_t b, size_t e) {
+        for (size_t i = b; i < e; ++i) {
+            int mk = 0;
+            for (int p = rowptr[i]; p < rowptr[i + 1]; ++p) {
+                const int o = col[p] - static_cast<int>(i);
+                mk |= 1 << static_cast<int>(std::lower_bound(all.begin(), all.end(), o) - all.begin());
+            }
+            mask[i] = mk;
+        }
+    });
+    return true;
+}
+
 }  // namespace hhp
 
 extern "C" hhp_status hhp_plan_stats(int m, int nnz, const int *rowptr, int rows_per_lane, int cap, int *n_slices,

@@ -138,6 +138,7 @@ struct SellArgs {
     int *err;
     int m, n_slices, n_chunks, n_long;
     bool has_perm;
+    int doff[kMaxDiag];  // uniform-diagonal plans: the diagonals' offsets (pos_len then holds row masks)
 };
 
 __device__ __forceinline__ double vfma(double a, double b, double c) { return fma(a, b, c); }
@@ -181,7 +182,7 @@ __device__ __forceinline__ void row_epilogue(const SellArgs<VT> &a, int r, VT ac
     }
 }
 
-template <typename VT, int R, int U, int EP, bool D16>
+template <typename VT, int R, int U, int EP, bool D16, bool UNI>
 __device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, long long base, int wmax, int lane,
                                          double &d0, double &d1, double &d2) {
     using VV = typename Vec<VT, R>::V;
@@ -224,11 +225,57 @@ __device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, long long
     };
     if constexpr (EARLY) load_w();
     const VV *vp = reinterpret_cast<const VV *>(a.sval + base) + lane;
-    const CW *cp = D16 ? reinterpret_cast<const CW *>(a.scol16 + base) + lane
-                       : reinterpret_cast<const CW *>(a.scol + base) + lane;
     VT acc[R];
 #pragma unroll
     for (int t = 0; t < R; ++t) acc[t] = VT(0);
+    if constexpr (UNI) {
+        // Uniform diagonals: step k of every row is its entry on diagonal doff[k] (the column is
+        // the row plus that offset; no index stream), absent where bit k of the row's mask is
+        // clear -- no gather and no multiply-add there, so every row still sums exactly its
+        // stored entries in CSR order. pos_len holds the masks.
+        int mk[R];
+#pragma unroll
+        for (int t = 0; t < R; ++t) mk[t] = len[t];
+        VV v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) v[u] = u < wmax ? ld_stream<VT>(vp + static_cast<size_t>(u) * 32) : VV();
+        int j = 0;
+        for (; j + U <= wmax; j += U) {
+            VV vn[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int jn = j + U + u;
+                vn[u] = jn < wmax ? ld_stream<VT>(vp + static_cast<size_t>(jn) * 32) : VV();
+            }
+            VT xv[U][R];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int off = a.doff[j + u];
+#pragma unroll
+                for (int t = 0; t < R; ++t) xv[u][t] = ((mk[t] >> (j + u)) & 1) ? __ldg(a.x + row[t] + off) : VT(0);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+#pragma unroll
+                for (int t = 0; t < R; ++t)
+                    if ((mk[t] >> (j + u)) & 1) acc[t] = vfma(comp<VV, VT>(v[u], t), xv[u][t], acc[t]);
+#pragma unroll
+            for (int u = 0; u < U; ++u) v[u] = vn[u];
+        }
+#pragma unroll 1
+        for (; j < wmax; ++j) {
+            const VV vt = ld_stream<VT>(vp + static_cast<size_t>(j) * 32);
+            const int off = a.doff[j];
+            VT xt[R];
+#pragma unroll
+            for (int t = 0; t < R; ++t) xt[t] = ((mk[t] >> j) & 1) ? __ldg(a.x + row[t] + off) : VT(0);
+#pragma unroll
+            for (int t = 0; t < R; ++t)
+                if ((mk[t] >> j) & 1) acc[t] = vfma(comp<VV, VT>(vt, t), xt[t], acc[t]);
+        }
+    } else {
+    const CW *cp = D16 ? reinterpret_cast<const CW *>(a.scol16 + base) + lane
+                       : reinterpret_cast<const CW *>(a.scol + base) + lane;
     // Software pipeline over full groups of U steps: the values and indices of group g+1
     // are requested before the gathers and multiply-adds of group g, so the HBM latency of the
     // streams overlaps the L1/L2 latency of the gathers (warps issue in order: a load placed
@@ -279,6 +326,7 @@ __device__ __forceinline__ void do_slice(const SellArgs<VT> &a, int s, long long
 #pragma unroll
         for (int t = 0; t < R; ++t)
             if (j < len[t]) acc[t] = vfma(comp<VV, VT>(vt, t), xt[t], acc[t]);
+    }
     }
     if constexpr (!EARLY) load_w();
     VT e0 = VT(0), e1 = VT(0), e2 = VT(0);
@@ -387,7 +435,7 @@ struct MinCtas {
     static constexpr int value = R * U >= 8 ? 3 : (R * U >= 4 ? 5 : 6);
 };
 
-template <typename VT, int R, int U, int EP, bool D16>
+template <typename VT, int R, int U, int EP, bool D16, bool UNI = false>
 __global__ void __launch_bounds__(256, MinCtas<R, U>::value) k_spmv(const SellArgs<VT> a) {
     // After a recorded device error, with the gate closed, or once the solver's status is
     // terminal, the launch returns at once (uniform across the grid). The three words were
@@ -409,7 +457,7 @@ __global__ void __launch_bounds__(256, MinCtas<R, U>::value) k_spmv(const SellAr
         if (u < a.n_slices) {
             const long long base = static_cast<long long>(static_cast<unsigned>(rec.z)) |
                                    (static_cast<long long>(rec.w) << 32);
-            do_slice<VT, R, U, EP, D16>(a, u, base, rec.y, lane, d0, d1, d2);
+            do_slice<VT, R, U, EP, D16, UNI>(a, u, base, rec.y, lane, d0, d1, d2);
         } else {
             do_chunk<VT, EP>(a, u - a.n_slices, lane);
         }
@@ -445,24 +493,29 @@ __global__ void __launch_bounds__(256, MinCtas<R, U>::value) k_spmv(const SellAr
     }
 }
 
-template <typename VT, int R, int U, bool D16>
+template <typename VT, int R, int U, bool D16, bool UNI = false>
 cudaError_t launch_rud(EpKind ep, const PlanDev &p, const SellArgs<VT> &a, cudaStream_t s) {
     const dim3 grid(p.ctas), block(p.warps_per_cta * 32);
     switch (ep) {
-        case EP_DOT1: return launch_k(k_spmv<VT, R, U, EP_DOT1, D16>, grid, block, 0, s, a);
-        case EP_DOT2: return launch_k(k_spmv<VT, R, U, EP_DOT2, D16>, grid, block, 0, s, a);
-        case EP_DOT3: return launch_k(k_spmv<VT, R, U, EP_DOT3, D16>, grid, block, 0, s, a);
-        case EP_RESID: return launch_k(k_spmv<VT, R, U, EP_RESID, D16>, grid, block, 0, s, a);
+        case EP_DOT1: return launch_k(k_spmv<VT, R, U, EP_DOT1, D16, UNI>, grid, block, 0, s, a);
+        case EP_DOT2: return launch_k(k_spmv<VT, R, U, EP_DOT2, D16, UNI>, grid, block, 0, s, a);
+        case EP_DOT3: return launch_k(k_spmv<VT, R, U, EP_DOT3, D16, UNI>, grid, block, 0, s, a);
+        case EP_RESID: return launch_k(k_spmv<VT, R, U, EP_RESID, D16, UNI>, grid, block, 0, s, a);
         default:
             // y = A x needs no epilogue arithmetic: a separate instantiation keeps the FP64 pipe
             // free of predicated-off scale and accumulate instructions
-            if (!a.scale && !a.accum) return launch_k(k_spmv<VT, R, U, EP_Y, D16>, grid, block, 0, s, a);
-            return launch_k(k_spmv<VT, R, U, EP_AXPBY, D16>, grid, block, 0, s, a);
+            if (!a.scale && !a.accum) return launch_k(k_spmv<VT, R, U, EP_Y, D16, UNI>, grid, block, 0, s, a);
+            return launch_k(k_spmv<VT, R, U, EP_AXPBY, D16, UNI>, grid, block, 0, s, a);
     }
 }
 
+// Index mode from the plan: uniform diagonals (no index stream; plans with R >= 2 only, the
+// layouts of short regular rows), 16-bit offsets, or int32 columns.
 template <typename VT, int R, int U>
 cudaError_t launch_ru(EpKind ep, const PlanDev &p, const SellArgs<VT> &a, cudaStream_t s) {
+    if constexpr (R >= 2) {
+        if (p.uni) return launch_rud<VT, R, U, false, true>(ep, p, a, s);
+    }
     return p.d16 ? launch_rud<VT, R, U, true>(ep, p, a, s) : launch_rud<VT, R, U, false>(ep, p, a, s);
 }
 
@@ -501,6 +554,26 @@ __global__ void k_sell_fill(const int *__restrict__ rowptr, const int *__restric
     }
 }
 
+// Uniform-diagonal re-layout: row r's entry on diagonal doff[k] goes to step k of its slice (rows
+// in natural order, slices K steps wide; absent entries stay zero and masked off).
+struct DiagSet {
+    int K;
+    int d[kMaxDiag];
+};
+template <typename VT>
+__global__ void k_sell_fill_uni(const int *__restrict__ rowptr, const int *__restrict__ col,
+                                const double *__restrict__ val, int m, int H, DiagSet ds, VT *sval) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
+        const long long dst = static_cast<long long>(r / H) * ds.K * H + r % H;
+        for (int p = rowptr[r]; p < rowptr[r + 1]; ++p) {
+            const int o = col[p] - r;
+            int k = 0;
+            while (k + 1 < ds.K && ds.d[k] != o) ++k;
+            sval[dst + static_cast<long long>(k) * H] = static_cast<VT>(val[p]);
+        }
+    }
+}
+
 // bad[0] = 1 if some entry of a row with at most long_thr entries has |col - row| >= 2^15.
 __global__ void k_offsets_fit(const int *__restrict__ rowptr, const int *__restrict__ col, int m, int long_thr,
                               int *bad) {
@@ -533,6 +606,16 @@ template <typename VT>
 hhp_status fill_values(hhp_mat *A, PlanDev &p, bool with_cols) {
     const long long npos = static_cast<long long>(p.n_slices) * p.H;
     if (npos == 0) return HHP_OK;
+    if (p.uni) {
+        DiagSet ds;
+        ds.K = p.K;
+        for (int k = 0; k < kMaxDiag; ++k) ds.d[k] = p.doff[k];
+        const int grid = static_cast<int>(std::min<long long>((A->m + 255) / 256, 8LL * A->ctx->num_sms));
+        k_sell_fill_uni<VT><<<grid, 256, 0, A->ctx->stream>>>(A->rowptr, A->col, A->val, A->m, p.H, ds,
+                                                              static_cast<VT *>(p.sval));
+        HHP_CUDA(cudaGetLastError());
+        return HHP_OK;
+    }
     const int grid = static_cast<int>(std::min<long long>((npos + 255) / 256, 8LL * A->ctx->num_sms));
     k_sell_fill<VT><<<grid, 256, 0, A->ctx->stream>>>(A->rowptr, A->col, A->val, p.pos_row, p.pos_len, p.slice_ptr,
                                                       p.H, npos, static_cast<VT *>(p.sval),
@@ -570,7 +653,40 @@ hhp_status build_plan_dev(hhp_mat *A, PlanDev &p) {
         build_plan(A->m, A->rowptr_host.data(), R, std::max(t.long_thr, 1), std::max(t.cap, 32),
                    std::max(t.window, 1), h);
     }
+    // Uniform diagonals (stencils): every entry on one of at most kMaxDiag diagonals, rows in
+    // natural order, no long rows. The slices then store values only, K steps each (step k =
+    // diagonal doff[k]), and pos_len holds each row's bit mask of present diagonals. The column
+    // check reads a prefix first, so a matrix with scattered columns costs one small copy.
+    bool uni = false;
+    int K = 0, doff[kMaxDiag] = {};
+    if (t.uni && R >= 2 && h.long_rows.empty() && !h.has_perm && !h.sorted && A->m > 0 && A->nnz > 0) {
+        std::vector<int> hc;
+        std::vector<int> mask;
+        const std::vector<int> &rp = A->rowptr_host;
+        int m_pre = static_cast<int>(std::upper_bound(rp.begin(), rp.end(), 65536) - rp.begin()) - 1;
+        m_pre = std::max(1, std::min(m_pre, A->m));
+        const size_t n_pre = static_cast<size_t>(rp[static_cast<size_t>(m_pre)]);
+        hc.resize(static_cast<size_t>(A->nnz));
+        HHP_CUDA(cudaStreamSynchronize(ctx->stream));
+        HHP_CUDA(cudaMemcpy(hc.data(), A->col, sizeof(int) * n_pre, cudaMemcpyDeviceToHost));
+        if (uniform_diagonals(m_pre, rp.data(), hc.data(), kMaxDiag, 0.10, doff, K, mask)) {
+            HHP_CUDA(cudaMemcpy(hc.data() + n_pre, A->col + n_pre, sizeof(int) * (hc.size() - n_pre),
+                                cudaMemcpyDeviceToHost));
+            uni = uniform_diagonals(A->m, rp.data(), hc.data(), kMaxDiag, 0.10, doff, K, mask);
+        }
+        if (uni) {
+            for (int s2 = 0; s2 <= h.n_slices; ++s2)
+                h.slice_ptr[static_cast<size_t>(s2)] = static_cast<long long>(s2) * K * h.H;
+            h.total = static_cast<long long>(h.n_slices) * K * h.H;
+            for (size_t q = 0; q < h.pos_len.size(); ++q)
+                h.pos_len[q] = q < static_cast<size_t>(A->m) ? mask[q] : 0;
+            h.padding = static_cast<double>(h.total) / static_cast<double>(A->nnz);
+        }
+    }
     p.release();
+    p.uni = uni;
+    p.K = K;
+    for (int k = 0; k < kMaxDiag; ++k) p.doff[k] = doff[k];
     p.rpl = R;
     p.unroll = U;
     p.H = h.H;
@@ -623,7 +739,7 @@ hhp_status build_plan_dev(hhp_mat *A, PlanDev &p) {
     // Index words: 16-bit offsets col - row when every slice row's entries lie within 2^15 of
     // the diagonal (stencils: 2 bytes per nonzero instead of 4), else int32 columns.
     p.d16 = false;
-    if (t.d16 && A->m > 0 && A->nnz > 0) {
+    if (t.d16 && !p.uni && A->m > 0 && A->nnz > 0) {
         int *bad = nullptr, hbad = 0;
         HHP_CUDA(cudaMalloc(&bad, sizeof(int)));
         cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream);
@@ -636,7 +752,9 @@ hhp_status build_plan_dev(hhp_mat *A, PlanDev &p) {
         HHP_CUDA(e2);
         p.d16 = hbad == 0;
     }
-    if (p.d16) {
+    if (p.uni) {
+        // no index stream
+    } else if (p.d16) {
         HHP_CUDA(cudaMalloc(&p.scol16, tot * sizeof(short)));
         HHP_CUDA(cudaMemsetAsync(p.scol16, 0, tot * sizeof(short), ctx->stream));
     } else {
@@ -700,6 +818,7 @@ SellArgs<VT> make_args(hhp_mat *A, const PlanDev &p, const VT *csr_val, const VT
     a.n_chunks = p.n_chunks;
     a.n_long = p.n_long;
     a.has_perm = p.has_perm;
+    for (int k = 0; k < kMaxDiag; ++k) a.doff[k] = p.doff[k];
     return a;
 }
 
