@@ -435,8 +435,17 @@ struct MinCtas {
     static constexpr int value = R * U >= 8 ? 3 : (R * U >= 4 ? 5 : 6);
 };
 
+// Uniform-diagonal slices carry no index words: the wide FP32 layouts (R * U >= 8) then fit 4 CTAs
+// of 256 threads per SM in 64 registers without spills, and the plan launches 4 (FP32 C4 mixed
+// solve 127.9 -> 121.1 us per iteration). FP64 keeps its counts (the stencil layout, R * U = 4,
+// runs 5; the wide FP64 one would spill at 64 registers).
+template <typename VT, int R, int U, bool UNI>
+struct MinCtasFor {
+    static constexpr int value = UNI && sizeof(VT) == 4 && R * U >= 8 ? 4 : MinCtas<R, U>::value;
+};
+
 template <typename VT, int R, int U, int EP, bool D16, bool UNI = false>
-__global__ void __launch_bounds__(256, MinCtas<R, U>::value) k_spmv(const SellArgs<VT> a) {
+__global__ void __launch_bounds__(256, MinCtasFor<VT, R, U, UNI>::value) k_spmv(const SellArgs<VT> a) {
     // After a recorded device error, with the gate closed, or once the solver's status is
     // terminal, the launch returns at once (uniform across the grid). The three words were
     // written by earlier launches: read together (one memory latency, not three), through L2.
@@ -683,6 +692,7 @@ hhp_status build_plan_dev(hhp_mat *A, PlanDev &p) {
             h.padding = static_cast<double>(h.total) / static_cast<double>(A->nnz);
         }
     }
+    if (uni && !std::is_same<VT, double>::value && R * U >= 8 && t.ctas_per_sm <= 0) cps = 4;
     p.release();
     p.uni = uni;
     p.K = K;
