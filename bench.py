@@ -42,6 +42,16 @@ METRIC = "BiCGStab time to rel-res 1e-10 (mixed vs FP64); SpMV GB/s/HBM peak; fw
 WORKLOAD = "c2: banded random 450000x450000, 17 nnz/row (7.65M nnz), FP64, int32 CSR, rtol 1e-10, x0=0"
 DATA = "synthetic, seeded (hethyppar_gb300.synth); stands in for cage13-scale SuiteSparse inputs"
 FLUSH_BYTES = 256 << 20  # twice the 129 MB L2
+HOLD_CYCLES = 400_000     # ~0.2 ms of GPU clock: the device stays busy while the host enqueues
+
+
+def _hold(stream):
+    """Keeps the device busy for ~0.2 ms on `stream` after an L2 flush, so that the host's launch
+    latency for the start event and the timed work (Python, ctypes, stream-order events) falls
+    inside the hold rather than between the events."""
+    import torch
+    with torch.cuda.stream(stream):
+        torch.cuda._sleep(HOLD_CYCLES)
 RTOL = 1e-10
 
 
@@ -482,6 +492,7 @@ def run_ours(args, rk):
             with torch.cuda.stream(stream):
                 flush.add_(1.0)
                 flush_r.sum()
+            _hold(stream)
 
     s = synth.config("c2")
     A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
@@ -890,6 +901,7 @@ def run_spmv_only(args):
         with torch.cuda.stream(stream):
             flush.add_(1.0)
             flush_r.sum()
+        _hold(stream)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         run()
@@ -931,6 +943,7 @@ def run_config_solve(args):
         with torch.cuda.stream(stream):
             flush.add_(1.0)
             flush_r.sum()
+        _hold(stream)
     s = synth.config(args.config)
     perm = reorder_color(s.rowptr, s.col)[0] if args.precond == "ilu0" else None
     A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val, perm=perm)
