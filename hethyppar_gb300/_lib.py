@@ -93,6 +93,7 @@ SIGNATURES = [
     ("hhp_csr_file_write", _I, [_S, _I, _I, _I, _P, _P, _P]),
     ("hhp_reorder_rcm", _I, [_I, _P, _P, _P]),
     ("hhp_reorder_color", _I, [_I, _P, _P, _P, _PI]),
+    ("hhp_mat_drop_csr", _I, [_P, _I]),
     ("hhp_ilu0_factor", _I, [_P, _P, _P, _P]),
     ("hhp_ilu0_apply_dev", _I, [_P, _P, _P, _P]),
     ("hhp_dot_dev", _I, [_P, _I, _P, _P, _P]),

@@ -199,6 +199,11 @@ class Matrix:
             v = _host(val, np.float64)
             check(lib().hhp_mat_set_values(self._h, _ptr(v)), "hhp_mat_set_values")
 
+    def drop_csr(self, keep_fp32: bool = False):
+        """hhp_mat_drop_csr: keep only the SpMV layouts (FP32 too if keep_fp32) and free the CSR
+        arrays; later calls that need them raise HHPError."""
+        check(lib().hhp_mat_drop_csr(self._h, 1 if keep_fp32 else 0), "hhp_mat_drop_csr")
+
     def get_csr(self):
         m, _ = self.shape
         rp = np.empty(m + 1, np.int32)

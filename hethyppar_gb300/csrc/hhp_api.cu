@@ -135,7 +135,14 @@ hhp_status mat_create_dev(hhp_ctx *ctx, int m, int n, int nnz, hhp_mat **out) {
     return HHP_OK;
 }
 
+hhp_status csr_needed(const hhp_mat *A, const char *what) {
+    if (!A->csr_dropped) return HHP_OK;
+    set_error("%s needs the matrix's CSR arrays, which hhp_mat_drop_csr released", what);
+    return HHP_ERR_STATE;
+}
+
 hhp_status mat_refresh_derived(hhp_mat *A) {
+    HHP_TRY(csr_needed(A, "the FP32 value copy"));
     if (!A->val32) {
         HHP_CUDA(cudaMalloc(&A->val32, (static_cast<size_t>(A->nnz) + 4) * sizeof(float)));
         HHP_CUDA(cudaMemsetAsync(A->val32, 0, (static_cast<size_t>(A->nnz) + 4) * sizeof(float), A->ctx->stream));
@@ -381,6 +388,34 @@ void hhp_mat_destroy(hhp_mat *A) {
     delete A;
 }
 
+hhp_status hhp_mat_drop_csr(hhp_mat *A, int keep_fp32) {
+    HHP_API_BEGIN
+    if (!A) {
+        set_error("hhp_mat_drop_csr: null matrix");
+        return HHP_ERR_ARG;
+    }
+    if (A->csr_dropped) return HHP_OK;
+    HHP_TRY(ensure_plan(A, false));
+    if (keep_fp32) {
+        if (!A->val32) HHP_TRY(mat_refresh_derived(A));
+        HHP_TRY(ensure_plan(A, true));
+    }
+    if (A->plan64.n_chunks > 0 || (A->plan32.built() && A->plan32.n_chunks > 0)) {
+        set_error("hhp_mat_drop_csr: rows longer than the slice limit are summed from the CSR arrays");
+        return HHP_ERR_ARG;
+    }
+    HHP_CUDA(cudaStreamSynchronize(A->ctx->stream));
+    cudaFree(A->col);
+    cudaFree(A->val);
+    cudaFree(A->val32);
+    A->col = nullptr;
+    A->val = nullptr;
+    A->val32 = nullptr;
+    A->csr_dropped = true;
+    return HHP_OK;
+    HHP_API_END
+}
+
 hhp_status hhp_mat_shape(const hhp_mat *A, int *m, int *n, int *nnz) {
     if (!A) return HHP_ERR_ARG;
     if (m) *m = A->m;
@@ -394,6 +429,7 @@ static hhp_status set_values(hhp_mat *A, const double *v, cudaMemcpyKind kind) {
         set_error("hhp_mat_set_values: invalid arguments");
         return HHP_ERR_ARG;
     }
+    HHP_TRY(csr_needed(A, "hhp_mat_set_values"));
     if (A->nnz > 0)
         HHP_CUDA(cudaMemcpyAsync(A->val, v, sizeof(double) * static_cast<size_t>(A->nnz), kind, A->ctx->stream));
     if (A->val32 || A->t || A->plan64.built() || A->plan32.built()) HHP_TRY(mat_refresh_derived(A));
@@ -409,6 +445,7 @@ hhp_status hhp_mat_set_values_dev(hhp_mat *A, const double *val) { return set_va
 hhp_status hhp_mat_get_csr(const hhp_mat *A, int *rowptr, int *col, double *val) {
     HHP_API_BEGIN
     if (!A) return HHP_ERR_ARG;
+    HHP_TRY(csr_needed(A, "hhp_mat_get_csr"));
     HHP_CUDA(cudaStreamSynchronize(A->ctx->stream));
     if (rowptr) HHP_CUDA(cudaMemcpy(rowptr, A->rowptr, sizeof(int) * (static_cast<size_t>(A->m) + 1), cudaMemcpyDeviceToHost));
     if (col && A->nnz) HHP_CUDA(cudaMemcpy(col, A->col, sizeof(int) * static_cast<size_t>(A->nnz), cudaMemcpyDeviceToHost));

@@ -676,6 +676,7 @@ hhp_status ensure_ilu(hhp_mat *A, int *levels) {
         set_error("ilu0 needs a square, non-empty matrix");
         return HHP_ERR_ARG;
     }
+    HHP_TRY(csr_needed(A, "ILU(0)"));
     IluDev *I = new IluDev();
     hhp_status rc;
     try {

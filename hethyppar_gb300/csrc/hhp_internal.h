@@ -163,9 +163,13 @@ struct hhp_mat {
     hhp_mat *jac_row = nullptr;
     double *jac_row_b = nullptr;
     hhp::IluDev *ilu = nullptr;       // ILU(0) factors (lazily built)
+    bool csr_dropped = false;         // col / val / val32 freed by hhp_mat_drop_csr
 };
 
 namespace hhp {
+
+// HHP_ERR_STATE (with the message) when A's CSR arrays were dropped and `what` needs them.
+hhp_status csr_needed(const hhp_mat *A, const char *what);
 
 // ---- SpMV launchers (hhp_spmv.cu) ----------------------------------------------------------------
 // Epilogue kinds of the fused SpMV.

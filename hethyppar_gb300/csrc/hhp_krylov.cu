@@ -1269,7 +1269,12 @@ hhp_status ensure_solver(hhp_mat *A, Solver **out, int maxit) {
 }
 
 hhp_status ensure_fp32_inner(hhp_mat *A, Solver *s) {
-    if (!A->val32) HHP_TRY(mat_refresh_derived(A));
+    // a matrix whose CSR was dropped keeps the FP32 layout it was given (or has none)
+    if (A->csr_dropped) {
+        if (!A->plan32.built()) return csr_needed(A, "the mixed form (drop the CSR with keep_fp32)");
+    } else if (!A->val32) {
+        HHP_TRY(mat_refresh_derived(A));
+    }
     if (!s->D32) {
         hhp_status st = HHP_OK;
         const size_t np = static_cast<size_t>(s->n_pad);

@@ -75,6 +75,7 @@ int grid_for(const hhp_mat *A, long long n) {
 
 hhp_status ensure_jacobi(hhp_mat *A) {
     if (A->jac) return HHP_OK;
+    HHP_TRY(csr_needed(A, "Jacobi preconditioning"));
     if (A->m != A->n) {
         set_error("Jacobi preconditioning needs a square matrix");
         return HHP_ERR_ARG;
@@ -137,6 +138,7 @@ hhp_status ensure_jacobi(hhp_mat *A) {
 // A with row i scaled by 1/a_ii (A->jac_row), and room for the scaled right-hand side.
 hhp_status ensure_jacobi_row(hhp_mat *A) {
     if (A->jac_row) return HHP_OK;
+    HHP_TRY(csr_needed(A, "row Jacobi preconditioning"));
     HHP_TRY(ensure_jacobi(A));  // the diagonal (and its checks) come from the column-scaled form
     cudaStream_t st = A->ctx->stream;
     hhp_mat *J = nullptr;

@@ -859,6 +859,7 @@ void PlanDev::release() {
 hhp_status ensure_plan(hhp_mat *A, bool fp32) {
     PlanDev &p = fp32 ? A->plan32 : A->plan64;
     if (p.built()) return HHP_OK;
+    HHP_TRY(csr_needed(A, fp32 ? "an FP32 SpMV layout" : "an FP64 SpMV layout"));
     if (fp32) return build_plan_dev<float>(A, p);
     return build_plan_dev<double>(A, p);
 }

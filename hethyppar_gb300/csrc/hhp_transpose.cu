@@ -169,6 +169,7 @@ int grid_for(const hhp_ctx *ctx, long long n, int threads) {
 
 hhp_status ensure_transpose(hhp_mat *A) {
     if (A->t) return HHP_OK;
+    HHP_TRY(csr_needed(A, "the transpose"));
     hhp_ctx *ctx = A->ctx;
     cudaStream_t st = ctx->stream;
     const int m = A->m, n = A->n, nnz = A->nnz;
@@ -243,6 +244,7 @@ hhp_status refresh_transpose_values(hhp_mat *A) {
 
 hhp_status launch_dlda(hhp_mat *A, cudaStream_t s, const double *lambda, const double *x, double *dlda) {
     if (A->nnz == 0) return HHP_OK;
+    HHP_TRY(csr_needed(A, "dL/dA"));
     k_dlda<<<grid_for(A->ctx, A->nnz, 256), 256, 0, s>>>(A->rowidx, A->col, lambda, x, A->nnz, dlda);
     A->ctx->kernel_launches += 1;
     HHP_CUDA(cudaGetLastError());

@@ -159,6 +159,15 @@ hhp_status hhp_mat_set_values(hhp_mat *mat, const double *val);
 hhp_status hhp_mat_set_values_dev(hhp_mat *mat, const double *val_dev);
 /* Copy the device CSR back to host arrays (m+1, nnz, nnz; any may be NULL). */
 hhp_status hhp_mat_get_csr(const hhp_mat *mat, int *rowptr, int *col, double *val);
+/* Solve-only matrices: builds the FP64 SpMV layout (and the FP32 one when keep_fp32 != 0, for the
+ * mixed form), then frees the canonical CSR's column and value arrays (12 bytes per nonzero) and
+ * the FP32 value copy, keeping the sliced copies the SpMV reads. Afterwards the matrix still
+ * serves SpMV and solves (FP64; mixed if keep_fp32) and everything built before the call (the
+ * transpose, Jacobi scaling, ILU(0) factors); whatever needs the CSR later -- new values,
+ * hhp_mat_get_csr, a first transpose, dL/dA, a first preconditioner, a layout not built --
+ * returns HHP_ERR_STATE. HHP_ERR_ARG when rows longer than the slice limit exist (their chunks
+ * are read from the CSR). Idempotent. */
+hhp_status hhp_mat_drop_csr(hhp_mat *mat, int keep_fp32);
 /* Host CSR of A^T built on the device (a stable radix sort of A's entries by column; within a row
  * of A^T entries are in increasing row order of A, as CSR_to_CSC src/util/hhp_matrix.c:1476-1535).
  * Arrays n+1, nnz, nnz. */
