@@ -436,8 +436,8 @@ struct MinCtas {
 };
 
 // Uniform-diagonal slices carry no index words: the wide FP32 layouts (R * U >= 8) then fit 4 CTAs
-// of 256 threads per SM in 64 registers without spills, and the plan launches 4 (FP32 C4 mixed
-// solve 127.9 -> 121.1 us per iteration). FP64 keeps its counts (the stencil layout, R * U = 4,
+// of 256 threads per SM in 64 registers without spills, and the plan launches 4 (the mixed solve
+// of the 160^3 7-point stencil: 127.9 -> 121.1 us per inner iteration). FP64 keeps its counts (the stencil layout, R * U = 4,
 // runs 5; the wide FP64 one would spill at 64 registers).
 template <typename VT, int R, int U, bool UNI>
 struct MinCtasFor {
@@ -711,7 +711,7 @@ hhp_status build_plan_dev(hhp_mat *A, PlanDev &p) {
     // A small matrix gets no more CTAs than it has work units for its warps: every CTA writes a
     // partial record that every consumer of the epilogue's dot products reduces, and a 65k-row
     // stencil (1024 slices) on 5 CTAs per SM left 5 of every 6 warps idle while its consumers
-    // reduced 760 records (C1: 27.7 -> 24.4 us per iteration on one CTA per SM)
+    // reduced 760 records (that solve: 27.7 -> 24.4 us per iteration on one CTA per SM)
     if (t.ctas_per_sm <= 0) {
         const long long units = static_cast<long long>(h.n_slices) + static_cast<long long>(h.chunks.size());
         const long long per_cps = static_cast<long long>(ctx->num_sms) * p.warps_per_cta;
