@@ -48,6 +48,7 @@ constexpr unsigned kBarrierSpins = 1u << 22;  // bounded wait (x ~64 ns sleeps: 
 
 struct IluTri {
     int n_levels = 0, n_slices = 0, n_long = 0, n_big = 0;
+    int head_slice = 0, head_long = 0, head_big = 0;  // lev_*[min(2, n_levels)], kept on the host
     long long slots = 0;
     int *lev_slice = nullptr;        // n_levels + 1: the slices of each level
     int *lev_long = nullptr;         // n_levels + 1: the long rows of each level
@@ -97,6 +98,7 @@ namespace {
 
 struct TriArgs {
     int n_levels;
+    int head_slice, head_long, head_big;  // ends of the first pass's ranges (levels 0 and 1)
     const int *lev_slice, *lev_long, *lev_big;
     const long long *slice_ptr;
     const int *slice_row, *slice_len, *scol;
@@ -105,8 +107,8 @@ struct TriArgs {
 };
 
 TriArgs args_of(const IluTri &t) {
-    return TriArgs{t.n_levels, t.lev_slice, t.lev_long, t.lev_big, t.slice_ptr, t.slice_row, t.slice_len, t.scol,
-                   t.sval, t.long_row, t.big_row};
+    return TriArgs{t.n_levels, t.head_slice, t.head_long, t.head_big, t.lev_slice, t.lev_long, t.lev_big,
+                   t.slice_ptr, t.slice_row, t.slice_len, t.scol, t.sval, t.long_row, t.big_row};
 }
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
@@ -258,15 +260,28 @@ __global__ void __launch_bounds__(kIluThreads, 1) k_ilu_tri(TriArgs t, const int
                                                          int *dev_err) {
     __shared__ double wsum[kIluThreads / 32];
     if (blockIdx.x == 0 && threadIdx.x == 0) *bar_other = 0u;
-    if (stop && *reinterpret_cast<volatile const int *>(stop) != ST_RUNNING) return;
-    if (*reinterpret_cast<volatile int *>(dev_err) != DEV_OK) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int gw = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int W = static_cast<int>((gridDim.x * blockDim.x) >> 5);
+    // The first pass's bounds are arguments, so this warp's first slices' row data is pulled into
+    // L1 while the two status words (written by earlier launches) are read together.
+    for (int s = gw; s < t.head_slice && s < gw + 2 * W; s += W) {
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(t.slice_row + 32LL * s + lane));
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(t.slice_len + 32LL * s + lane));
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(t.slice_ptr + s));
+    }
+    const int run = stop ? *reinterpret_cast<volatile const int *>(stop) : ST_RUNNING;
+    const int err = *reinterpret_cast<volatile int *>(dev_err);
+    if (run != ST_RUNNING || err != DEV_OK) return;
     unsigned barriers = 0;
     for (int lev = 0; lev < t.n_levels; ++lev) {
-        const Dep<UPPER> z{in, dinv, out, lev == 1};
-        for (int q = t.lev_big[lev] + blockIdx.x; q < t.lev_big[lev + 1]; q += gridDim.x) {
+        // levels 0 and 1 as one range of rows (level-0 rows have no entries, so `z` is never
+        // called for them): a warp's slices of both levels are in flight together
+        const bool head = lev == 0;
+        const int le = head && t.n_levels > 1 ? 2 : lev + 1;
+        const Dep<UPPER> z{in, dinv, out, le == 2};
+        const int big_lo = head ? 0 : t.lev_big[lev], big_hi = head ? t.head_big : t.lev_big[le];
+        for (int q = big_lo + blockIdx.x; q < big_hi; q += gridDim.x) {
             const int row = t.big_row[q];
             const int b = UPPER ? dpos[row] + 1 : rowptr[row];
             const int e = UPPER ? rowptr[row + 1] : dpos[row];
@@ -282,7 +297,8 @@ __global__ void __launch_bounds__(kIluThreads, 1) k_ilu_tri(TriArgs t, const int
             }
             __syncthreads();
         }
-        for (int q = t.lev_long[lev] + gw; q < t.lev_long[lev + 1]; q += W) {
+        const int long_lo = head ? 0 : t.lev_long[lev], long_hi = head ? t.head_long : t.lev_long[le];
+        for (int q = long_lo + gw; q < long_hi; q += W) {
             const int row = t.long_row[q];
             const int b = UPPER ? dpos[row] + 1 : rowptr[row];
             const int e = UPPER ? rowptr[row + 1] : dpos[row];
@@ -297,8 +313,8 @@ __global__ void __launch_bounds__(kIluThreads, 1) k_ilu_tri(TriArgs t, const int
         // before its FMAs, so a warp has two slices' chains of dependent requests (row data, then
         // slots, then gathers) in flight at once. A step past a lane's row length loads nothing
         // and adds fma(-0, 0, acc), which leaves acc unchanged bit for bit.
-        const int s_hi = t.lev_slice[lev + 1];
-        for (int s = t.lev_slice[lev] + gw; s < s_hi; s += 2 * W) {
+        const int s_hi = head ? t.head_slice : t.lev_slice[le];
+        for (int s = (head ? 0 : t.lev_slice[lev]) + gw; s < s_hi; s += 2 * W) {
             const int sb = s + W;
             const bool two = sb < s_hi;
             const int r0 = t.slice_row[32 * s + lane];
@@ -333,6 +349,7 @@ __global__ void __launch_bounds__(kIluThreads, 1) k_ilu_tri(TriArgs t, const int
             if (r0 >= 0) __stcg(out + r0, UPPER ? a0 * dinv[r0] : a0);
             if (r1 >= 0) __stcg(out + r1, UPPER ? a1 * dinv[r1] : a1);
         }
+        lev = le - 1;
         if (lev >= 1 && lev + 1 < t.n_levels && !grid_barrier(bar, ++barriers, dev_err)) return;
     }
 }
@@ -429,6 +446,10 @@ hhp_status upload_tri(const TriHost &h, IluTri &d, int **sidx_dev, cudaStream_t 
     d.n_long = static_cast<int>(h.long_row.size());
     d.n_big = static_cast<int>(h.big_row.size());
     d.slots = h.slice_ptr.back();
+    const size_t head = static_cast<size_t>(std::min(2, h.n_levels));
+    d.head_slice = h.lev_slice[head];
+    d.head_long = h.lev_long[head];
+    d.head_big = h.lev_big[head];
     HHP_TRY(upload(&d.lev_slice, h.lev_slice, st));
     HHP_TRY(upload(&d.lev_long, h.lev_long, st));
     HHP_TRY(upload(&d.slice_ptr, h.slice_ptr, st));
