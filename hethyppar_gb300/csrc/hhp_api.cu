@@ -405,6 +405,7 @@ hhp_status hhp_mat_drop_csr(hhp_mat *A, int keep_fp32) {
         return HHP_ERR_ARG;
     }
     HHP_CUDA(cudaStreamSynchronize(A->ctx->stream));
+    ilu_keep_col(A);  // ILU(0) factors built before the drop keep their column array
     cudaFree(A->col);
     cudaFree(A->val);
     cudaFree(A->val32);

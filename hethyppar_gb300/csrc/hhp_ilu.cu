@@ -10,9 +10,10 @@
 //   lays every triangle out by level: rows with at most kIluLong entries in 32-row slices
 //   (column-major inside a slice, so a warp's lanes read consecutive slots, rows sorted by
 //   length inside a level so a slice's lanes have similar lengths), longer rows on a list that
-//   a whole warp sums.
-// * One cooperative kernel factors A (IKJ order, a warp per row) and one cooperative kernel per
-//   triangle solves it, each walking the levels in order with a grid barrier between levels:
+//   a whole warp sums, rows past kIluBig entries on one that a whole block sums.
+// * One cooperative kernel factors A (IKJ order, a warp per row) and one kernel per triangle
+//   solves it, each walking the levels in order with a grid barrier between levels (levels 0
+//   and 1 share a pass, so a two-level triangle needs no barrier and gets an ordinary launch):
 //   two launches per application whatever the level count, so the solve graph stays small.
 //   Every barrier wait is bounded; a wait that runs out sets the context's error word and the
 //   kernel returns, which ends the solve with HHP_ERR_TIMEOUT.
@@ -90,6 +91,7 @@ struct IluDev {
     // A row whose columns are not ascending (a matrix reordered by csr_permute keeps its rows'
     // entry order) is factored in ascending column order: col holds the sorted columns and src[q]
     // the CSR position of sorted entry q (both empty / null when every row is already sorted).
+    // After hhp_mat_drop_csr, col is the matrix's own column array, taken over (ilu_keep_col).
     int *col = nullptr;
     std::vector<int> src;
 };
@@ -721,6 +723,14 @@ long long ilu_generation(const hhp_mat *A) { return A->ilu ? A->ilu->gen : 0; }
 void release_ilu(hhp_mat *A) {
     free_ilu(A->ilu);
     A->ilu = nullptr;
+}
+
+void ilu_keep_col(hhp_mat *A) {
+    // the warp- and block-summed rows of the triangles read their columns from this array
+    if (A->ilu && !A->ilu->col) {
+        A->ilu->col = A->col;
+        A->col = nullptr;
+    }
 }
 
 hhp_status launch_ilu_apply(hhp_mat *A, cudaStream_t st, const double *in, double *out, const int *stop) {

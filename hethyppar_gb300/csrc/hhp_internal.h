@@ -222,6 +222,8 @@ hhp_status solve_jacobi_row(hhp_mat *A, const double *b, double *x, const double
 // in A's CSR order, to the host.
 hhp_status ensure_ilu(hhp_mat *A, int *levels = nullptr);
 void release_ilu(hhp_mat *A);
+// Before hhp_mat_drop_csr frees A->col: factors that read their columns there take it over.
+void ilu_keep_col(hhp_mat *A);
 hhp_status launch_ilu_apply(hhp_mat *A, cudaStream_t st, const double *in, double *out, const int *stop);
 hhp_status ilu_factors(hhp_mat *A, double *lu_host);
 // Identifies the current factorization (0: none); graphs that captured its arrays compare it.

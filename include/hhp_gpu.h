@@ -79,8 +79,9 @@ typedef enum {
  * (src/entry/bicgstab_gpu_dp.c:165-196): rho_new = r.r0 and ||r|| as direct dot products of the
  * new residual. AUTO (0, the default): MERGED for hhp_bicgstab*, CLASSIC for the adjoint solve of
  * hhp_bicgstab_backward* (whose tolerances sit near the rounding floor, where the direct dot
- * products reach a lower true residual). Fixed-iteration runs always use CLASSIC; the FP32 inner
- * loop of the mixed form is classic. */
+ * products reach a lower true residual). Fixed-iteration runs and ILU(0)-preconditioned solves
+ * always use CLASSIC; the FP32 inner loop of the mixed form follows the same choice (MERGED: its
+ * kernel with the x and r updates also takes the reliable-update test). */
 typedef enum { HHP_LOOP_AUTO = 0, HHP_LOOP_MERGED = 1, HHP_LOOP_CLASSIC = 2 } hhp_loop;
 
 typedef struct {
@@ -163,7 +164,8 @@ hhp_status hhp_mat_get_csr(const hhp_mat *mat, int *rowptr, int *col, double *va
  * mixed form), then frees the canonical CSR's column and value arrays (12 bytes per nonzero) and
  * the FP32 value copy, keeping the sliced copies the SpMV reads. Afterwards the matrix still
  * serves SpMV and solves (FP64; mixed if keep_fp32) and everything built before the call (the
- * transpose, Jacobi scaling, ILU(0) factors); whatever needs the CSR later -- new values,
+ * transpose, Jacobi scaling, ILU(0) factors, which keep the column array: 4 bytes per nonzero);
+ * whatever needs the CSR later -- new values,
  * hhp_mat_get_csr, a first transpose, dL/dA, a first preconditioner, a layout not built --
  * returns HHP_ERR_STATE. HHP_ERR_ARG when rows longer than the slice limit exist (their chunks
  * are read from the CSR). Idempotent. */

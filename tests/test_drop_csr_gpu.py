@@ -64,3 +64,26 @@ def test_long_rows_keep_their_csr(ctx):
     y = A.spmv(s.x_target)
     assert np.allclose(y, orc.spmv(s.rowptr, s.col, s.val, s.x_target), rtol=1e-12, atol=1e-12)
     A.close()
+
+
+def test_ilu_factors_built_before_the_drop_keep_working(ctx):
+    # rows of up to 251 entries: no SpMV chunks, so the drop is allowed, but triangle rows past 64
+    # entries, which the ILU(0) kernels sum warp-wide from the factors' column array
+    s = synth.powerlaw(20_000, max_len=250, n_dense=0, seed=11)
+    i = np.repeat(np.arange(s.rowptr.size - 1), np.diff(s.rowptr))
+    assert np.bincount(i[s.col < i]).max() > 64 and np.diff(s.rowptr).max() <= 256
+    A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
+    lu0, lev0 = A.ilu0_factor()
+    r = dev(s.b)
+    z0, z1 = torch.empty_like(r), torch.empty_like(r)
+    A.ilu0_apply_dev(r, z0)
+    x0, i0 = bicgstab(ctx, A, s.b, rtol=1e-10, maxit=500, precond="ilu0")
+    A.drop_csr()
+    A.ilu0_apply_dev(r, z1)
+    torch.cuda.synchronize()
+    assert torch.equal(z0, z1)
+    x1, i1 = bicgstab(ctx, A, s.b, rtol=1e-10, maxit=500, precond="ilu0")
+    assert i1.status == i0.status == 0 and i1.iters == i0.iters and np.array_equal(x1, x0)
+    lu1, lev1 = A.ilu0_factor()
+    assert lev1 == lev0 and np.array_equal(lu1, lu0)
+    A.close()
