@@ -260,6 +260,8 @@ bool uniform_diagonals(int m, const int *rowptr, const int *col, int max_k, doub
     std::vector<char> ok(nt, 1);
     const size_t step = (n + nt - 1) / nt;
     parallel_ranges(n, 65536, [&](size_t b, size_t e) {
+        // parallel_ranges derives nt and step exactly as above and gives range t the rows
+        // [t * step, (t + 1) * step): b / step is the range's own index, one set per range
         const size_t id = step ? b / step : 0;
         std::vector<int> &d = sets[std::min(id, nt - 1)];
         for (size_t i = b; i < e; ++i) {
