@@ -1,5 +1,6 @@
 // sanitize_host.cpp -- drives the library's host-only code (Matrix Market and binary CSR reader,
-// vector files, SpMV work plan, reverse Cuthill-McKee) with ordinary, malformed and large inputs.
+// vector files, SpMV work plan and its uniform-diagonal check, reverse Cuthill-McKee, multicolour
+// order) with ordinary, malformed and large inputs.
 // tests/test_sanitize_cpu.py compiles it with hhp_io.cpp, hhp_plan.cpp and hhp_reorder.cpp under
 // AddressSanitizer + UndefinedBehaviorSanitizer, and again under ThreadSanitizer for the parallel
 // reader; any report, leak or failed check ends the run with a nonzero status. No CUDA call is
@@ -290,6 +291,90 @@ void rcm() {
     CHECK(hhp_reorder_rcm(-1, rp, col, perm) == HHP_ERR_ARG);
 }
 
+// 5-point stencil of an nx x nx grid, columns ascending in every row.
+void stencil5(int nx, std::vector<int> &rp, std::vector<int> &col) {
+    const int m = nx * nx;
+    rp.assign(1, 0);
+    col.clear();
+    for (int i = 0; i < m; ++i) {
+        const int x = i % nx, y = i / nx;
+        if (y > 0) col.push_back(i - nx);
+        if (x > 0) col.push_back(i - 1);
+        col.push_back(i);
+        if (x + 1 < nx) col.push_back(i + 1);
+        if (y + 1 < nx) col.push_back(i + nx);
+        rp.push_back(static_cast<int>(col.size()));
+    }
+}
+
+void uniform() {
+    int doff[hhp::kMaxDiag] = {};
+    int K = -1;
+    std::vector<int> mask, rp, col;
+    // 160,000 rows: the threaded pass (one offset set per range) runs with several ranges
+    stencil5(400, rp, col);
+    const int m = static_cast<int>(rp.size()) - 1;
+    CHECK(hhp::uniform_diagonals(m, rp.data(), col.data(), hhp::kMaxDiag, 0.10, doff, K, mask));
+    CHECK(K == 5 && doff[0] == -400 && doff[1] == -1 && doff[2] == 0 && doff[3] == 1 && doff[4] == 400);
+    CHECK(mask.size() == static_cast<size_t>(m));
+    for (int i = 0; i < m && K == 5; ++i) {
+        int want = 0;
+        for (int p = rp[static_cast<size_t>(i)]; p < rp[static_cast<size_t>(i) + 1]; ++p)
+            for (int k = 0; k < K; ++k)
+                if (col[static_cast<size_t>(p)] - i == doff[k]) want |= 1 << k;
+        CHECK(mask[static_cast<size_t>(i)] == want);
+    }
+    // refusals: a row whose columns do not ascend, more offsets than allowed, too much padding,
+    // no rows
+    std::vector<int> c2 = col;
+    std::swap(c2[100], c2[101]);
+    CHECK(!hhp::uniform_diagonals(m, rp.data(), c2.data(), hhp::kMaxDiag, 0.10, doff, K, mask));
+    CHECK(!hhp::uniform_diagonals(m, rp.data(), col.data(), 4, 0.10, doff, K, mask));
+    {
+        // every row has its diagonal, one row in 50 also an entry 7 to the right: 2 offsets for
+        // 1.02 entries per row pads by ~96 %
+        std::vector<int> r3(1, 0), c3;
+        for (int i = 0; i < 200000; ++i) {
+            c3.push_back(i);
+            if (i % 50 == 0 && i + 7 < 200000) c3.push_back(i + 7);
+            r3.push_back(static_cast<int>(c3.size()));
+        }
+        CHECK(!hhp::uniform_diagonals(200000, r3.data(), c3.data(), hhp::kMaxDiag, 0.10, doff, K, mask));
+        CHECK(hhp::uniform_diagonals(200000, r3.data(), c3.data(), hhp::kMaxDiag, 1.0, doff, K, mask));
+        CHECK(K == 2 && doff[0] == 0 && doff[1] == 7);
+    }
+    CHECK(!hhp::uniform_diagonals(0, rp.data(), col.data(), hhp::kMaxDiag, 0.10, doff, K, mask));
+}
+
+void color() {
+    std::mt19937 rng(9);
+    std::vector<int> rp, col;
+    stencil5(300, rp, col);
+    const int m = static_cast<int>(rp.size()) - 1;
+    std::vector<int> perm(static_cast<size_t>(m), -1);
+    int nc = -1;
+    CHECK(hhp_reorder_color(m, rp.data(), col.data(), perm.data(), &nc) == HHP_OK);
+    CHECK(nc == 2);  // the 5-point stencil is bipartite: red-black
+    for (int m2 : {0, 1, 37, 20000}) {
+        std::vector<int> lens(static_cast<size_t>(m2));
+        for (auto &x : lens) x = static_cast<int>(rng() % 7);
+        const std::vector<int> r2 = rowptr_of(lens);
+        std::vector<int> c2(static_cast<size_t>(r2.back()) + 1);
+        for (int k = 0; k < r2.back(); ++k) c2[static_cast<size_t>(k)] = static_cast<int>(rng() % static_cast<unsigned>(m2));
+        std::vector<int> p2(static_cast<size_t>(m2) + 1, -1);
+        int n2 = -1;
+        CHECK(hhp_reorder_color(m2, r2.data(), c2.data(), p2.data(), &n2) == HHP_OK);
+        std::vector<int> seen(static_cast<size_t>(m2), 0);
+        for (int i = 0; i < m2; ++i)
+            if (p2[static_cast<size_t>(i)] >= 0 && p2[static_cast<size_t>(i)] < m2) ++seen[static_cast<size_t>(p2[static_cast<size_t>(i)])];
+        for (int i = 0; i < m2; ++i) CHECK(seen[static_cast<size_t>(i)] == 1);
+        CHECK(m2 == 0 ? n2 == 0 : n2 >= 1);
+    }
+    const int brp[3] = {0, 1, 2}, bcol[2] = {0, 5};
+    int bperm[2], bn = 0;
+    CHECK(hhp_reorder_color(2, brp, bcol, bperm, &bn) == HHP_ERR_ARG);
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
@@ -302,7 +387,9 @@ int main(int argc, char **argv) {
     large_matrix_market();
     vector_files();
     work_plan();
+    uniform();
     rcm();
+    color();
     if (g_fail) {
         std::fprintf(stderr, "%d checks failed\n", g_fail);
         return 1;

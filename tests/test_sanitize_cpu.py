@@ -1,5 +1,5 @@
-"""The library's host-only sources (Matrix Market / binary CSR reader, vector files, SpMV work plan,
-reverse Cuthill-McKee) built with sanitizers and driven by tests/sanitize_host.cpp: AddressSanitizer
+"""The library's host-only sources (Matrix Market / binary CSR reader, vector files, SpMV work plan
+and its uniform-diagonal check, reverse Cuthill-McKee, multicolour order) built with sanitizers and driven by tests/sanitize_host.cpp: AddressSanitizer
 with UndefinedBehaviorSanitizer and leak checking, then ThreadSanitizer for the reader's parallel
 parse. Any sanitizer report or failed check fails the test. No GPU is involved."""
 import os
