@@ -79,11 +79,11 @@ struct Solver {
     cudaStream_t s2 = nullptr, s3 = nullptr;  // capture streams: loop body, IF body
     cudaEvent_t ev_in = nullptr;              // joins the two input uploads
     cudaGraphExec_t g64 = nullptr, g64m = nullptr, gmix = nullptr, gmixm = nullptr;  // classic / merged
-    // ILU(0)-preconditioned FP64 loop: p^ and s^, and its graph with the factorization generation
-    // it was captured against (a refactorization reallocates the factors)
+    // ILU(0)-preconditioned FP64 loop: p^ and s^, and its graphs (classic, merged) with the
+    // factorization generation each was captured against (a refactorization reallocates the factors)
     double *PH = nullptr, *SH = nullptr;
-    cudaGraphExec_t g64i = nullptr;
-    long long g64i_gen = 0;
+    cudaGraphExec_t g64i = nullptr, g64im = nullptr;
+    long long g64i_gen = 0, g64im_gen = 0;
     int g64_kernels_pro = 0, g64_kernels_epi = 0, gmix_kernels_pro = 0, gmix_kernels_epi = 0, unroll = 4;
 };
 
@@ -255,6 +255,7 @@ __device__ __forceinline__ int step_p(int status, int iter, int it0, int maxit, 
 // 4 units under the 128-register limit of 512-thread blocks).
 constexpr int kPre = 4;
 constexpr int kPreX = 3;
+constexpr int kPreXPC = 2;  // K_XRP with right preconditioning: seven operand streams
 
 // Scalar work (divisions, tests) is done once per block by thread 0 and broadcast through shared
 // memory: on GB300 an FP64 division is a sequence of FP64 instructions on the slowest pipe, so
@@ -609,12 +610,13 @@ constexpr double kCancel = 64.0 * 2.220446049250313e-16;
 
 // K_XRP: omega, x += alpha p + omega s, r = s - omega t, the stop tests of the finished iteration,
 // beta = (rho_new / rho)(alpha / omega) and p = r + beta (p - omega v). Half step (||s|| below the
-// threshold): x += alpha p, r = s, stop.
-template <typename T>
+// threshold): x += alpha p, r = s, stop. PC (right preconditioning): x takes PX = M^-1 p and
+// SX = M^-1 s instead of p and s (two more operand streams, so fewer units are prefetched).
+template <typename T, bool PC = false>
 __global__ void __launch_bounds__(512) k_xrp(DevScal *sc, T *X, T *R, T *P, const T *S, const T *Tv, const T *V,
                                              int nu, SpmvParts sp, const double *part_s, int nparts, double *hist,
                                              int hist_cap, cudaGraphConditionalHandle cond, int first_in_body,
-                                             const int *dev_err, int use_cond) {
+                                             const int *dev_err, int use_cond, const T *PX, const T *SX) {
     const bool dead = dead_step(sc);  // tested after the operand and record loads are in flight
     // scalars written by earlier launches, read with the operand loads (off the critical path)
     const double thr2 = sc->thr2_rec, alpha = sc->alpha, rho_prev = sc->rho_prev;
@@ -623,10 +625,11 @@ __global__ void __launch_bounds__(512) k_xrp(DevScal *sc, T *X, T *R, T *P, cons
     __shared__ double bc[3];
     __shared__ int go;  // 0: nothing to do, 1: full step and p, 2: half step, 3: full step, last
     constexpr int E = Unit<T>::E;
+    constexpr int KX = PC ? kPreXPC : kPreX;
     const int stride = gridDim.x * blockDim.x, u0 = blockIdx.x * blockDim.x + threadIdx.x;
-    T x[kPreX][E], p[kPreX][E], s[kPreX][E], t[kPreX][E], vv[kPreX][E];
+    T x[KX][E], p[KX][E], s[KX][E], t[KX][E], vv[KX][E], px[PC ? KX : 1][E], sx[PC ? KX : 1][E];
 #pragma unroll
-    for (int k = 0; k < kPreX; ++k) {
+    for (int k = 0; k < KX; ++k) {
         const int u = u0 + k * stride;
         if (u < nu) {
             ldu(x[k], X, u);
@@ -634,6 +637,10 @@ __global__ void __launch_bounds__(512) k_xrp(DevScal *sc, T *X, T *R, T *P, cons
             ldu(s[k], S, u);
             ldu(t[k], Tv, u);
             ldu(vv[k], V, u);
+            if constexpr (PC) {
+                ldu(px[k], PX, u);
+                ldu(sx[k], SX, u);
+            }
         }
     }
     double q[8];  // t.s, t.t, r0.t (4-wide SpMV records), s.s, r0.s (4-wide K_S records)
@@ -709,18 +716,19 @@ __global__ void __launch_bounds__(512) k_xrp(DevScal *sc, T *X, T *R, T *P, cons
     if (mode == 0) return;
     const T ta = static_cast<T>(bc[0]), tw = static_cast<T>(bc[1]), tnw = static_cast<T>(-bc[1]),
             tb = static_cast<T>(bc[2]);
-    auto unit = [&](int u, T(&xx)[E], T(&pp)[E], const T(&ss)[E], const T(&tt)[E], const T(&vx)[E]) {
+    auto unit = [&](int u, T(&xx)[E], T(&pp)[E], const T(&ss)[E], const T(&tt)[E], const T(&vx)[E],
+                    const T(&pxx)[E], const T(&sxx)[E]) {
         T r[E];
         if (mode == 2) {
 #pragma unroll
             for (int e = 0; e < E; ++e) {
-                xx[e] = tfma(ta, pp[e], xx[e]);
+                xx[e] = tfma(ta, PC ? pxx[e] : pp[e], xx[e]);
                 r[e] = ss[e];
             }
         } else {
 #pragma unroll
             for (int e = 0; e < E; ++e) {
-                xx[e] = tfma(tw, ss[e], tfma(ta, pp[e], xx[e]));
+                xx[e] = tfma(tw, PC ? sxx[e] : ss[e], tfma(ta, PC ? pxx[e] : pp[e], xx[e]));
                 r[e] = tfma(tnw, tt[e], ss[e]);
             }
             if (mode == 1) {
@@ -733,32 +741,41 @@ __global__ void __launch_bounds__(512) k_xrp(DevScal *sc, T *X, T *R, T *P, cons
         stu(R, u, r);
     };
 #pragma unroll
-    for (int k = 0; k < kPreX; ++k) {
+    for (int k = 0; k < KX; ++k) {
         const int u = u0 + k * stride;
-        if (u < nu) unit(u, x[k], p[k], s[k], t[k], vv[k]);
+        if (u < nu) unit(u, x[k], p[k], s[k], t[k], vv[k], px[PC ? k : 0], sx[PC ? k : 0]);
     }
-    // whole batches of kPreX units, then the last few one at a time (see K_P)
-    int ub = u0 + kPreX * stride;
-    for (; ub + (kPreX - 1) * stride < nu; ub += kPreX * stride) {
+    // whole batches of KX units, then the last few one at a time (see K_P)
+    int ub = u0 + KX * stride;
+    for (; ub + (KX - 1) * stride < nu; ub += KX * stride) {
 #pragma unroll
-        for (int k = 0; k < kPreX; ++k) {
+        for (int k = 0; k < KX; ++k) {
             ldu(x[k], X, ub + k * stride);
             ldu(p[k], P, ub + k * stride);
             ldu(s[k], S, ub + k * stride);
             ldu(t[k], Tv, ub + k * stride);
             ldu(vv[k], V, ub + k * stride);
+            if constexpr (PC) {
+                ldu(px[k], PX, ub + k * stride);
+                ldu(sx[k], SX, ub + k * stride);
+            }
         }
 #pragma unroll
-        for (int k = 0; k < kPreX; ++k) unit(ub + k * stride, x[k], p[k], s[k], t[k], vv[k]);
+        for (int k = 0; k < KX; ++k)
+            unit(ub + k * stride, x[k], p[k], s[k], t[k], vv[k], px[PC ? k : 0], sx[PC ? k : 0]);
     }
     for (int u = ub; u < nu; u += stride) {
-        T xx[E], pp[E], ss[E], tt[E], vx[E];
+        T xx[E], pp[E], ss[E], tt[E], vx[E], pxx[E], sxx[E];
         ldu(xx, X, u);
         ldu(pp, P, u);
         ldu(ss, S, u);
         ldu(tt, Tv, u);
         ldu(vx, V, u);
-        unit(u, xx, pp, ss, tt, vx);
+        if constexpr (PC) {
+            ldu(pxx, PX, u);
+            ldu(sxx, SX, u);
+        }
+        unit(u, xx, pp, ss, tt, vx, pxx, sxx);
     }
 }
 
@@ -1262,7 +1279,8 @@ hhp_status ensure_solver(hhp_mat *A, Solver **out, int maxit) {
         if (s->gmix) cudaGraphExecDestroy(s->gmix);
         if (s->gmixm) cudaGraphExecDestroy(s->gmixm);
         if (s->g64i) cudaGraphExecDestroy(s->g64i);
-        s->g64 = s->g64m = s->gmix = s->gmixm = s->g64i = nullptr;
+        if (s->g64im) cudaGraphExecDestroy(s->g64im);
+        s->g64 = s->g64m = s->gmix = s->gmixm = s->g64i = s->g64im = nullptr;
     }
     *out = s;
     return HHP_OK;
@@ -1401,18 +1419,31 @@ hhp_status capture_loop(Solver *s, cudaStream_t stream, DevScal *sc, T *X, T *R,
     for (int k = 0; k < s->unroll && st == HHP_OK; ++k) {
         if constexpr (std::is_same<T, double>::value) {
             if (merged) {
-                st = launch_spmv64(A, s->s2, EP_DOT1, P, V, R0, 1.0, 0.0, nullptr, nullptr, stop);
+                // ILU(0): the SpMVs read p^ = M^-1 p and s^ = M^-1 s, and K_XRP adds alpha p^ +
+                // omega s^ to x; the dot products and the r and p updates are those of p and s
+                const double *pv = P, *sv = S;
+                if (ilu) {
+                    st = launch_ilu_apply(A, s->s2, P, s->PH, stop);
+                    if (st != HHP_OK) break;
+                    pv = s->PH;
+                }
+                st = launch_spmv64(A, s->s2, EP_DOT1, pv, V, R0, 1.0, 0.0, nullptr, nullptr, stop);
                 if (st != HHP_OK) break;
                 if (launch_k(k_s<double, true>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, sc, S, R, V, R0, nu,
                              parts_of(pl), part_s) != cudaSuccess) {
                     st = HHP_ERR_CUDA;
                     break;
                 }
-                st = launch_spmv64(A, s->s2, EP_DOT3, S, Tv, S, 1.0, 0.0, nullptr, R0, stop);
+                if (ilu) {
+                    st = launch_ilu_apply(A, s->s2, S, s->SH, stop);
+                    if (st != HHP_OK) break;
+                    sv = s->SH;
+                }
+                st = launch_spmv64(A, s->s2, EP_DOT3, sv, Tv, S, 1.0, 0.0, nullptr, R0, stop);
                 if (st != HHP_OK) break;
-                if (launch_k(k_xrp<double>, dim3(s->nblk), dim3(s->nthr), 0, s->s2, sc, X, R, P, S, Tv, V, nu,
-                             parts_of(pl), part_s, s->nblk, s->hist, s->hist_cap, cond, k == 0 ? 1 : 0,
-                             A->ctx->dev_err, 1) != cudaSuccess)
+                if (launch_k(ilu ? k_xrp<double, true> : k_xrp<double, false>, dim3(s->nblk), dim3(s->nthr), 0,
+                             s->s2, sc, X, R, P, S, Tv, V, nu, parts_of(pl), part_s, s->nblk, s->hist,
+                             s->hist_cap, cond, k == 0 ? 1 : 0, A->ctx->dev_err, 1, pv, sv) != cudaSuccess)
                     st = HHP_ERR_CUDA;
                 continue;
             }
@@ -1567,13 +1598,23 @@ hhp_status run_direct64(Solver *s, bool merged, bool ilu) {
     for (;;) {
         for (int k = 0; k < s->unroll; ++k) {
             if (merged) {
-                HHP_TRY(launch_spmv64(A, st, EP_DOT1, s->P, s->V, s->R0, 1.0, 0.0, nullptr, nullptr, stop));
+                const double *pv = s->P, *sv = s->S;
+                if (ilu) {
+                    HHP_TRY(launch_ilu_apply(A, st, s->P, s->PH, stop));
+                    pv = s->PH;
+                }
+                HHP_TRY(launch_spmv64(A, st, EP_DOT1, pv, s->V, s->R0, 1.0, 0.0, nullptr, nullptr, stop));
                 HHP_CUDA(launch_k(k_s<double, true>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->S, s->R, s->V,
                                   s->R0, nu, parts_of(pl), s->part_s));
-                HHP_TRY(launch_spmv64(A, st, EP_DOT3, s->S, s->T, s->S, 1.0, 0.0, nullptr, s->R0, stop));
-                HHP_CUDA(launch_k(k_xrp<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->X, s->R, s->P, s->S,
-                                  s->T, s->V, nu, parts_of(pl), s->part_s, s->nblk, s->hist, s->hist_cap,
-                                  cudaGraphConditionalHandle(), k == 0 ? 1 : 0, A->ctx->dev_err, 0));
+                if (ilu) {
+                    HHP_TRY(launch_ilu_apply(A, st, s->S, s->SH, stop));
+                    sv = s->SH;
+                }
+                HHP_TRY(launch_spmv64(A, st, EP_DOT3, sv, s->T, s->S, 1.0, 0.0, nullptr, s->R0, stop));
+                HHP_CUDA(launch_k(ilu ? k_xrp<double, true> : k_xrp<double, false>, dim3(s->nblk), dim3(s->nthr), 0,
+                                  st, s->sc, s->X, s->R, s->P, s->S, s->T, s->V, nu, parts_of(pl), s->part_s, s->nblk,
+                                  s->hist, s->hist_cap, cudaGraphConditionalHandle(), k == 0 ? 1 : 0,
+                                  A->ctx->dev_err, 0, pv, sv));
                 A->ctx->kernel_launches += 2;
                 continue;
             }
@@ -1632,7 +1673,7 @@ hhp_status build_g64(Solver *s, bool merged, bool ilu = false) {
         HHP_CUDA(launch_k(k_init<double>, dim3(s->nblk), dim3(s->nthr), 0, st, s->sc, s->R, s->B, s->R0, s->P, s->V,
                           nu, parts_of(A->plan64), s->x0_nz, s->part_b, s->nblk, s->part_xr, s->part_s));
         rc = capture_loop<double>(s, st, s->sc, s->X, s->R, s->R0, s->P, s->V, s->S, s->T, s->part_xr, s->part_s,
-                                  false, merged && !ilu, ilu);
+                                  false, merged, ilu);
         if (rc != HHP_OK) break;
         rc = launch_spmv64(A, st, EP_RESID, s->X, s->Y, s->B, 1.0, 0.0);
         if (rc != HHP_OK) break;
@@ -1645,7 +1686,7 @@ hhp_status build_g64(Solver *s, bool merged, bool ilu = false) {
         return rc;
     }
     HHP_CUDA(e);
-    cudaGraphExec_t &ge = ilu ? s->g64i : merged ? s->g64m : s->g64;
+    cudaGraphExec_t &ge = ilu ? (merged ? s->g64im : s->g64i) : merged ? s->g64m : s->g64;
     cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
     cudaGraphDestroy(g);
     HHP_CUDA(ie);
@@ -1654,7 +1695,7 @@ hhp_status build_g64(Solver *s, bool merged, bool ilu = false) {
     // launch_spmv64 / launch_ilu_apply counted their captured launches; graph launches are counted
     // when executed.
     A->ctx->kernel_launches -= 2 + (ilu ? 6 : 2) * s->unroll;
-    if (ilu) s->g64i_gen = ilu_generation(A);
+    if (ilu) (merged ? s->g64im_gen : s->g64i_gen) = ilu_generation(A);
     return HHP_OK;
 }
 
@@ -1845,6 +1886,10 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
             cudaGraphExecDestroy(s->g64i);
             s->g64i = nullptr;
         }
+        if (s->g64im && s->g64im_gen != ilu_generation(A)) {
+            cudaGraphExecDestroy(s->g64im);
+            s->g64im = nullptr;
+        }
     }
     if (mixed) HHP_TRY(ensure_fp32_inner(A, s));
     HHP_CUDA(cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), st));
@@ -1891,11 +1936,11 @@ hhp_status solve_any(hhp_mat *A, const double *b_in, double *x_io, const double 
         // the merged loop unless the caller asked for the classic one or for the reference's
         // fixed-iteration runs (which follow its dot products exactly); an adjoint solve has
         // resolved AUTO to CLASSIC before it gets here
-        // (ILU(0) runs the classic schedule with its two applications, 4 more kernels)
-        const bool merged = o->loop != HHP_LOOP_CLASSIC && !h.fixed && !ilu;
-        cudaGraphExec_t &ge = ilu ? s->g64i : merged ? s->g64m : s->g64;
+        // (ILU(0) adds its two applications, 4 kernels, to either schedule)
+        const bool merged = o->loop != HHP_LOOP_CLASSIC && !h.fixed;
+        cudaGraphExec_t &ge = ilu ? (merged ? s->g64im : s->g64i) : merged ? s->g64m : s->g64;
         if (use_graph && !ge) HHP_TRY(build_g64(s, merged, ilu));
-        const long long per_iter = ilu ? 9 : merged ? 4 : 5;
+        const long long per_iter = (merged ? 4 : 5) + (ilu ? 4 : 0);
         h.maxit = o->maxit - it_before;
         int dev_status = ST_RUNNING;
         double prev_true = INFINITY;
@@ -2043,6 +2088,7 @@ void solver_release(Solver *s) {
     if (s->gmix) cudaGraphExecDestroy(s->gmix);
     if (s->gmixm) cudaGraphExecDestroy(s->gmixm);
     if (s->g64i) cudaGraphExecDestroy(s->g64i);
+    if (s->g64im) cudaGraphExecDestroy(s->g64im);
     double *d[] = {s->X, s->B, s->R, s->R0, s->P, s->V, s->S, s->T, s->Y, s->part_xr, s->part_s, s->part_xr32,
                    s->part_s32, s->part_b, s->hist, s->PH, s->SH};
     cudaFree(s->x0_nz);

@@ -62,7 +62,7 @@ typedef enum { HHP_PREC_FP64 = 0, HHP_PREC_MIXED = 1 } hhp_precision;
  * application is two triangular solves walking the dependency levels of L and U, so its cost
  * grows with their number: reorder a stencil-like matrix with hhp_reorder_color first (two levels
  * for the 5- and 7-point stencils) -- the natural order of an N x N grid has 2N - 1. FP64 only
- * (HHP_ERR_ARG with the mixed form); the classic loop. Rows may store their entries in any
+ * (HHP_ERR_ARG with the mixed form); either loop schedule. Rows may store their entries in any
  * column order (each is factored and solved in ascending column order); every diagonal must be
  * stored and no column twice in a row (HHP_ERR_ARG), and the pivots u_ii must be nonzero
  * (HHP_ERR_BREAKDOWN). */
@@ -79,9 +79,10 @@ typedef enum {
  * (src/entry/bicgstab_gpu_dp.c:165-196): rho_new = r.r0 and ||r|| as direct dot products of the
  * new residual. AUTO (0, the default): MERGED for hhp_bicgstab*, CLASSIC for the adjoint solve of
  * hhp_bicgstab_backward* (whose tolerances sit near the rounding floor, where the direct dot
- * products reach a lower true residual). Fixed-iteration runs and ILU(0)-preconditioned solves
- * always use CLASSIC; the FP32 inner loop of the mixed form follows the same choice (MERGED: its
- * kernel with the x and r updates also takes the reliable-update test). */
+ * products reach a lower true residual). Fixed-iteration runs always use CLASSIC. ILU(0) adds its
+ * two applications to either schedule (MERGED: 8 kernels per iteration, CLASSIC: 9). The FP32
+ * inner loop of the mixed form follows the same choice (MERGED: its kernel with the x and r
+ * updates also takes the reliable-update test). */
 typedef enum { HHP_LOOP_AUTO = 0, HHP_LOOP_MERGED = 1, HHP_LOOP_CLASSIC = 2 } hhp_loop;
 
 typedef struct {

@@ -137,6 +137,27 @@ def test_host_device_and_direct_launch_agree(ctx):
     A.close()
 
 
+@pytest.mark.parametrize("loop", ["merged", "classic"])
+def test_both_schedules(ctx, loop):
+    # the merged loop (the default: 8 kernels per iteration, K_XRP adding alpha p^ + omega s^ to x)
+    # and the classic one (9: K_XR, then K_P) reach the tolerance within 5 % of the oracle's
+    # preconditioned loop, graph and direct launches bit for bit alike
+    perm, (rp0, col0, val0), (rp, col, val, _), b, xt = _system("stencil3d16", True)
+    k_ref, _, _ = orc.ilu0_iters_to_tol(rp, col, val, b, np.zeros(b.size), 1e-10, 2000)
+    A = Matrix.from_csr(ctx, rp0, col0, val0, perm=perm)
+    x, res = bicgstab(ctx, A, b, rtol=1e-10, maxit=2000, precond="ilu0", loop=loop)
+    r = b - orc.spmv(rp, col, val, x)
+    assert res.status == 0 and np.sqrt(orc.dot(r, r) / orc.dot(b, b)) <= 1.0000001e-10
+    assert abs(res.iters - k_ref) <= max(1, 0.05 * k_ref), (res.iters, k_ref)
+    os.environ["HHP_SOLVE_GRAPH"] = "0"
+    try:
+        xd, rd = bicgstab(ctx, A, b, rtol=1e-10, maxit=2000, precond="ilu0", loop=loop)
+    finally:
+        del os.environ["HHP_SOLVE_GRAPH"]
+    assert rd.iters == res.iters and np.array_equal(xd, x)
+    A.close()
+
+
 def test_fixed_iterations_and_history(ctx):
     s = synth.convdiff2d(32, 20.0)
     A = Matrix.from_csr(ctx, s.rowptr, s.col, s.val)
