@@ -930,7 +930,8 @@ def run_config_solve(args):
     """One configuration's solve, timed alone (profiler target and per-config check): --steps solves
     of --config in FP64 (--precision fp64) or the mixed form (--precision fp32), rtol 1e-10 (C5:
     1e-12; C3: --iters fixed iterations, as it does not converge unpreconditioned). --precond ilu0:
-    the ILU(0)-preconditioned solve of the multicolour-ordered system, --iters fixed iterations.
+    the ILU(0)-preconditioned solve of the multicolour-ordered system, --iters fixed iterations
+    (classic schedule), or with --iters 0 to 1e-10 on the default schedule.
     Prints one JSON line with the median CUDA-event time, L2 flushed before each solve."""
     import torch
     from hethyppar_gb300 import Context, Matrix, bicgstab, reorder_color, synth
@@ -951,8 +952,10 @@ def run_config_solve(args):
     x = torch.zeros(s.n, dtype=torch.float64, device="cuda")
     kw = {"rtol": 1e-12 if args.config == "c5" else RTOL, "maxit": 50000,
           "precision": "mixed" if args.precision == "fp32" else "fp64"}
-    if args.config == "c3" or args.precond == "ilu0":
+    if args.config == "c3" or (args.precond == "ilu0" and args.iters > 0):
         kw = {"rtol": 0.0, "maxit": args.iters, "fixed_iters": True}
+    elif args.precond == "ilu0":  # --iters 0: to 1e-10 on the default (merged) schedule
+        kw = {"rtol": RTOL, "maxit": 50000}
     if args.precond == "ilu0":
         kw["precond"] = "ilu0"
     res = []
@@ -982,7 +985,7 @@ def main():
     ap.add_argument("--mode", default="solve", choices=["solve", "spmv", "solve-config"],
                     help="spmv: time the SpMV kernel alone on --config (kernel sweeps, profiler target); "
                          "solve-config: time the solve of --config alone")
-    ap.add_argument("--iters", type=int, default=200, help="solve-config on c3: fixed iterations")
+    ap.add_argument("--iters", type=int, default=200, help="solve-config on c3, and with --precond ilu0: fixed iterations (0 with ilu0: to 1e-10)")
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--precond", default="none", choices=["none", "ilu0"],
