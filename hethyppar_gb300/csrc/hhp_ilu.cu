@@ -50,6 +50,7 @@ constexpr unsigned kBarrierSpins = 1u << 22;  // bounded wait (x ~64 ns sleeps: 
 struct IluTri {
     int n_levels = 0, n_slices = 0, n_long = 0, n_big = 0;
     int head_slice = 0, head_long = 0, head_big = 0;  // lev_*[min(2, n_levels)], kept on the host
+    int lev1_slice = 0;                               // lev_slice[1]: the first level-1 slice
     long long slots = 0;
     int *lev_slice = nullptr;        // n_levels + 1: the slices of each level
     int *lev_long = nullptr;         // n_levels + 1: the long rows of each level
@@ -86,6 +87,10 @@ struct IluDev {
     int *frow = nullptr;      // m: rows grouped by L level (the factorization's schedule)
     int *flev = nullptr;      // levels_L + 1
     IluTri L, U;
+    // Two colours: every row is on level 1 of exactly one triangle (L's level-1 rows are U's
+    // level-0 rows and the other way round). An application is then two passes over half the
+    // rows each (see launch_ilu_apply).
+    bool two_colour = false;
     unsigned *bar = nullptr;  // barrier counters: forward, backward, factorization
     int *bad = nullptr;       // first row with a zero or non-finite pivot (INT_MAX: none)
     // A row whose columns are not ascending (a matrix reordered by csr_permute keeps its rows'
@@ -101,6 +106,9 @@ namespace {
 struct TriArgs {
     int n_levels;
     int head_slice, head_long, head_big;  // ends of the first pass's ranges (levels 0 and 1)
+    int first_slice;  // where the first pass's slices start (lev1_slice: level-0 rows skipped)
+    int scale;        // forward solve of two colours: out = (in - sum) * (1 / u_ii)
+    int dep_out;      // backward solve of two colours: level-1 dependencies read from out
     const int *lev_slice, *lev_long, *lev_big;
     const long long *slice_ptr;
     const int *slice_row, *slice_len, *scol;
@@ -109,7 +117,7 @@ struct TriArgs {
 };
 
 TriArgs args_of(const IluTri &t) {
-    return TriArgs{t.n_levels, t.head_slice, t.head_long, t.head_big, t.lev_slice, t.lev_long, t.lev_big,
+    return TriArgs{t.n_levels, t.head_slice, t.head_long, t.head_big, 0, 0, 0, t.lev_slice, t.lev_long, t.lev_big,
                    t.slice_ptr, t.slice_row, t.slice_len, t.scol, t.sval, t.long_row, t.big_row};
 }
 
@@ -267,7 +275,7 @@ __global__ void __launch_bounds__(kIluThreads, 1) k_ilu_tri(TriArgs t, const int
     const int W = static_cast<int>((gridDim.x * blockDim.x) >> 5);
     // The first pass's bounds are arguments, so this warp's first slices' row data is pulled into
     // L1 while the two status words (written by earlier launches) are read together.
-    for (int s = gw; s < t.head_slice && s < gw + 2 * W; s += W) {
+    for (int s = t.first_slice + gw; s < t.head_slice && s < t.first_slice + gw + 2 * W; s += W) {
         asm volatile("prefetch.global.L1 [%0];" ::"l"(t.slice_row + 32LL * s + lane));
         asm volatile("prefetch.global.L1 [%0];" ::"l"(t.slice_len + 32LL * s + lane));
         asm volatile("prefetch.global.L1 [%0];" ::"l"(t.slice_ptr + s));
@@ -281,7 +289,8 @@ __global__ void __launch_bounds__(kIluThreads, 1) k_ilu_tri(TriArgs t, const int
         // called for them): a warp's slices of both levels are in flight together
         const bool head = lev == 0;
         const int le = head && t.n_levels > 1 ? 2 : lev + 1;
-        const Dep<UPPER> z{in, dinv, out, le == 2};
+        const Dep<UPPER> z{in, dinv, out, le == 2 && !t.dep_out};
+        const bool scale = UPPER || t.scale;
         const int big_lo = head ? 0 : t.lev_big[lev], big_hi = head ? t.head_big : t.lev_big[le];
         for (int q = big_lo + blockIdx.x; q < big_hi; q += gridDim.x) {
             const int row = t.big_row[q];
@@ -294,7 +303,7 @@ __global__ void __launch_bounds__(kIluThreads, 1) k_ilu_tri(TriArgs t, const int
                 double tot = 0.0;
                 for (int w = 0; w < kIluThreads / 32; ++w) tot += wsum[w];
                 double r = in[row] - tot;
-                if (UPPER) r = r * dinv[row];
+                if (scale) r = r * dinv[row];
                 __stcg(out + row, r);
             }
             __syncthreads();
@@ -307,7 +316,7 @@ __global__ void __launch_bounds__(kIluThreads, 1) k_ilu_tri(TriArgs t, const int
             const double acc = warp_sum(strided_dot(lu, col, z, b + lane, e, 32));
             if (lane == 0) {
                 double r = in[row] - acc;
-                if (UPPER) r = r * dinv[row];
+                if (scale) r = r * dinv[row];
                 __stcg(out + row, r);
             }
         }
@@ -316,7 +325,7 @@ __global__ void __launch_bounds__(kIluThreads, 1) k_ilu_tri(TriArgs t, const int
         // slots, then gathers) in flight at once. A step past a lane's row length loads nothing
         // and adds fma(-0, 0, acc), which leaves acc unchanged bit for bit.
         const int s_hi = head ? t.head_slice : t.lev_slice[le];
-        for (int s = (head ? 0 : t.lev_slice[lev]) + gw; s < s_hi; s += 2 * W) {
+        for (int s = (head ? t.first_slice : t.lev_slice[lev]) + gw; s < s_hi; s += 2 * W) {
             const int sb = s + W;
             const bool two = sb < s_hi;
             const int r0 = t.slice_row[32 * s + lane];
@@ -348,8 +357,8 @@ __global__ void __launch_bounds__(kIluThreads, 1) k_ilu_tri(TriArgs t, const int
 #pragma unroll
                 for (int j = 0; j < 4; ++j) a1 = fma(-v[4 + j], zz[4 + j], a1);
             }
-            if (r0 >= 0) __stcg(out + r0, UPPER ? a0 * dinv[r0] : a0);
-            if (r1 >= 0) __stcg(out + r1, UPPER ? a1 * dinv[r1] : a1);
+            if (r0 >= 0) __stcg(out + r0, scale ? a0 * dinv[r0] : a0);
+            if (r1 >= 0) __stcg(out + r1, scale ? a1 * dinv[r1] : a1);
         }
         lev = le - 1;
         if (lev >= 1 && lev + 1 < t.n_levels && !grid_barrier(bar, ++barriers, dev_err)) return;
@@ -452,6 +461,7 @@ hhp_status upload_tri(const TriHost &h, IluTri &d, int **sidx_dev, cudaStream_t 
     d.head_slice = h.lev_slice[head];
     d.head_long = h.lev_long[head];
     d.head_big = h.lev_big[head];
+    d.lev1_slice = h.n_levels >= 2 ? h.lev_slice[1] : 0;
     HHP_TRY(upload(&d.lev_slice, h.lev_slice, st));
     HHP_TRY(upload(&d.lev_long, h.lev_long, st));
     HHP_TRY(upload(&d.slice_ptr, h.slice_ptr, st));
@@ -545,6 +555,9 @@ hhp_status build_ilu(hhp_mat *A, IluDev *I, int *levels_out) {
         levels_out[0] = nL;
         levels_out[1] = nU;
     }
+    I->two_colour = nL == 2 && nU == 2;
+    for (int i = 0; i < m && I->two_colour; ++i)
+        I->two_colour = levL[static_cast<size_t>(i)] + levU[static_cast<size_t>(i)] == 1;
     TriHost TL, TU;
     const int *cp = col.data();
     layout_triangle(
@@ -742,6 +755,32 @@ hhp_status launch_ilu_apply(hhp_mat *A, cudaStream_t st, const double *in, doubl
     const int *rp = A->rowptr, *col = I->col ? I->col : A->col, *dpos = I->dpos;
     const double *lu = I->lu, *dinv = I->dinv;
     int *err = A->ctx->dev_err;
+    if (I->two_colour) {
+        // L's level-1 rows are U's level-0 rows: their final value is (r_i - sum l_ik r_k) / u_ii,
+        // which the forward pass writes straight to out. U's level-1 rows are L's level-0 rows,
+        // whose y is r itself: the backward pass reads r and the forward pass's results. Each
+        // pass walks half the rows, y is not used, and every value is the one the two full
+        // solves give, bit for bit (same sums, same order, the same multiplication by 1 / u_ii).
+        unsigned *b = I->bar, *bo = I->bar + 1;
+        const double *x = in;
+        double *y = out;
+        {
+            TriArgs t = args_of(I->L);
+            t.first_slice = I->L.lev1_slice;
+            t.scale = 1;
+            void *args[] = {&t, &rp, &col, &dpos, &lu, &dinv, &x, &y, &b, &bo, &stop, &err};
+            HHP_CUDA(launch_coop(reinterpret_cast<const void *>(k_ilu_tri<false>), I->grid, args, st, false));
+        }
+        {
+            TriArgs t = args_of(I->U);
+            t.first_slice = I->U.lev1_slice;
+            t.dep_out = 1;
+            void *args[] = {&t, &rp, &col, &dpos, &lu, &dinv, &x, &y, &bo, &b, &stop, &err};
+            HHP_CUDA(launch_coop(reinterpret_cast<const void *>(k_ilu_tri<true>), I->grid, args, st, false));
+        }
+        A->ctx->kernel_launches += 2;
+        return HHP_OK;
+    }
     {  // y = L^-1 in
         TriArgs t = args_of(I->L);
         unsigned *b = I->bar, *bo = I->bar + 1;
